@@ -1,0 +1,762 @@
+// extern "C" surface of libcpm_gpu.so (declared in include/cpm_gpu.h).
+//
+// The builder restates crates/cpm-py/src/builder.rs:35-525 in C++: string
+// parsing with the reference's messages, field-by-field accumulation of the
+// user configuration, resolve at run time (config.rs:200-257) and the
+// theta helpers. Results wrap cpmhost::Result (convert.rs:27-256).
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/cpm_gpu.h"
+#include "cpm_engine.h"
+#include "cpm_host.h"
+#include "cpm_kernels.h"
+
+using namespace cpmhost;
+
+static thread_local std::string g_err;
+
+static int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+static int ok() { return CPM_OK; }
+
+extern "C" const char* cpm_last_error(void) { return g_err.c_str(); }
+extern "C" const char* cpm_version(void) { return "0.2.0+gb300"; }
+
+// Rust's `{:?}` of a &str.
+static std::string dbg(const char* s) {
+    std::string o = "\"";
+    for (const unsigned char* p = (const unsigned char*)s; *p; ++p) {
+        const unsigned char c = *p;
+        if (c == '"') o += "\\\"";
+        else if (c == '\\') o += "\\\\";
+        else if (c == '\n') o += "\\n";
+        else if (c == '\r') o += "\\r";
+        else if (c == '\t') o += "\\t";
+        else if (c < 0x20 || c == 0x7f) { char b[16]; std::snprintf(b, sizeof b, "\\u{%x}", c); o += b; }
+        else o += (char)c;
+    }
+    return o + "\"";
+}
+
+struct cpm_builder {
+    Config cfg;  // grid, boundary, seed and neighbourhoods are set at construction
+    bool energy_set = false;
+    bool adhesion_set = false;
+    bool init_set = false;
+    std::map<std::string, size_t> type_index;
+};
+
+struct cpm_result {
+    Result r;
+};
+
+// builder.rs:35-96
+static int parse_boundary(const char* s, bool& periodic) {
+    if (!std::strcmp(s, "fixed")) { periodic = false; return 0; }
+    if (!std::strcmp(s, "periodic")) { periodic = true; return 0; }
+    return fail(CPM_E_CONFIG, "unknown boundary " + dbg(s) + "; expected \"fixed\" or \"periodic\"");
+}
+static int parse_nbh(const char* s, int& k) {
+    static const char* names[] = {"von_neumann", "moore", "eighteen", "twenty_six", "twenty_six_weighted"};
+    for (int i = 0; i < 5; ++i)
+        if (!std::strcmp(s, names[i])) { k = i; return 0; }
+    return fail(CPM_E_CONFIG, "unknown neighbourhood " + dbg(s) +
+                                  "; expected one of \"von_neumann\", \"moore\", \"eighteen\", \"twenty_six\", "
+                                  "\"twenty_six_weighted\"");
+}
+
+extern "C" int cpm_builder_new(const uint64_t* grid, size_t grid_len, const char* boundary, uint64_t seed,
+                               const char* copy_neighborhood, const char* energy_neighborhood,
+                               const char* connectivity_neighborhood, const char* acceptance, const char* proposal,
+                               const char* const* keys, const int32_t* values, size_t n_keys, cpm_builder** out) {
+    if (!out || !boundary || !copy_neighborhood || !connectivity_neighborhood || (grid_len && !grid))
+        return fail(CPM_E_ARG, "null argument");
+    auto b = std::make_unique<cpm_builder>();
+    int e;
+    if ((e = parse_boundary(boundary, b->cfg.periodic))) return e;
+    if ((e = parse_nbh(copy_neighborhood, b->cfg.copy_nbh))) return e;
+    if (energy_neighborhood) {
+        if ((e = parse_nbh(energy_neighborhood, b->cfg.energy_nbh))) return e;
+        b->energy_set = true;
+    }
+    if ((e = parse_nbh(connectivity_neighborhood, b->cfg.conn_nbh))) return e;
+    if (acceptance) {
+        if (!std::strcmp(acceptance, "metropolis")) b->cfg.acceptance = ACC_METROPOLIS;
+        else if (!std::strcmp(acceptance, "metropolis_hastings")) b->cfg.acceptance = ACC_METROPOLIS_HASTINGS;
+        else return fail(CPM_E_CONFIG, "unknown acceptance mode " + dbg(acceptance) +
+                                           "; expected \"metropolis\" or \"metropolis_hastings\"");
+    }
+    if (proposal) {
+        if (!std::strcmp(proposal, "uniform")) b->cfg.proposal = PROP_UNIFORM;
+        else if (!std::strcmp(proposal, "edge_list")) b->cfg.proposal = PROP_EDGE_LIST;
+        else return fail(CPM_E_CONFIG, "unknown proposal mode " + dbg(proposal) + "; expected \"uniform\" or \"edge_list\"");
+    }
+    for (size_t i = 0; i < n_keys; ++i) {
+        const bool v = values[i] != 0;
+        if (!std::strcmp(keys[i], "volume")) b->cfg.active.volume = v;
+        else if (!std::strcmp(keys[i], "interface")) b->cfg.active.interface = v;
+        else if (!std::strcmp(keys[i], "adhesion")) b->cfg.active.adhesion = v;
+        else if (!std::strcmp(keys[i], "act")) b->cfg.active.act = v;
+        else return fail(CPM_E_CONFIG, "unknown active_terms key " + dbg(keys[i]) +
+                                           "; expected one of \"volume\", \"interface\", \"adhesion\", \"act\"");
+    }
+    if (grid_len != 2 && grid_len != 3)
+        return fail(CPM_E_CONFIG, "grid must have length 2 or 3 (dimensionality is inferred from it, not from an "
+                                  "explicit `dimension` argument); got length " + std::to_string(grid_len));
+    b->cfg.D = (int)grid_len;
+    for (size_t d = 0; d < grid_len; ++d) b->cfg.grid[d] = (int64_t)grid[d];
+    b->cfg.seed = seed;
+    *out = b.release();
+    return ok();
+}
+
+extern "C" int cpm_builder_register_cell_type(cpm_builder* b, const char* name, uint32_t target_volume,
+                                              uint32_t target_interface, double lambda_volume, double lambda_interface,
+                                              double lambda_act, uint32_t max_act) {
+    if (!b || !name) return fail(CPM_E_ARG, "null argument");
+    if (b->type_index.count(name)) return fail(CPM_E_CONFIG, "cell type " + dbg(name) + " has already been added");
+    CellType t;
+    t.name = name;
+    t.target_volume = target_volume;
+    t.target_interface = target_interface;
+    t.lambda_volume = lambda_volume;
+    t.lambda_interface = lambda_interface;
+    t.lambda_act = lambda_act;
+    t.max_act = max_act;
+    const std::string e = cell_type_error(t);
+    if (!e.empty()) return fail(CPM_E_CONFIG, e);
+    const size_t idx = b->type_index.size();
+    b->type_index[name] = idx;
+    b->cfg.types.push_back(t);
+    b->cfg.cell_counts.push_back(0);
+    return ok();
+}
+
+extern "C" int cpm_builder_add_cells(cpm_builder* b, const char* cell_type, uint64_t n) {
+    if (!b || !cell_type) return fail(CPM_E_ARG, "null argument");
+    auto it = b->type_index.find(cell_type);
+    if (it == b->type_index.end())
+        return fail(CPM_E_CONFIG, "unknown cell type " + dbg(cell_type) + "; call register_cell_type first");
+    b->cfg.cell_counts[it->second] = n;
+    return ok();
+}
+
+extern "C" int cpm_builder_set_adhesion(cpm_builder* b, const double* values, const size_t* row_lengths, size_t n_rows) {
+    if (!b || (n_rows && (!row_lengths))) return fail(CPM_E_ARG, "null argument");
+    b->cfg.adhesion.assign(n_rows, {});
+    size_t k = 0;
+    for (size_t r = 0; r < n_rows; ++r) {
+        b->cfg.adhesion[r].assign(values + k, values + k + row_lengths[r]);
+        k += row_lengths[r];
+    }
+    b->adhesion_set = true;
+    return ok();
+}
+
+extern "C" int cpm_builder_initialize(cpm_builder* b, const uint32_t* lattice, size_t lattice_len,
+                                      const uint64_t* cell_type_of, size_t cto_len, int32_t has_cto, int32_t warn) {
+    if (!b) return fail(CPM_E_ARG, "null argument");
+    if (lattice) {
+        if (!has_cto) return fail(CPM_E_CONFIG, "cell_type_of is required when lattice is supplied");
+        b->cfg.init_explicit = true;
+        b->cfg.init_lattice.assign(lattice, lattice + lattice_len);
+        b->cfg.init_type_of.assign(cell_type_of, cell_type_of + cto_len);
+    } else {
+        b->cfg.init_explicit = false;
+        b->cfg.init_lattice.clear();
+        b->cfg.init_type_of.clear();
+        b->cfg.warn_on_default_init = warn != 0;
+    }
+    b->init_set = true;
+    return ok();
+}
+
+// UserConfig::resolve (config.rs:200-257) with the windows supplied.
+static int resolve(const cpm_builder* b, uint64_t burn, uint64_t readout, uint64_t interval, Config& c) {
+    if (!b->adhesion_set) return fail(CPM_E_CONFIG, "adhesion matrix is required");
+    c = b->cfg;
+    if (!b->energy_set) c.energy_nbh = c.D == 2 ? NBH_MOORE : NBH_EIGHTEEN;
+    c.burn_in = burn;
+    c.readout = readout;
+    c.interval = interval;
+    c.min_cell_volume = 1;
+    return ok();
+}
+
+static int check_supported(const Config& c) {
+    if (c.acceptance != ACC_METROPOLIS)
+        return fail(CPM_E_UNSUPPORTED, "acceptance = \"metropolis_hastings\" is a test instrument of the reference and is not run by the GB300 engine");
+    if (c.proposal != PROP_UNIFORM)
+        return fail(CPM_E_UNSUPPORTED, "proposal = \"edge_list\" is not run by the GB300 engine (use \"uniform\")");
+    if (c.active.act) return fail(CPM_E_UNSUPPORTED, "the Act energy term is not run by the GB300 engine");
+    return ok();
+}
+
+static int code_for(const std::string& e) {
+    if (e.rfind("CUDA error", 0) == 0) return CPM_E_CUDA;
+    return CPM_E_INIT;
+}
+
+extern "C" int cpm_builder_run(const cpm_builder* b, uint64_t burn, uint64_t readout, uint64_t interval,
+                               int32_t include_lattice, int32_t* used_default, cpm_result** out) {
+    if (!b || !out) return fail(CPM_E_ARG, "null argument");
+    Config c;
+    int e = resolve(b, burn, readout, interval, c);
+    if (e) return e;
+    std::string msg = validate(c);
+    if (!msg.empty()) return fail(CPM_E_CONFIG, msg);
+    if ((e = check_supported(c))) return e;
+    Initial init;
+    msg = initialize(c, init);
+    if (!msg.empty()) return fail(CPM_E_INIT, msg);
+    ReadoutOptions ro;
+    ro.include_lattice = include_lattice != 0;
+    ro.topology = true;
+    std::vector<Result> rs;
+    msg = run_many({c}, {init}, ro, rs);
+    if (!msg.empty()) return fail(code_for(msg), msg);
+    auto r = std::make_unique<cpm_result>();
+    r->r = std::move(rs[0]);
+    if (used_default) *used_default = init.used_default;
+    *out = r.release();
+    return ok();
+}
+
+extern "C" int cpm_builder_run_batch(const cpm_builder* b, const double* thetas, const size_t* lens, size_t n,
+                                     uint64_t burn, uint64_t readout, uint64_t interval, uint64_t master_seed,
+                                     int32_t include_lattice, int32_t* any_used_default, cpm_result** out) {
+    if (!b || (n && (!out || !lens))) return fail(CPM_E_ARG, "null argument");
+    Config c;
+    int e = resolve(b, burn, readout, interval, c);
+    if (e) return e;
+    const size_t expected = theta_len(c.types.size());
+    std::vector<std::vector<double>> th(n);
+    size_t k = 0;
+    for (size_t i = 0; i < n; ++i) {
+        if (lens[i] != expected)
+            return fail(CPM_E_THETA, "theta at index " + std::to_string(i) + " has length " + std::to_string(lens[i]) +
+                                         ", expected " + std::to_string(expected));
+        th[i].assign(thetas + k, thetas + k + lens[i]);
+        k += lens[i];
+    }
+    if ((e = check_supported(c))) return e;
+    ReadoutOptions ro;
+    ro.include_lattice = include_lattice != 0;
+    ro.topology = true;
+    std::vector<Result> rs;
+    const std::string msg = run_batch(c, th, master_seed, ro, rs);
+    if (!msg.empty()) {
+        int code = code_for(msg);
+        if (msg.find("must") != std::string::npos || msg.find("adhesion") != std::string::npos) code = CPM_E_CONFIG;
+        if (msg.rfind("max_act[", 0) == 0) code = CPM_E_THETA;
+        return fail(code, msg);
+    }
+    bool any = false;
+    for (size_t i = 0; i < n; ++i) {
+        any = any || rs[i].used_default;
+        auto r = std::make_unique<cpm_result>();
+        r->r = std::move(rs[i]);
+        out[i] = r.release();
+    }
+    if (any_used_default) *any_used_default = any;
+    return ok();
+}
+
+// builder.rs:405-430: placeholder windows, then resolve + validate.
+static int resolve_for_theta(const cpm_builder* b, Config& c) {
+    int e = resolve(b, 1, 1, 1, c);
+    if (e) return e;
+    const std::string msg = validate(c);
+    if (!msg.empty()) return fail(CPM_E_CONFIG, msg);
+    return ok();
+}
+
+extern "C" int cpm_builder_theta_len(const cpm_builder* b, size_t* out) {
+    if (!b || !out) return fail(CPM_E_ARG, "null argument");
+    Config c;
+    int e = resolve_for_theta(b, c);
+    if (e) return e;
+    *out = theta_len(c.types.size());
+    return ok();
+}
+
+extern "C" int cpm_builder_extract_theta(const cpm_builder* b, double* out, size_t cap) {
+    if (!b || !out) return fail(CPM_E_ARG, "null argument");
+    Config c;
+    int e = resolve_for_theta(b, c);
+    if (e) return e;
+    const std::vector<double> th = theta_extract(c);
+    if (cap < th.size()) return fail(CPM_E_ARG, "buffer too small");
+    std::memcpy(out, th.data(), th.size() * sizeof(double));
+    return ok();
+}
+
+extern "C" int cpm_builder_theta_name(const cpm_builder* b, size_t index, char* buf, size_t cap) {
+    if (!b || !buf) return fail(CPM_E_ARG, "null argument");
+    Config c;
+    int e = resolve_for_theta(b, c);
+    if (e) return e;
+    const std::vector<std::string> names = theta_names(c);
+    if (index >= names.size()) return fail(CPM_E_ARG, "theta index out of range");
+    if (cap < names[index].size() + 1) return fail(CPM_E_ARG, "buffer too small");
+    std::memcpy(buf, names[index].c_str(), names[index].size() + 1);
+    return ok();
+}
+
+extern "C" void cpm_builder_free(cpm_builder* b) { delete b; }
+
+// ------------------------------------------------------------- results ----
+extern "C" int cpm_result_info_get(const cpm_result* r, cpm_result_info* o) {
+    if (!r || !o) return fail(CPM_E_ARG, "null argument");
+    std::memset(o, 0, sizeof *o);
+    o->dim = r->r.D;
+    o->n_types = (int32_t)r->r.cell_type_names.size();
+    for (size_t d = 0; d < r->r.grid.size(); ++d) o->grid[d] = r->r.grid[d];
+    o->n_cells = r->r.cell_type_index.size();
+    o->n_samples = r->r.samples.size();
+    o->used_default = r->r.used_default;
+    return ok();
+}
+
+static void copy_str(char* dst, size_t cap, const std::string& s) {
+    std::snprintf(dst, cap, "%s", s.c_str());
+}
+
+extern "C" int cpm_result_metadata_get(const cpm_result* r, cpm_metadata* o) {
+    if (!r || !o) return fail(CPM_E_ARG, "null argument");
+    std::memset(o, 0, sizeof *o);
+    const Metadata& m = r->r.metadata;
+    copy_str(o->cpm_version, sizeof o->cpm_version, m.cpm_version);
+    copy_str(o->convention_hash, sizeof o->convention_hash, m.convention_hash);
+    copy_str(o->model_hash, sizeof o->model_hash, m.model_hash);
+    copy_str(o->seed_policy, sizeof o->seed_policy, m.seed_policy);
+    o->convention_version = m.convention_version;
+    o->theta_layout_version = m.theta_layout_version;
+    o->seed = m.seed;
+    o->derived_phi = m.derived_phi;
+    return ok();
+}
+
+extern "C" int cpm_result_status_get(const cpm_result* r, cpm_status* o) {
+    if (!r || !o) return fail(CPM_E_ARG, "null argument");
+    std::memset(o, 0, sizeof *o);
+    copy_str(o->kind, sizeof o->kind, r->r.status.kind);
+    o->has_cell = r->r.status.has_cell;
+    o->cell_id = r->r.status.cell_id;
+    o->at_mcs = r->r.status.at_mcs;
+    return ok();
+}
+
+extern "C" int cpm_result_cell_type_index(const cpm_result* r, uint32_t* out) {
+    if (!r || !out) return fail(CPM_E_ARG, "null argument");
+    std::memcpy(out, r->r.cell_type_index.data(), r->r.cell_type_index.size() * 4);
+    return ok();
+}
+
+extern "C" int cpm_result_cell_type_name(const cpm_result* r, size_t t, char* buf, size_t cap) {
+    if (!r || !buf) return fail(CPM_E_ARG, "null argument");
+    if (t >= r->r.cell_type_names.size()) return fail(CPM_E_ARG, "type index out of range");
+    const std::string& s = r->r.cell_type_names[t];
+    if (cap < s.size() + 1) return fail(CPM_E_ARG, "buffer too small");
+    std::memcpy(buf, s.c_str(), s.size() + 1);
+    return ok();
+}
+
+extern "C" int cpm_result_sample_sizes(const cpm_result* r, size_t s, cpm_sample_sizes* o) {
+    if (!r || !o) return fail(CPM_E_ARG, "null argument");
+    if (s >= r->r.samples.size()) return fail(CPM_E_ARG, "sample index out of range");
+    const Sample& S = r->r.samples[s];
+    std::memset(o, 0, sizeof *o);
+    o->n_contact = S.contact_a.size();
+    o->n_fragmented = S.fragmented.size();
+    o->n_medium = S.medium_volumes.size();
+    o->has_lattice = S.has_lattice;
+    return ok();
+}
+
+extern "C" int cpm_result_sample_read(const cpm_result* r, size_t s, const cpm_sample_out* o) {
+    if (!r || !o) return fail(CPM_E_ARG, "null argument");
+    if (s >= r->r.samples.size()) return fail(CPM_E_ARG, "sample index out of range");
+    const Sample& S = r->r.samples[s];
+    const int D = r->r.D;
+    if (o->mcs) *o->mcs = S.mcs;
+    if (o->conservative_energy) *o->conservative_energy = S.energy;
+    for (size_t i = 0; i < S.cells.size(); ++i) {
+        const CellSample& c = S.cells[i];
+        if (o->ids) o->ids[i] = c.id;
+        if (o->volume) o->volume[i] = c.volume;
+        if (o->interface) o->interface[i] = c.interface;
+        for (int d = 0; d < D; ++d) {
+            if (o->centroid) o->centroid[i * D + d] = c.centroid[d];
+            if (o->eigenvalues) o->eigenvalues[i * D + d] = c.eigenvalues[d];
+        }
+        if (o->radius_of_gyration_sq) o->radius_of_gyration_sq[i] = c.rg2;
+        if (o->kappa_sq) o->kappa_sq[i] = c.kappa2;
+    }
+    for (size_t k = 0; k < S.contact_a.size(); ++k) {
+        if (o->contact_a) o->contact_a[k] = S.contact_a[k];
+        if (o->contact_b) o->contact_b[k] = S.contact_b[k];
+        if (o->contact_count) o->contact_count[k] = S.contact_n[k];
+    }
+    if (o->fragmented_cells && !S.fragmented.empty())
+        std::memcpy(o->fragmented_cells, S.fragmented.data(), S.fragmented.size() * 4);
+    if (o->medium_component_volumes && !S.medium_volumes.empty())
+        std::memcpy(o->medium_component_volumes, S.medium_volumes.data(), S.medium_volumes.size() * 4);
+    if (o->medium_component_touches_boundary && !S.medium_touches.empty())
+        std::memcpy(o->medium_component_touches_boundary, S.medium_touches.data(), S.medium_touches.size());
+    if (o->lattice && S.has_lattice) std::memcpy(o->lattice, S.lattice.data(), S.lattice.size() * 4);
+    return ok();
+}
+
+extern "C" int cpm_result_stats(const cpm_result* r, uint64_t* out16) {
+    if (!r || !out16) return fail(CPM_E_ARG, "null argument");
+    std::memset(out16, 0, 16 * sizeof(uint64_t));
+    for (size_t i = 0; i < r->r.stats.size() && i < 16; ++i) out16[i] = r->r.stats[i];
+    return ok();
+}
+
+extern "C" void cpm_result_free(cpm_result* r) { delete r; }
+
+// -------------------------------------------------------------- engine ----
+struct cpm_engine {
+    std::vector<Config> configs;
+    std::vector<Initial> initials;
+    DeviceSims sims;
+    double* d_energy = nullptr;
+    uint32_t* d_recount = nullptr;
+    size_t recount_cap = 0;
+    ~cpm_engine() {
+        if (d_energy) cudaFree(d_energy);
+        if (d_recount) cudaFree(d_recount);
+    }
+};
+
+static int prepare(const cpm_builder* const* builders, size_t n, std::vector<Config>& cfgs, std::vector<Initial>& inits,
+                   uint64_t burn, uint64_t readout, uint64_t interval) {
+    cfgs.resize(n);
+    inits.resize(n);
+    for (size_t i = 0; i < n; ++i) {
+        if (!builders[i]) return fail(CPM_E_ARG, "null builder");
+        int e = resolve(builders[i], burn, readout, interval, cfgs[i]);
+        if (e) return e;
+        std::string msg = validate(cfgs[i]);
+        if (!msg.empty()) return fail(CPM_E_CONFIG, msg);
+        if ((e = check_supported(cfgs[i]))) return e;
+        msg = initialize(cfgs[i], inits[i]);
+        if (!msg.empty()) return fail(CPM_E_INIT, msg);
+    }
+    return ok();
+}
+
+extern "C" int cpm_engine_create(const cpm_builder* const* builders, size_t n, void* stream, cpm_engine** out) {
+    if (!builders || !out || n == 0) return fail(CPM_E_ARG, "null argument");
+    auto e = std::make_unique<cpm_engine>();
+    int rc = prepare(builders, n, e->configs, e->initials, 1, 1, 1);
+    if (rc) return rc;
+    std::vector<int> zeros(n, 0), ones(n, 1);
+    const std::string msg = e->sims.create(e->configs, e->initials, zeros, ones, false, (cudaStream_t)stream);
+    if (!msg.empty()) return fail(code_for(msg), msg);
+    if (cudaMalloc(&e->d_energy, sizeof(double)) != cudaSuccess) return fail(CPM_E_CUDA, "cudaMalloc failed");
+    *out = e.release();
+    return ok();
+}
+
+extern "C" int cpm_engine_size(const cpm_engine* e, size_t* out) {
+    if (!e || !out) return fail(CPM_E_ARG, "null argument");
+    *out = e->sims.size();
+    return ok();
+}
+
+static bool bad_sim(const cpm_engine* e, size_t i) { return !e || i >= e->sims.size(); }
+
+extern "C" int cpm_engine_sim_info(const cpm_engine* e, size_t i, cpm_sim_info* o) {
+    if (bad_sim(e, i) || !o) return fail(CPM_E_ARG, "bad engine or simulation index");
+    const SimLayout& L = e->sims.layout(i);
+    const SimDesc& s = e->sims.host_desc(i);
+    std::memset(o, 0, sizeof *o);
+    o->dim = L.g.D;
+    o->periodic = L.g.periodic;
+    for (int d = 0; d < 3; ++d) { o->dims[d] = L.g.dims[d]; o->padded_dims[d] = L.g.pdims[d]; o->strides[d] = L.g.strides[d]; }
+    o->n_sites = L.g.n_sites;
+    o->n_padded = L.g.n_padded;
+    o->n_cells = L.n_cells;
+    o->n_energy = L.NE;
+    o->n_colors = s.n_colors;
+    return ok();
+}
+
+extern "C" int cpm_engine_run_mcs(cpm_engine* e, uint64_t n) {
+    if (!e) return fail(CPM_E_ARG, "null argument");
+    if (n == 0) return ok();
+    std::vector<RunPlan> plans(e->sims.size());
+    for (size_t i = 0; i < plans.size(); ++i) {
+        RunPlan& p = plans[i];
+        std::memset(&p, 0, sizeof p);
+        p.sim = (int)i;
+        p.burn_in = n;
+        p.interval = n;
+        p.energy_sample_start = ~0ull;
+        p.n_samples = 0;
+    }
+    const std::string msg = e->sims.run(plans);
+    if (!msg.empty()) return fail(code_for(msg), msg);
+    return ok();
+}
+
+extern "C" int cpm_engine_synchronize(cpm_engine* e) {
+    if (!e) return fail(CPM_E_ARG, "null argument");
+    const std::string msg = e->sims.sync();
+    if (!msg.empty()) return fail(CPM_E_CUDA, msg);
+    return ok();
+}
+
+extern "C" int cpm_engine_mcs(const cpm_engine* e, size_t i, uint64_t* out) {
+    if (bad_sim(e, i) || !out) return fail(CPM_E_ARG, "bad engine or simulation index");
+    const std::string msg = e->sims.read_mcs(i, *out);
+    return msg.empty() ? ok() : fail(CPM_E_CUDA, msg);
+}
+
+extern "C" int cpm_engine_read_padded(const cpm_engine* e, size_t i, uint32_t* out) {
+    if (bad_sim(e, i) || !out) return fail(CPM_E_ARG, "bad engine or simulation index");
+    std::vector<uint32_t> p;
+    const std::string msg = e->sims.read_padded(i, p);
+    if (!msg.empty()) return fail(CPM_E_CUDA, msg);
+    std::memcpy(out, p.data(), p.size() * 4);
+    return ok();
+}
+
+extern "C" int cpm_engine_read_lattice(const cpm_engine* e, size_t i, uint32_t* out) {
+    if (bad_sim(e, i) || !out) return fail(CPM_E_ARG, "bad engine or simulation index");
+    std::vector<uint32_t> p;
+    const std::string msg = e->sims.read_padded(i, p);
+    if (!msg.empty()) return fail(CPM_E_CUDA, msg);
+    const Geometry& g = e->sims.layout(i).g;
+    int64_t x[3] = {0, 0, 0};
+    for (int64_t q = 0; q < g.n_sites; ++q) {
+        out[q] = p[g.flat(x)];
+        for (int d = g.D - 1; d >= 0; --d) { if (++x[d] < g.dims[d]) break; x[d] = 0; }
+    }
+    return ok();
+}
+
+extern "C" int cpm_engine_read_cells(const cpm_engine* e, size_t i, uint32_t* volume, uint32_t* interface,
+                                     int64_t* sp, int64_t* so) {
+    if (bad_sim(e, i)) return fail(CPM_E_ARG, "bad engine or simulation index");
+    std::vector<uint32_t> v, it;
+    std::vector<int64_t> a, b;
+    const std::string msg = e->sims.read_cells(i, v, it, a, b);
+    if (!msg.empty()) return fail(CPM_E_CUDA, msg);
+    if (volume) std::memcpy(volume, v.data(), v.size() * 4);
+    if (interface) std::memcpy(interface, it.data(), it.size() * 4);
+    if (sp) std::memcpy(sp, a.data(), a.size() * 8);
+    if (so) std::memcpy(so, b.data(), b.size() * 8);
+    return ok();
+}
+
+extern "C" int cpm_engine_energy(const cpm_engine* e, size_t i, double* out) {
+    if (bad_sim(e, i) || !out) return fail(CPM_E_ARG, "bad engine or simulation index");
+    const SimLayout& L = e->sims.layout(i);
+    cudaError_t ce = cpmgpu::launch_energy(L.g.D, L.NE, e->sims.device_desc(i), e->d_energy, e->sims.stream());
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(out, e->d_energy, sizeof(double), cudaMemcpyDeviceToHost, e->sims.stream());
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->sims.stream());
+    if (ce != cudaSuccess) return fail(CPM_E_CUDA, std::string("CUDA error: ") + cudaGetErrorString(ce));
+    return ok();
+}
+
+extern "C" int cpm_engine_recount_check(const cpm_engine* ec, size_t i, int32_t* okp, uint32_t* volume, uint32_t* interface) {
+    cpm_engine* e = const_cast<cpm_engine*>(ec);
+    if (bad_sim(e, i)) return fail(CPM_E_ARG, "bad engine or simulation index");
+    const SimLayout& L = e->sims.layout(i);
+    const size_t n1 = L.n_cells + 1;
+    if (e->recount_cap < 2 * n1) {
+        if (e->d_recount) cudaFree(e->d_recount);
+        e->d_recount = nullptr;
+        if (cudaMalloc(&e->d_recount, 2 * n1 * 4) != cudaSuccess) return fail(CPM_E_CUDA, "cudaMalloc failed");
+        e->recount_cap = 2 * n1;
+    }
+    cudaStream_t st = e->sims.stream();
+    cudaError_t ce = cudaMemsetAsync(e->d_recount, 0, 2 * n1 * 4, st);
+    if (ce == cudaSuccess)
+        ce = cpmgpu::launch_recount(L.g.D, L.NE, e->sims.device_desc(i), L.g.n_sites, e->d_recount, e->d_recount + n1, st);
+    std::vector<uint32_t> rc(2 * n1);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(rc.data(), e->d_recount, 2 * n1 * 4, cudaMemcpyDeviceToHost, st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+    if (ce != cudaSuccess) return fail(CPM_E_CUDA, std::string("CUDA error: ") + cudaGetErrorString(ce));
+    std::vector<uint32_t> v, it;
+    std::vector<int64_t> a, b;
+    const std::string msg = e->sims.read_cells(i, v, it, a, b);
+    if (!msg.empty()) return fail(CPM_E_CUDA, msg);
+    bool same = true;
+    for (size_t id = 1; id < n1; ++id)
+        if (rc[id] != v[id] || rc[n1 + id] != it[id]) same = false;
+    if (okp) *okp = same;
+    if (volume) std::memcpy(volume, rc.data(), n1 * 4);
+    if (interface) std::memcpy(interface, rc.data() + n1, n1 * 4);
+    return ok();
+}
+
+extern "C" int cpm_engine_stats(const cpm_engine* e, size_t i, uint64_t* out16) {
+    if (bad_sim(e, i) || !out16) return fail(CPM_E_ARG, "bad engine or simulation index");
+    std::vector<uint64_t> s;
+    const std::string msg = e->sims.read_stats(i, s);
+    if (!msg.empty()) return fail(CPM_E_CUDA, msg);
+    std::memcpy(out16, s.data(), 16 * 8);
+    return ok();
+}
+
+extern "C" int cpm_engine_write_state(cpm_engine* e, size_t i, const uint32_t* padded, const uint32_t* volume,
+                                      const uint32_t* interface, const int64_t* sp, const int64_t* so) {
+    if (bad_sim(e, i) || !padded || !volume || !interface) return fail(CPM_E_ARG, "bad engine, index or buffer");
+    const SimLayout& L = e->sims.layout(i);
+    const size_t n1 = L.n_cells + 1, D = L.g.D;
+    std::vector<uint32_t> p(padded, padded + L.g.n_padded), v(volume, volume + n1), it(interface, interface + n1);
+    std::vector<int64_t> a, b;
+    if (sp) a.assign(sp, sp + n1 * D);
+    if (so) b.assign(so, so + n1 * D * D);
+    const std::string msg = e->sims.write_state(i, p, v, it, sp ? &a : nullptr, so ? &b : nullptr);
+    return msg.empty() ? ok() : fail(CPM_E_CUDA, msg);
+}
+
+extern "C" int cpm_engine_evaluate_moves(cpm_engine* e, size_t i, size_t n, const int64_t* target, const int32_t* k,
+                                         const double* u, cpm_move* out) {
+    if (bad_sim(e, i) || (n && (!target || !k || !u || !out))) return fail(CPM_E_ARG, "bad engine, index or buffer");
+    if (n == 0) return ok();
+    const SimLayout& L = e->sims.layout(i);
+    const int ncopy = 2 * L.g.D;
+    for (size_t m = 0; m < n; ++m) {
+        if (k[m] < 0 || k[m] >= ncopy) return fail(CPM_E_ARG, "copy direction out of range");
+        // the target must be an interior site (its stencil then stays inside the padded array)
+        int64_t f = target[m];
+        if (f < 0 || f >= L.g.n_padded) return fail(CPM_E_ARG, "target outside the lattice");
+        for (int d = 0; d < L.g.D; ++d) {
+            const int64_t c = f / L.g.strides[d];
+            f %= L.g.strides[d];
+            if (c == 0 || c == L.g.pdims[d] - 1) return fail(CPM_E_ARG, "target is a halo site");
+        }
+    }
+    std::string err;
+    const uint64_t* t3 = L.g.D == 3 ? device_table3d(err) : nullptr;
+    if (L.g.D == 3 && !t3) return fail(CPM_E_CUDA, err);
+    int64_t* d_t = nullptr;
+    int32_t* d_k = nullptr;
+    double* d_u = nullptr;
+    MoveOut* d_o = nullptr;
+    cudaError_t ce = cudaMalloc(&d_t, n * 8);
+    if (ce == cudaSuccess) ce = cudaMalloc(&d_k, n * 4);
+    if (ce == cudaSuccess) ce = cudaMalloc(&d_u, n * 8);
+    if (ce == cudaSuccess) ce = cudaMalloc(&d_o, n * sizeof(MoveOut));
+    cudaStream_t st = e->sims.stream();
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_t, target, n * 8, cudaMemcpyHostToDevice, st);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_k, k, n * 4, cudaMemcpyHostToDevice, st);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_u, u, n * 8, cudaMemcpyHostToDevice, st);
+    if (ce == cudaSuccess) ce = cpmgpu::launch_evaluate(L.g.D, L.NE, e->sims.device_desc(i), (int64_t)n, d_t, d_k, d_u, d_o, t3, st);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(out, d_o, n * sizeof(MoveOut), cudaMemcpyDeviceToHost, st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+    cudaFree(d_t); cudaFree(d_k); cudaFree(d_u); cudaFree(d_o);
+    if (ce != cudaSuccess) return fail(CPM_E_CUDA, std::string("CUDA error: ") + cudaGetErrorString(ce));
+    return ok();
+}
+
+extern "C" int cpm_engine_commit_moves(cpm_engine* e, size_t i, size_t n, const int64_t* target, const uint32_t* gaining) {
+    if (bad_sim(e, i) || (n && (!target || !gaining))) return fail(CPM_E_ARG, "bad engine, index or buffer");
+    if (n == 0) return ok();
+    const SimLayout& L = e->sims.layout(i);
+    for (size_t m = 0; m < n; ++m) {
+        int64_t f = target[m];
+        if (f < 0 || f >= L.g.n_padded) return fail(CPM_E_ARG, "target outside the lattice");
+        for (int d = 0; d < L.g.D; ++d) {
+            const int64_t c = f / L.g.strides[d];
+            f %= L.g.strides[d];
+            if (c == 0 || c == L.g.pdims[d] - 1) return fail(CPM_E_ARG, "target is a halo site");
+        }
+        if (gaining[m] > (uint32_t)L.n_cells) return fail(CPM_E_ARG, "gaining cell id out of range");
+    }
+    int64_t* d_t = nullptr;
+    uint32_t* d_g = nullptr;
+    cudaStream_t st = e->sims.stream();
+    cudaError_t ce = cudaMalloc(&d_t, n * 8);
+    if (ce == cudaSuccess) ce = cudaMalloc(&d_g, n * 4);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_t, target, n * 8, cudaMemcpyHostToDevice, st);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_g, gaining, n * 4, cudaMemcpyHostToDevice, st);
+    if (ce == cudaSuccess) ce = cpmgpu::launch_commit_moves(L.g.D, L.NE, e->sims.device_desc(i), (int64_t)n, d_t, d_g, st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+    cudaFree(d_t); cudaFree(d_g);
+    if (ce != cudaSuccess) return fail(CPM_E_CUDA, std::string("CUDA error: ") + cudaGetErrorString(ce));
+    return ok();
+}
+
+extern "C" void cpm_engine_destroy(cpm_engine* e) { delete e; }
+
+// ---------------------------------------------------------- many-run ----
+extern "C" int cpm_run_many(const cpm_builder* const* builders, size_t n, uint64_t burn, uint64_t readout,
+                            uint64_t interval, int32_t include_lattice, int32_t topology, cpm_result** out) {
+    if (!builders || !out) return fail(CPM_E_ARG, "null argument");
+    std::vector<Config> cfgs;
+    std::vector<Initial> inits;
+    int rc = prepare(builders, n, cfgs, inits, burn, readout, interval);
+    if (rc) return rc;
+    ReadoutOptions ro;
+    ro.include_lattice = include_lattice != 0;
+    ro.topology = topology != 0;
+    std::vector<Result> rs;
+    const std::string msg = run_many(cfgs, inits, ro, rs);
+    if (!msg.empty()) return fail(code_for(msg), msg);
+    for (size_t i = 0; i < n; ++i) {
+        auto r = std::make_unique<cpm_result>();
+        r->r = std::move(rs[i]);
+        out[i] = r.release();
+    }
+    return ok();
+}
+
+// ------------------------------------------------------ host-only helpers ----
+extern "C" int cpm_builder_initial_state(const cpm_builder* b, uint32_t* lattice_out, size_t cap, uint32_t* type_of_out,
+                                         size_t* n_cells, int32_t* used_default) {
+    if (!b || !n_cells) return fail(CPM_E_ARG, "null argument");
+    Config c;
+    int e = resolve(b, 1, 1, 1, c);
+    if (e) return e;
+    std::string msg = validate(c);
+    if (!msg.empty()) return fail(CPM_E_CONFIG, msg);
+    Initial init;
+    msg = initialize(c, init);
+    if (!msg.empty()) return fail(CPM_E_INIT, msg);
+    if (lattice_out) {
+        if (cap < init.lattice.size()) return fail(CPM_E_ARG, "lattice buffer too small");
+        std::memcpy(lattice_out, init.lattice.data(), init.lattice.size() * 4);
+    }
+    if (type_of_out) {
+        if (*n_cells < init.type_of.size()) return fail(CPM_E_ARG, "type_of buffer too small");
+        std::memcpy(type_of_out, init.type_of.data(), init.type_of.size() * 4);
+    }
+    *n_cells = init.type_of.size();
+    if (used_default) *used_default = init.used_default;
+    return ok();
+}
+
+extern "C" int cpm_builder_hashes(const cpm_builder* b, uint64_t burn, uint64_t readout, uint64_t interval,
+                                  const uint32_t* lattice, size_t lattice_len, const uint32_t* type_of, size_t n_cells,
+                                  char* conv_out, char* model_out) {
+    if (!b || !conv_out || !model_out || (lattice_len && !lattice) || (n_cells && !type_of))
+        return fail(CPM_E_ARG, "null argument");
+    Config c;
+    int e = resolve(b, burn, readout, interval, c);
+    if (e) return e;
+    const std::string ch = convention_hash(c);
+    const std::string mh = model_hash(c, std::vector<uint32_t>(lattice, lattice + lattice_len),
+                                      std::vector<uint32_t>(type_of, type_of + n_cells));
+    std::memcpy(conv_out, ch.c_str(), 65);
+    std::memcpy(model_out, mh.c_str(), 65);
+    return ok();
+}
+
+extern "C" uint64_t cpm_derive_seed_u64(uint64_t master, uint64_t index) { return derive_seed_u64(master, index); }

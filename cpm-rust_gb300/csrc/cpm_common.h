@@ -1,0 +1,109 @@
+// Plain-old-data layout shared by the host engine and the sm_103a kernels.
+//
+// One `SimDesc` describes one device-resident simulation: its halo-padded
+// sigma lattice (the reference's layout, crates/cpm-core/src/lattice.rs:70-255),
+// the per-cell arrays (crates/cpm-core/src/state.rs:168-248), the offset
+// tables (crates/cpm-core/src/model.rs:44-76) and the parameters the local
+// Delta-H needs (crates/cpm-core/src/energy.rs:72-309). Per-cell arrays are
+// indexed by cell id (length n_cells + 1, slot 0 = medium, never read for
+// volume/interface terms) so the hot loop needs no `id - 1` branch.
+#pragma once
+#include <stdint.h>
+
+#define CPM_MAX_D 3
+#define CPM_MAX_STENCIL 26
+
+// Statistics counters per simulation (device, u64 each).
+enum CpmStat {
+    CPM_STAT_ATTEMPTS = 0,   // sites visited (one per site per MCS)
+    CPM_STAT_NONNULL = 1,    // passed the early-out (sigma[t] != sigma[s])
+    CPM_STAT_TOPO_REJECT = 2,
+    CPM_STAT_GUARD_REJECT = 3,
+    CPM_STAT_EVALUATED = 4,  // reached Delta-H
+    CPM_STAT_ACCEPTED = 5,
+    CPM_STAT_ROUNDS = 6,     // conflict-resolution rounds (summed over passes)
+    CPM_STAT_PASSES = 7,
+    CPM_STAT_SPIN_TIMEOUTS = 8,  // bounded waits that gave up (must stay 0)
+    CPM_STAT_COUNT = 16
+};
+
+struct SimDesc {
+    // ---- geometry ----
+    int32_t D;
+    int32_t periodic;
+    int32_t dims[3];
+    int32_t pdims[3];
+    int64_t strides[3];
+    int64_t n_sites;
+    int64_t n_padded;
+    // checkerboard colouring: per axis 1, 2 or 3 colours; `lim` is the
+    // exclusive upper coordinate of the parity colours on that axis.
+    int32_t ncol[3];
+    int32_t lim[3];
+    int32_t n_colors;
+    int32_t max_class;  // largest colour-class size
+    // ---- stencils (flat padded-index deltas) ----
+    int32_t n_copy;
+    int32_t n_energy;
+    int64_t copy_off[6];
+    int64_t energy_off[CPM_MAX_STENCIL];
+    int64_t topo_off[CPM_MAX_STENCIL];
+    int8_t energy_vec[CPM_MAX_STENCIL][3];  // integer offset of each energy neighbour
+    uint32_t energy_pos_mask;               // offsets whose first nonzero component is > 0
+    uint32_t table2d[8];                    // 2D simple-point table (256 bits)
+    // ---- parameters ----
+    int32_t n_types;
+    uint32_t min_cell_volume;
+    uint64_t seed;
+    const double* J;                // (n_types+1)^2 row-major, 0 = medium
+    const double* lambda_v;         // per type
+    const double* lambda_i;
+    const uint32_t* target_v;
+    const uint32_t* target_i;
+    // ---- state ----
+    int32_t n_cells;
+    int32_t pad0;
+    uint32_t* sigma;                // n_padded
+    const uint16_t* adh_of;         // per id: type + 1 (0 for medium)
+    uint32_t* volume;               // per id
+    uint32_t* interface;            // per id
+    int64_t* sum_pos;               // per id * D
+    int64_t* sum_outer;             // per id * D * D
+    unsigned long long* slots;      // per id (only when they do not fit in shared memory)
+    unsigned long long* stats;      // CPM_STAT_COUNT
+    uint64_t mcs;                   // MCS already completed (RNG counter base)
+    // ---- run-window outputs (device) ----
+    double* energy_out;             // energies written by the run plan
+    uint32_t* sample_volume;        // n_samples * (n_cells+1)
+    uint32_t* sample_interface;
+    int64_t* sample_sum_pos;        // n_samples * (n_cells+1) * D
+    int64_t* sample_sum_outer;      // n_samples * (n_cells+1) * D * D
+    uint32_t* sample_lattice;       // n_samples * n_sites (unpadded) or null
+    int32_t* error;                 // first error code (0 = none)
+};
+
+// One unit of device work: a whole run plan for one simulation, replaying
+// output.rs:434-468 (burn-in in interval-sized chunks with the energy trace
+// over its final quarter, then `n_samples` readout chunks with one sample
+// after each).
+struct RunPlan {
+    int32_t sim;
+    int32_t n_samples;
+    uint64_t burn_in;
+    uint64_t interval;
+    uint64_t energy_sample_start;  // burned_in >= this -> record energy
+    uint64_t readout_chunks;       // == n_samples
+    int32_t write_samples;
+    int32_t write_lattice;
+};
+
+// Per-move record of the parity harness (same layout as the oracle's).
+struct MoveOut {
+    int64_t target_flat, source_flat;
+    uint32_t losing, gaining;
+    int32_t null_move, topology_ok, volume_guard_ok, evaluated;
+    int32_t delta_i_losing, delta_i_gaining;
+    double delta_h;
+    int32_t accepted;
+    int32_t pad;
+};

@@ -1,0 +1,239 @@
+// Device-side building blocks of the Cellular Potts hot path (sm_103a).
+//
+// Restates, on the GPU, the per-attempt logic of the reference
+// (crates/cpm-core/src/monte_carlo.rs:52-145): the early-out, the
+// simple-point connectivity test (connectivity.rs:42-65), the volume guard
+// (monte_carlo.rs:77-79), the local Delta-H in FP64 with the reference's
+// operation order (energy.rs:92-103, 167-202, 242-264, 521-523) and the
+// commit bookkeeping (dynamics.rs:23-183). Random numbers come from a
+// counter-based Philox4x32-10 (Salmon et al., "Parallel random numbers: as
+// easy as 1, 2, 3", SC'11), so every attempt's draws are a pure function of
+// (seed, mcs, site) and independent of scheduling.
+#pragma once
+#include <stdint.h>
+#include "cpm_common.h"
+
+namespace cpmgpu {
+
+// ---------------------------------------------------------------- Philox ----
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+        const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+        c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return c;
+}
+
+enum : uint32_t { TAG_SITE = 0u, TAG_ORDER = 1u, TAG_PASS = 2u };
+
+// Draws of one site attempt at one MCS: x -> copy direction, (z,w) -> u.
+__device__ __forceinline__ uint4 site_draw(uint64_t seed, uint64_t mcs, uint32_t site) {
+    return philox4x32_10(make_uint4(site, (uint32_t)mcs, (uint32_t)(mcs >> 32) ^ (TAG_SITE << 28), 0x43504D31u),
+                         (uint32_t)seed, (uint32_t)(seed >> 32));
+}
+__device__ __forceinline__ uint4 aux_draw(uint64_t seed, uint64_t mcs, uint32_t tag, uint32_t a, uint32_t b) {
+    return philox4x32_10(make_uint4(a, (uint32_t)mcs, (uint32_t)(mcs >> 32) ^ (tag << 28), b),
+                         (uint32_t)seed, (uint32_t)(seed >> 32));
+}
+// 53-bit uniform in [0,1), same resolution as rand's gen::<f64>().
+__device__ __forceinline__ double u53(uint4 r) {
+    const uint64_t v = (((uint64_t)r.z << 32) | r.w) >> 11;
+    return __dmul_rn((double)v, 1.0 / 9007199254740992.0);  // times 2^-53: exact
+}
+// Priority hash for the conflict-resolution order (murmur3 finaliser).
+__device__ __forceinline__ uint32_t mix32(uint32_t h) {
+    h ^= h >> 16; h *= 0x85EBCA6Bu;
+    h ^= h >> 13; h *= 0xC2B2AE35u;
+    h ^= h >> 16;
+    return h;
+}
+
+// ------------------------------------------------------ simple points ----
+// 2D: the 256-entry table (simple_point.rs:288-306) as 8 words.
+__device__ __forceinline__ bool table2d_bit(const uint32_t* t2, uint32_t p) {
+    return (t2[p >> 5] >> (p & 31u)) & 1u;
+}
+// 3D: the 2^26-bit table (simple_point.rs:337-366), L2-resident in HBM.
+__device__ __forceinline__ bool table3d_bit(const uint64_t* t3, uint32_t p) {
+    return (__ldg(t3 + (p >> 6)) >> (p & 63u)) & 1ull;
+}
+
+template <int D>
+__device__ __forceinline__ bool preserves_topology(const SimDesc& s, const uint32_t* sig, int64_t t, uint32_t losing,
+                                                   const uint32_t* t2, const uint64_t* t3) {
+    if (losing == 0) return true;  // medium is exempt (connectivity.rs:48-50)
+    constexpr int NF = D == 2 ? 8 : 26;
+    uint32_t p = 0;
+#pragma unroll
+    for (int i = 0; i < NF; ++i) p |= (uint32_t)(sig[t + s.topo_off[i]] == losing) << i;
+    return D == 2 ? table2d_bit(t2, p) : table3d_bit(t3, p);
+}
+
+// ------------------------------------------------------------ Delta-H ----
+// term(t, x) = lambda[t] * (x - target[t])^2, powi(2) == x*x (energy.rs:85-88).
+__device__ __forceinline__ double quad_term(double lambda, uint32_t target, double x) {
+    const double d = __dsub_rn(x, (double)target);
+    return __dmul_rn(lambda, __dmul_rn(d, d));
+}
+
+struct DeltaOut {
+    double dh;
+    int dl, dg;  // integer interface deltas (every weight is 1.0)
+};
+
+// Terms::total_delta = volume + interface + adhesion, each accumulated in the
+// reference's order. Explicit _rn intrinsics forbid FMA contraction, so the
+// result is bit-identical to the reference's separately rounded f64 ops.
+template <int NE>
+__device__ __forceinline__ DeltaOut delta_h(const SimDesc& s, const uint32_t* sig, const uint16_t* adh_of,
+                                            const uint32_t* volume, const uint32_t* interface, int64_t t,
+                                            uint32_t L, uint32_t G) {
+    const int nt1 = s.n_types + 1;
+    const int li = adh_of[L], gi = adh_of[G];
+    const double* JL = s.J + li * nt1;
+    const double* JG = s.J + gi * nt1;
+    double adh = 0.0;
+    int cl = 0, cg = 0;
+#pragma unroll
+    for (int k = 0; k < NE; ++k) {
+        const uint32_t nc = sig[t + s.energy_off[k]];
+        cl += nc == L;
+        cg += nc == G;
+        const int ni = adh_of[nc];
+        const double before = nc != L ? JL[ni] : 0.0;
+        const double after = nc != G ? JG[ni] : 0.0;
+        adh = __dadd_rn(adh, __dsub_rn(after, before));  // w == 1.0: w*x == x
+    }
+    DeltaOut o;
+    o.dl = 2 * cl - NE;  // sum_k (n == L ? +1 : -1)
+    o.dg = NE - 2 * cg;  // sum_k (n == G ? -1 : +1)
+    double vol = 0.0, itf = 0.0;
+    if (L) {
+        const int ty = li - 1;
+        const double v = (double)volume[L];
+        vol = __dadd_rn(vol, __dsub_rn(quad_term(s.lambda_v[ty], s.target_v[ty], __dsub_rn(v, 1.0)),
+                                       quad_term(s.lambda_v[ty], s.target_v[ty], v)));
+    }
+    if (G) {
+        const int ty = gi - 1;
+        const double v = (double)volume[G];
+        vol = __dadd_rn(vol, __dsub_rn(quad_term(s.lambda_v[ty], s.target_v[ty], __dadd_rn(v, 1.0)),
+                                       quad_term(s.lambda_v[ty], s.target_v[ty], v)));
+    }
+    if (L) {
+        const int ty = li - 1;
+        const double i = (double)interface[L];
+        itf = __dadd_rn(itf, __dsub_rn(quad_term(s.lambda_i[ty], s.target_i[ty], __dadd_rn(i, (double)o.dl)),
+                                       quad_term(s.lambda_i[ty], s.target_i[ty], i)));
+    }
+    if (G) {
+        const int ty = gi - 1;
+        const double i = (double)interface[G];
+        itf = __dadd_rn(itf, __dsub_rn(quad_term(s.lambda_i[ty], s.target_i[ty], __dadd_rn(i, (double)o.dg)),
+                                       quad_term(s.lambda_i[ty], s.target_i[ty], i)));
+    }
+    o.dh = __dadd_rn(__dadd_rn(vol, itf), adh);
+    return o;
+}
+
+// Metropolis arm of decide_acceptance (monte_carlo.rs:158).
+__device__ __forceinline__ bool metropolis(double dh, double u) {
+    return dh <= 0.0 || u < exp(-dh);
+}
+
+// ------------------------------------------------------------- commit ----
+// Nearest periodic image of `coord` to `centroid` (dynamics.rs:193-202).
+__device__ __forceinline__ int64_t nearest_image(int64_t coord, double centroid, int64_t extent, bool periodic) {
+    if (!periodic) return coord;
+    int64_t best = coord;
+    double bd = fabs(__dsub_rn((double)coord, centroid));
+    const double d1 = fabs(__dsub_rn((double)(coord - extent), centroid));
+    if (d1 < bd) { best = coord - extent; bd = d1; }
+    const double d2 = fabs(__dsub_rn((double)(coord + extent), centroid));
+    if (d2 < bd) { best = coord + extent; }
+    return best;
+}
+
+// Writes sigma[t] = v and, under a periodic boundary, every halo cell that
+// mirrors t (the local equivalent of lattice.rs:240-254's full refresh).
+template <int D>
+__device__ __forceinline__ void write_site(const SimDesc& s, uint32_t* sig, const int* x, uint32_t v) {
+    int alt[3][3], na[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) { na[d] = 1; alt[d][0] = 0; alt[d][1] = 0; alt[d][2] = 0; }
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        alt[d][0] = x[d] + 1;
+        if (s.periodic) {
+            if (x[d] == 0) alt[d][na[d]++] = s.pdims[d] - 1;       // far halo mirrors coordinate 0
+            if (x[d] == s.dims[d] - 1) alt[d][na[d]++] = 0;        // near halo mirrors the last one
+        }
+    }
+    for (int a = 0; a < na[0]; ++a)
+        for (int b = 0; b < (D > 1 ? na[1] : 1); ++b)
+            for (int c = 0; c < (D > 2 ? na[2] : 1); ++c) {
+                int64_t f = (int64_t)alt[0][a] * s.strides[0];
+                if (D > 1) f += (int64_t)alt[1][b] * s.strides[1];
+                if (D > 2) f += (int64_t)alt[2][c] * s.strides[2];
+                sig[f] = v;
+            }
+}
+
+// dynamics::commit for an accepted move whose cells this thread owns
+// exclusively (contact is recounted at sample time, not maintained here).
+template <int D>
+__device__ __forceinline__ void commit_move(const SimDesc& s, uint32_t* sig, uint32_t* volume, uint32_t* interface,
+                                            int64_t* sum_pos, int64_t* sum_outer, const int* x, uint32_t L,
+                                            uint32_t G, int dl, int dg) {
+    write_site<D>(s, sig, x, G);
+    if (L) {
+        volume[L] -= 1;
+        interface[L] += (uint32_t)dl;
+        int64_t* sp = sum_pos + (int64_t)L * D;
+        int64_t* so = sum_outer + (int64_t)L * D * D;
+#pragma unroll
+        for (int d = 0; d < D; ++d) sp[d] -= x[d];
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+#pragma unroll
+            for (int e = 0; e < D; ++e) so[d * D + e] -= (int64_t)x[d] * x[e];
+    }
+    if (G) {
+        const uint32_t vnew = volume[G] + 1;
+        volume[G] = vnew;
+        interface[G] += (uint32_t)dg;
+        uint32_t vb = vnew >= 1 ? vnew - 1 : 0;
+        if (vb < 1) vb = 1;
+        int64_t* sp = sum_pos + (int64_t)G * D;
+        int64_t* so = sum_outer + (int64_t)G * D * D;
+        int64_t img[3];
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const double cen = (double)sp[d] / (double)vb;
+            img[d] = nearest_image(x[d], cen, s.dims[d], s.periodic != 0);
+        }
+#pragma unroll
+        for (int d = 0; d < D; ++d) sp[d] += img[d];
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+#pragma unroll
+            for (int e = 0; e < D; ++e) so[d * D + e] += img[d] * img[e];
+    }
+}
+
+// Interior coordinates of a padded flat index.
+template <int D>
+__device__ __forceinline__ void coords_of(const SimDesc& s, int64_t f, int* x) {
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        const int64_t c = f / s.strides[d];
+        f -= c * s.strides[d];
+        x[d] = (int)c - 1;
+    }
+}
+
+}  // namespace cpmgpu

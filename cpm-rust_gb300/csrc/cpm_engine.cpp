@@ -1,0 +1,759 @@
+// Device residency, the run window and result assembly (host side).
+//
+// run_many() is the GB300 form of the reference's run path: it uploads every
+// simulation once, runs each one's whole run plan (burn-in + readout,
+// output.rs:434-468) inside one persistent sweep launch, and then assembles
+// the reference's readouts on the host from the device samples: per-cell
+// volume/interface/centroid/gyration (output.rs:147-302), the contact graph
+// (state.rs:127-157), labelling (labelling.rs:70-154), the run status
+// (output.rs:388-522) and the metadata hashes (config.rs:479-556).
+#include "cpm_engine.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <thread>
+
+#include "cpm_kernels.h"
+
+namespace cpmhost {
+
+static thread_local std::string g_cuda_error;
+std::string last_cuda_error() { return g_cuda_error; }
+
+#define CUDA_TRY(expr)                                                                   \
+    do {                                                                                 \
+        cudaError_t _e = (expr);                                                         \
+        if (_e != cudaSuccess) {                                                         \
+            g_cuda_error = std::string(#expr) + ": " + cudaGetErrorString(_e);           \
+            return std::string("CUDA error: ") + cudaGetErrorString(_e) + " (" #expr ")"; \
+        }                                                                                \
+    } while (0)
+
+int energy_count(int D, int kind) {
+    if (kind == NBH_VON_NEUMANN) return 2 * D;
+    if (kind == NBH_MOORE) return 8;
+    if (kind == NBH_EIGHTEEN) return 18;
+    return 26;
+}
+
+// ------------------------------------------------------------ 3D table ----
+const uint64_t* device_table3d(std::string& err) {
+    static std::mutex mu;
+    static std::map<int, uint64_t*> tables;
+    std::lock_guard<std::mutex> lock(mu);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) { err = std::string("CUDA error: ") + cudaGetErrorString(e); return nullptr; }
+    auto it = tables.find(dev);
+    if (it != tables.end()) return it->second;
+    uint32_t face[26], full[26], origin;
+    simple_point_masks(3, face, full, &origin);
+    uint64_t* words = nullptr;
+    uint32_t* d_adj = nullptr;
+    const size_t bytes = ((size_t)1 << 26) / 8;
+    if ((e = cudaMalloc(&words, bytes)) != cudaSuccess || (e = cudaMalloc(&d_adj, 52 * sizeof(uint32_t))) != cudaSuccess) {
+        err = std::string("CUDA error: ") + cudaGetErrorString(e);
+        return nullptr;
+    }
+    cudaMemcpy(d_adj, face, 26 * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    cudaMemcpy(d_adj + 26, full, 26 * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    e = cpmgpu::launch_table3d(words, d_adj, d_adj + 26, origin, 0);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    cudaFree(d_adj);
+    if (e != cudaSuccess) { err = std::string("CUDA error: ") + cudaGetErrorString(e); cudaFree(words); return nullptr; }
+    tables[dev] = words;
+    return words;
+}
+
+// --------------------------------------------------------- DeviceSims ----
+DeviceSims::~DeviceSims() {
+    if (arena_) cudaFree(arena_);
+    if (d_descs_) cudaFree(d_descs_);
+    if (d_plans_) cudaFree(d_plans_);
+    if (d_next_) cudaFree(d_next_);
+}
+
+namespace {
+struct Carve {
+    size_t off = 0;
+    size_t take(size_t bytes) {
+        const size_t o = off;
+        off += (bytes + 255) & ~(size_t)255;
+        return o;
+    }
+};
+}  // namespace
+
+std::string DeviceSims::create(const std::vector<Config>& configs, const std::vector<Initial>& initials,
+                               const std::vector<int>& n_samples, const std::vector<int>& n_energy,
+                               bool lattice_samples, cudaStream_t stream) {
+    stream_ = stream;
+    const size_t N = configs.size();
+    layouts_.resize(N);
+    descs_.resize(N);
+    uint32_t t2[8];
+    table2d(t2);
+    bool need_t3 = false;
+    // ---- sizes
+    struct Offs { size_t sigma, adh, vol, itf, sp, so, slots, stats, J, lv, li, tv, ti, energy, svol, sitf, ssp, sso, slat, err; };
+    std::vector<Offs> offs(N);
+    Carve cv;
+    for (size_t i = 0; i < N; ++i) {
+        const Config& c = configs[i];
+        SimLayout& L = layouts_[i];
+        L.g.init(c);
+        if (L.g.n_padded >= ((int64_t)1 << 31)) return "lattice too large for the device engine (padded sites must be < 2^31)";
+        L.NE = energy_count(c.D, c.energy_nbh);
+        L.n_cells = (int)initials[i].type_of.size();
+        L.n_samples = n_samples[i];
+        L.n_energy = n_energy[i];
+        L.lattice_samples = lattice_samples;
+        if (c.D == 3) need_t3 = true;
+        const size_t n1 = (size_t)L.n_cells + 1, nt = c.types.size(), D = (size_t)c.D;
+        Offs& o = offs[i];
+        o.sigma = cv.take(L.g.n_padded * 4);
+        o.adh = cv.take(n1 * 2);
+        o.vol = cv.take(n1 * 4);
+        o.itf = cv.take(n1 * 4);
+        o.sp = cv.take(n1 * D * 8);
+        o.so = cv.take(n1 * D * D * 8);
+        o.slots = cv.take(n1 * 8);
+        o.stats = cv.take(CPM_STAT_COUNT * 8);
+        o.J = cv.take((nt + 1) * (nt + 1) * 8);
+        o.lv = cv.take(nt * 8);
+        o.li = cv.take(nt * 8);
+        o.tv = cv.take(nt * 4);
+        o.ti = cv.take(nt * 4);
+        o.energy = cv.take((size_t)std::max(1, L.n_energy) * 8);
+        o.svol = cv.take((size_t)L.n_samples * n1 * 4);
+        o.sitf = cv.take((size_t)L.n_samples * n1 * 4);
+        o.ssp = cv.take((size_t)L.n_samples * n1 * D * 8);
+        o.sso = cv.take((size_t)L.n_samples * n1 * D * D * 8);
+        o.slat = lattice_samples ? cv.take((size_t)L.n_samples * L.g.n_sites * 4) : 0;
+        o.err = cv.take(8);
+    }
+    const uint64_t* t3 = nullptr;
+    if (need_t3) {
+        std::string err;
+        t3 = device_table3d(err);
+        if (!t3) return err;
+    }
+    CUDA_TRY(cudaMalloc(&arena_, std::max<size_t>(cv.off, 256)));
+    CUDA_TRY(cudaMalloc(&d_descs_, std::max<size_t>(N, 1) * sizeof(SimDesc)));
+    CUDA_TRY(cudaMalloc(&d_next_, sizeof(int) * 8));
+    (void)t3;
+    // ---- host staging, then one upload per buffer
+    std::vector<char> stage(cv.off, 0);
+    for (size_t i = 0; i < N; ++i) {
+        const Config& c = configs[i];
+        const SimLayout& L = layouts_[i];
+        const Offs& o = offs[i];
+        const size_t n1 = (size_t)L.n_cells + 1, nt = c.types.size();
+        std::vector<uint32_t> padded = pad_lattice(L.g, initials[i].lattice);
+        Derived dv = derive(c, L.g, padded, L.n_cells);
+        std::memcpy(stage.data() + o.sigma, padded.data(), padded.size() * 4);
+        std::vector<uint16_t> adh(n1, 0);
+        for (size_t id = 1; id < n1; ++id) adh[id] = (uint16_t)(initials[i].type_of[id - 1] + 1);
+        std::memcpy(stage.data() + o.adh, adh.data(), n1 * 2);
+        std::memcpy(stage.data() + o.vol, dv.volume.data(), n1 * 4);
+        std::memcpy(stage.data() + o.itf, dv.interface.data(), n1 * 4);
+        std::memcpy(stage.data() + o.sp, dv.sum_pos.data(), dv.sum_pos.size() * 8);
+        std::memcpy(stage.data() + o.so, dv.sum_outer.data(), dv.sum_outer.size() * 8);
+        std::vector<double> J((nt + 1) * (nt + 1));
+        for (size_t a = 0; a <= nt; ++a)
+            for (size_t b = 0; b <= nt; ++b) J[a * (nt + 1) + b] = c.adhesion[a][b];
+        std::memcpy(stage.data() + o.J, J.data(), J.size() * 8);
+        for (size_t t = 0; t < nt; ++t) {
+            const double lv = c.types[t].lambda_volume, li = c.types[t].lambda_interface;
+            std::memcpy(stage.data() + o.lv + t * 8, &lv, 8);
+            std::memcpy(stage.data() + o.li + t * 8, &li, 8);
+            std::memcpy(stage.data() + o.tv + t * 4, &c.types[t].target_volume, 4);
+            std::memcpy(stage.data() + o.ti + t * 4, &c.types[t].target_interface, 4);
+        }
+        // descriptor
+        SimDesc& s = descs_[i];
+        std::memset(&s, 0, sizeof s);
+        s.D = c.D;
+        s.periodic = c.periodic;
+        for (int d = 0; d < 3; ++d) {
+            s.dims[d] = (int32_t)L.g.dims[d];
+            s.pdims[d] = (int32_t)L.g.pdims[d];
+            s.strides[d] = L.g.strides[d];
+        }
+        s.n_sites = L.g.n_sites;
+        s.n_padded = L.g.n_padded;
+        s.n_colors = 1;
+        s.max_class = 1;
+        for (int d = 0; d < 3; ++d) {
+            if (d >= c.D) { s.ncol[d] = 1; s.lim[d] = 1; continue; }
+            const int64_t Ld = L.g.dims[d];
+            if (Ld == 1) { s.ncol[d] = 1; s.lim[d] = 1; }
+            else if (c.periodic && (Ld & 1)) { s.ncol[d] = 3; s.lim[d] = (int32_t)(Ld - 1); }
+            else { s.ncol[d] = 2; s.lim[d] = (int32_t)Ld; }
+            s.n_colors *= s.ncol[d];
+            s.max_class *= (int32_t)((s.lim[d] + 1) / 2);
+        }
+        auto cs = stencil(NBH_VON_NEUMANN, c.D);
+        s.n_copy = (int)cs.size();
+        for (size_t k = 0; k < cs.size(); ++k)
+            s.copy_off[k] = cs[k][0] * L.g.strides[0] + cs[k][1] * L.g.strides[1] + cs[k][2] * L.g.strides[2];
+        auto es = stencil(c.energy_nbh, c.D);
+        s.n_energy = (int)es.size();
+        s.energy_pos_mask = 0;
+        for (size_t k = 0; k < es.size(); ++k) {
+            s.energy_off[k] = es[k][0] * L.g.strides[0] + es[k][1] * L.g.strides[1] + es[k][2] * L.g.strides[2];
+            for (int d = 0; d < 3; ++d) s.energy_vec[k][d] = (int8_t)es[k][d];
+            for (int d = 0; d < c.D; ++d) {
+                if (es[k][d] > 0) { s.energy_pos_mask |= 1u << k; break; }
+                if (es[k][d] < 0) break;
+            }
+        }
+        auto ts = stencil(c.D == 2 ? NBH_MOORE : NBH_TWENTY_SIX, c.D);
+        for (size_t k = 0; k < ts.size(); ++k)
+            s.topo_off[k] = ts[k][0] * L.g.strides[0] + ts[k][1] * L.g.strides[1] + ts[k][2] * L.g.strides[2];
+        std::memcpy(s.table2d, t2, sizeof t2);
+        s.n_types = (int)nt;
+        s.min_cell_volume = c.min_cell_volume;
+        s.seed = c.seed;
+        s.n_cells = L.n_cells;
+        char* base = arena_;
+        s.sigma = (uint32_t*)(base + o.sigma);
+        s.adh_of = (const uint16_t*)(base + o.adh);
+        s.volume = (uint32_t*)(base + o.vol);
+        s.interface = (uint32_t*)(base + o.itf);
+        s.sum_pos = (int64_t*)(base + o.sp);
+        s.sum_outer = (int64_t*)(base + o.so);
+        s.slots = (unsigned long long*)(base + o.slots);
+        s.stats = (unsigned long long*)(base + o.stats);
+        s.J = (const double*)(base + o.J);
+        s.lambda_v = (const double*)(base + o.lv);
+        s.lambda_i = (const double*)(base + o.li);
+        s.target_v = (const uint32_t*)(base + o.tv);
+        s.target_i = (const uint32_t*)(base + o.ti);
+        s.mcs = 0;
+        s.energy_out = (double*)(base + o.energy);
+        s.sample_volume = (uint32_t*)(base + o.svol);
+        s.sample_interface = (uint32_t*)(base + o.sitf);
+        s.sample_sum_pos = (int64_t*)(base + o.ssp);
+        s.sample_sum_outer = (int64_t*)(base + o.sso);
+        s.sample_lattice = lattice_samples ? (uint32_t*)(base + o.slat) : nullptr;
+        s.error = (int32_t*)(base + o.err);
+    }
+    CUDA_TRY(cudaMemcpyAsync(arena_, stage.data(), cv.off, cudaMemcpyHostToDevice, stream_));
+    CUDA_TRY(cudaMemcpyAsync(d_descs_, descs_.data(), N * sizeof(SimDesc), cudaMemcpyHostToDevice, stream_));
+    CUDA_TRY(cudaStreamSynchronize(stream_));
+    return "";
+}
+
+std::string DeviceSims::run(const std::vector<RunPlan>& plans, int grid_override) {
+    std::string err;
+    const uint64_t* t3 = nullptr;
+    // group plans by kernel variant
+    std::map<std::pair<int, int>, std::vector<RunPlan>> groups;
+    for (const RunPlan& p : plans) {
+        const SimLayout& L = layouts_[p.sim];
+        groups[{L.g.D, L.NE}].push_back(p);
+        if (L.g.D == 3 && !t3) {
+            t3 = device_table3d(err);
+            if (!t3) return err;
+        }
+    }
+    size_t total = 0;
+    for (auto& kv : groups) total += kv.second.size();
+    if (total > plans_cap_) {
+        if (d_plans_) cudaFree(d_plans_);
+        d_plans_ = nullptr;
+        CUDA_TRY(cudaMalloc(&d_plans_, total * sizeof(RunPlan)));
+        plans_cap_ = total;
+    }
+    std::vector<RunPlan> flat;
+    std::vector<std::pair<size_t, size_t>> ranges;
+    for (auto& kv : groups) {
+        // largest simulations first: better tail behaviour of the persistent queue
+        std::sort(kv.second.begin(), kv.second.end(), [&](const RunPlan& a, const RunPlan& b) {
+            return layouts_[a.sim].g.n_sites > layouts_[b.sim].g.n_sites;
+        });
+        ranges.push_back({flat.size(), kv.second.size()});
+        flat.insert(flat.end(), kv.second.begin(), kv.second.end());
+    }
+    CUDA_TRY(cudaMemcpyAsync(d_plans_, flat.data(), flat.size() * sizeof(RunPlan), cudaMemcpyHostToDevice, stream_));
+    CUDA_TRY(cudaMemsetAsync(d_next_, 0, sizeof(int) * 8, stream_));
+    int dev = 0, sms = 1;
+    CUDA_TRY(cudaGetDevice(&dev));
+    CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    size_t gi = 0;
+    for (auto& kv : groups) {
+        const auto r = ranges[gi];
+        int max_cells = 0;
+        for (size_t k = 0; k < r.second; ++k) max_cells = std::max(max_cells, layouts_[flat[r.first + k].sim].n_cells);
+        int grid = grid_override > 0 ? grid_override : std::min<int>((int)r.second, sms * 4);
+        CUDA_TRY(cpmgpu::launch_sweep(kv.first.first, kv.first.second, d_descs_, d_plans_ + r.first, (int)r.second,
+                                      d_next_ + gi, t3, max_cells, std::max(1, grid), stream_));
+        ++gi;
+    }
+    return "";
+}
+
+std::string DeviceSims::sync() {
+    CUDA_TRY(cudaStreamSynchronize(stream_));
+    return "";
+}
+
+std::string DeviceSims::read_padded(size_t i, std::vector<uint32_t>& out) const {
+    out.resize((size_t)layouts_[i].g.n_padded);
+    CUDA_TRY(cudaMemcpy(out.data(), descs_[i].sigma, out.size() * 4, cudaMemcpyDeviceToHost));
+    return "";
+}
+
+std::string DeviceSims::read_cells(size_t i, std::vector<uint32_t>& vol, std::vector<uint32_t>& itf,
+                                   std::vector<int64_t>& sp, std::vector<int64_t>& so) const {
+    const size_t n1 = layouts_[i].n_cells + 1, D = layouts_[i].g.D;
+    vol.resize(n1); itf.resize(n1); sp.resize(n1 * D); so.resize(n1 * D * D);
+    CUDA_TRY(cudaMemcpy(vol.data(), descs_[i].volume, n1 * 4, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(itf.data(), descs_[i].interface, n1 * 4, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(sp.data(), descs_[i].sum_pos, sp.size() * 8, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(so.data(), descs_[i].sum_outer, so.size() * 8, cudaMemcpyDeviceToHost));
+    return "";
+}
+
+std::string DeviceSims::read_energy(size_t i, std::vector<double>& e) const {
+    e.resize(layouts_[i].n_energy);
+    if (!e.empty()) CUDA_TRY(cudaMemcpy(e.data(), descs_[i].energy_out, e.size() * 8, cudaMemcpyDeviceToHost));
+    return "";
+}
+
+std::string DeviceSims::read_samples(size_t i, int n, std::vector<uint32_t>& vol, std::vector<uint32_t>& itf,
+                                     std::vector<int64_t>& sp, std::vector<int64_t>& so,
+                                     std::vector<uint32_t>* lattice) const {
+    const size_t n1 = layouts_[i].n_cells + 1, D = layouts_[i].g.D;
+    vol.resize(n * n1); itf.resize(n * n1); sp.resize(n * n1 * D); so.resize(n * n1 * D * D);
+    if (n == 0) return "";
+    CUDA_TRY(cudaMemcpy(vol.data(), descs_[i].sample_volume, vol.size() * 4, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(itf.data(), descs_[i].sample_interface, itf.size() * 4, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(sp.data(), descs_[i].sample_sum_pos, sp.size() * 8, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(so.data(), descs_[i].sample_sum_outer, so.size() * 8, cudaMemcpyDeviceToHost));
+    if (lattice && descs_[i].sample_lattice) {
+        lattice->resize((size_t)n * layouts_[i].g.n_sites);
+        CUDA_TRY(cudaMemcpy(lattice->data(), descs_[i].sample_lattice, lattice->size() * 4, cudaMemcpyDeviceToHost));
+    }
+    return "";
+}
+
+std::string DeviceSims::read_stats(size_t i, std::vector<uint64_t>& stats) const {
+    stats.resize(CPM_STAT_COUNT);
+    CUDA_TRY(cudaMemcpy(stats.data(), descs_[i].stats, CPM_STAT_COUNT * 8, cudaMemcpyDeviceToHost));
+    return "";
+}
+
+std::string DeviceSims::read_mcs(size_t i, uint64_t& mcs) const {
+    CUDA_TRY(cudaMemcpy(&mcs, &d_descs_[i].mcs, 8, cudaMemcpyDeviceToHost));
+    return "";
+}
+
+std::string DeviceSims::write_state(size_t i, const std::vector<uint32_t>& padded, const std::vector<uint32_t>& vol,
+                                    const std::vector<uint32_t>& itf, const std::vector<int64_t>* sp,
+                                    const std::vector<int64_t>* so) {
+    const size_t n1 = layouts_[i].n_cells + 1;
+    if (padded.size() != (size_t)layouts_[i].g.n_padded || vol.size() != n1 || itf.size() != n1)
+        return "write_state: size mismatch";
+    CUDA_TRY(cudaMemcpy(descs_[i].sigma, padded.data(), padded.size() * 4, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(descs_[i].volume, vol.data(), n1 * 4, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(descs_[i].interface, itf.data(), n1 * 4, cudaMemcpyHostToDevice));
+    if (sp) CUDA_TRY(cudaMemcpy(descs_[i].sum_pos, sp->data(), sp->size() * 8, cudaMemcpyHostToDevice));
+    if (so) CUDA_TRY(cudaMemcpy(descs_[i].sum_outer, so->data(), so->size() * 8, cudaMemcpyHostToDevice));
+    return "";
+}
+
+// ============================================================ readouts ====
+// output.rs:183-231 — closed-form eigenvalues of the symmetric gyration tensor.
+static void symmetric_eigenvalues(int D, const double g[3][3], double out[3]) {
+    if (D == 2) {
+        const double a = g[0][0], b = g[0][1], d = g[1][1];
+        const double tr = a + d;
+        const double disc = std::sqrt(std::max((a - d) * (a - d) + 4.0 * b * b, 0.0));
+        out[0] = (tr + disc) / 2.0;
+        out[1] = (tr - disc) / 2.0;
+        return;
+    }
+    const double p1 = g[0][1] * g[0][1] + g[0][2] * g[0][2] + g[1][2] * g[1][2];
+    if (p1 == 0.0) { out[0] = g[0][0]; out[1] = g[1][1]; out[2] = g[2][2]; return; }
+    const double q = (g[0][0] + g[1][1] + g[2][2]) / 3.0;
+    const double a0 = g[0][0] - q, a1 = g[1][1] - q, a2 = g[2][2] - q;
+    const double p = std::sqrt((a0 * a0 + a1 * a1 + a2 * a2 + 2.0 * p1) / 6.0);
+    auto b = [&](int i, int j) { return (g[i][j] - (i == j ? q : 0.0)) / p; };
+    const double det = b(0, 0) * (b(1, 1) * b(2, 2) - b(1, 2) * b(2, 1)) - b(0, 1) * (b(1, 0) * b(2, 2) - b(1, 2) * b(2, 0)) +
+                       b(0, 2) * (b(1, 0) * b(2, 1) - b(1, 1) * b(2, 0));
+    const double r = std::min(1.0, std::max(-1.0, det / 2.0));
+    const double phi = std::acos(r) / 3.0;
+    const double e1 = q + 2.0 * p * std::cos(phi);
+    const double e3 = q + 2.0 * p * std::cos(phi + 2.0 * M_PI / 3.0);
+    out[0] = e1; out[1] = 3.0 * q - e1 - e3; out[2] = e3;
+}
+
+// output.rs:147-178 and 289-302
+static void cell_summary(int D, uint32_t id, uint32_t vol, uint32_t itf, const int64_t* sp, const int64_t* so,
+                         CellSample& o) {
+    o.id = id; o.volume = vol; o.interface = itf;
+    for (int d = 0; d < 3; ++d) { o.centroid[d] = 0.0; o.eigenvalues[d] = 0.0; }
+    const double v = (double)vol;
+    for (int d = 0; d < D; ++d) o.centroid[d] = (double)sp[d] / v;
+    double g[3][3] = {{0}};
+    for (int a = 0; a < D; ++a)
+        for (int b = 0; b < D; ++b) g[a][b] = (double)so[a * D + b] / v - o.centroid[a] * o.centroid[b];
+    double e[3];
+    symmetric_eigenvalues(D, g, e);
+    for (int i = 1; i < D; ++i)
+        for (int j = i; j > 0 && e[j] > e[j - 1]; --j) std::swap(e[j], e[j - 1]);
+    double sum = 0.0, sq = 0.0;
+    for (int i = 0; i < D; ++i) sum += e[i];
+    for (int i = 0; i < D; ++i) sq += e[i] * e[i];
+    const double dd = (double)D;
+    o.kappa2 = sum > 0.0 ? (dd / (dd - 1.0)) * (sq / (sum * sum)) - 1.0 / (dd - 1.0) : 0.0;
+    o.rg2 = sum;
+    for (int i = 0; i < D; ++i) o.eigenvalues[i] = e[i];
+}
+
+// Contact graph (state.rs:127-157) and labelling (labelling.rs:70-154) of
+// one lattice snapshot.
+static void topology_readouts(const Config& c, const Geometry& g, const std::vector<uint32_t>& padded, int n_cells,
+                              Sample& smp) {
+    const int D = c.D;
+    auto offs = [&](int kind) {
+        std::vector<int64_t> v;
+        for (auto& o : stencil(kind, D)) v.push_back(o[0] * g.strides[0] + o[1] * g.strides[1] + o[2] * g.strides[2]);
+        return v;
+    };
+    const std::vector<int64_t> eoff = offs(c.energy_nbh);
+    const std::vector<int64_t> coff = offs(NBH_VON_NEUMANN);
+    const std::vector<int64_t> moff = offs(D == 2 ? NBH_MOORE : NBH_TWENTY_SIX);
+    auto interior = [&](int64_t f) {
+        for (int d = 0; d < D; ++d) {
+            const int64_t q = f / g.strides[d];
+            f %= g.strides[d];
+            if (q == 0 || q == g.pdims[d] - 1) return false;
+        }
+        return true;
+    };
+    auto wrapped = [&](int64_t f) {
+        int64_t ic[3] = {0, 0, 0};
+        for (int d = 0; d < D; ++d) {
+            const int64_t q = f / g.strides[d];
+            f %= g.strides[d];
+            ic[d] = q == 0 ? g.dims[d] - 1 : (q == g.pdims[d] - 1 ? 0 : q - 1);
+        }
+        return g.flat(ic);
+    };
+    // contact (sparse, canonical (min, max) pairs)
+    std::map<uint64_t, uint32_t> contact;
+    int64_t x[3] = {0, 0, 0};
+    for (int64_t s = 0; s < g.n_sites; ++s) {
+        const int64_t i = g.flat(x);
+        const uint32_t ic = padded[i];
+        for (int64_t off : eoff) {
+            const int64_t j = i + off;
+            int64_t key;
+            bool has;
+            if (interior(j)) { key = j; has = true; }
+            else if (g.periodic) { key = wrapped(j); has = true; }
+            else { key = 0; has = false; }
+            if (has && key <= i) continue;
+            const uint32_t jc = padded[j];
+            if (jc == ic) continue;
+            const uint32_t a = std::min(ic, jc), b = std::max(ic, jc);
+            contact[((uint64_t)a << 32) | b] += 1;
+        }
+        for (int d = D - 1; d >= 0; --d) { if (++x[d] < g.dims[d]) break; x[d] = 0; }
+    }
+    for (auto& kv : contact) {
+        smp.contact_a.push_back((uint32_t)(kv.first >> 32));
+        smp.contact_b.push_back((uint32_t)kv.first);
+        smp.contact_n.push_back(kv.second);
+    }
+    // labelling
+    std::vector<char> vis((size_t)g.n_padded, 0);
+    std::vector<uint32_t> comps(n_cells + 1, 0);
+    std::deque<int64_t> q;
+    x[0] = x[1] = x[2] = 0;
+    for (int64_t s = 0; s < g.n_sites; ++s) {
+        const int64_t seed = g.flat(x);
+        for (int d = D - 1; d >= 0; --d) { if (++x[d] < g.dims[d]) break; x[d] = 0; }
+        if (vis[seed]) continue;
+        const uint32_t owner = padded[seed];
+        const std::vector<int64_t>& of = owner == 0 ? moff : coff;
+        vis[seed] = 1;
+        q.push_back(seed);
+        uint32_t vol = 0;
+        bool touches = false;
+        while (!q.empty()) {
+            const int64_t site = q.front();
+            q.pop_front();
+            ++vol;
+            for (int64_t off : of) {
+                const int64_t nb = site + off;
+                if (!interior(nb)) {
+                    if (owner == 0 && !g.periodic) touches = true;
+                    if (!g.periodic) continue;
+                }
+                const int64_t cn = interior(nb) ? nb : wrapped(nb);
+                if (vis[cn] || padded[cn] != owner) continue;
+                vis[cn] = 1;
+                q.push_back(cn);
+            }
+        }
+        if (owner == 0) { smp.medium_volumes.push_back(vol); smp.medium_touches.push_back(touches); }
+        else comps[owner] += 1;
+    }
+    for (int id = 1; id <= n_cells; ++id)
+        if (comps[id] > 1) smp.fragmented.push_back((uint32_t)id);
+}
+
+// output.rs:388-420
+static bool not_equilibrated(const std::vector<double>& y) {
+    const size_t n = y.size();
+    if (n < 3) return false;
+    double xm = 0.0, ym = 0.0;
+    for (size_t i = 0; i < n; ++i) xm += (double)i;
+    xm /= (double)n;
+    for (size_t i = 0; i < n; ++i) ym += y[i];
+    ym /= (double)n;
+    double num = 0.0, den = 0.0;
+    for (size_t i = 0; i < n; ++i) { num += ((double)i - xm) * (y[i] - ym); den += ((double)i - xm) * ((double)i - xm); }
+    if (den == 0.0) return false;
+    const double slope = num / den, icpt = ym - slope * xm;
+    double rv = 0.0;
+    for (size_t i = 0; i < n; ++i) { const double r = y[i] - (icpt + slope * (double)i); rv += r * r; }
+    const double rs = std::sqrt(rv / (double)n);
+    if (rs == 0.0) return std::fabs(slope) * (double)(n - 1) > 0.0;
+    return std::fabs(slope) * (double)(n - 1) > 2.0 * rs;
+}
+
+// output.rs:456-522 (priority NotEquilibrated > Fragmented > CellLost > Degenerate)
+static Status status_of(const Config& c, const std::vector<double>& trace, const std::vector<Sample>& samples,
+                        int n_cells, bool have_topology) {
+    Status st;
+    if (not_equilibrated(trace)) { st.kind = "NotEquilibrated"; return st; }
+    if (have_topology)
+        for (auto& s : samples)
+            if (!s.fragmented.empty()) {
+                st.kind = "Fragmented"; st.has_cell = true; st.cell_id = s.fragmented[0]; st.at_mcs = s.mcs;
+                return st;
+            }
+    if (!samples.empty()) {
+        size_t window = (size_t)std::ceil((double)samples.size() * 0.5);
+        window = std::min(std::max<size_t>(window, 1), samples.size());
+        const size_t start = samples.size() - window;
+        for (int id = 1; id <= n_cells; ++id) {
+            bool all = true;
+            for (size_t k = start; k < samples.size(); ++k)
+                if (!(samples[k].cells[id - 1].volume <= c.min_cell_volume)) { all = false; break; }
+            if (all) {
+                st.kind = "CellLost"; st.has_cell = true; st.cell_id = (uint32_t)id; st.at_mcs = samples[start].mcs;
+                return st;
+            }
+        }
+    }
+    if (have_topology && n_cells >= 2 && !samples.empty()) {
+        const Sample& last = samples.back();
+        std::vector<std::vector<uint32_t>> adj(n_cells + 1);
+        std::vector<char> present(n_cells + 1, 0);
+        uint32_t start = 0;
+        for (size_t k = 0; k < last.contact_a.size(); ++k) {
+            const uint32_t a = last.contact_a[k], b = last.contact_b[k];
+            if (a == 0 || b == 0) continue;
+            adj[a].push_back(b); adj[b].push_back(a);
+            present[a] = present[b] = 1;
+            if (!start) start = a;
+        }
+        if (start) {
+            std::vector<char> vis(n_cells + 1, 0);
+            std::vector<uint32_t> stck{start};
+            vis[start] = 1;
+            size_t cnt = 1;
+            while (!stck.empty()) {
+                const uint32_t u = stck.back();
+                stck.pop_back();
+                for (uint32_t w : adj[u]) if (!vis[w]) { vis[w] = 1; ++cnt; stck.push_back(w); }
+            }
+            if (cnt == (size_t)n_cells) st.kind = "Degenerate";
+        }
+    }
+    return st;
+}
+
+// Number of energy-trace points the burn-in loop records (output.rs:441-454).
+static int trace_points(uint64_t burn_in, uint64_t interval, uint64_t start) {
+    uint64_t burned = 0;
+    int n = 0;
+    while (burned < burn_in) {
+        burned += std::min(interval, burn_in - burned);
+        if (burned >= start) ++n;
+    }
+    return n;
+}
+
+static RunPlan plan_for(const Config& c, int sim, bool write_lattice) {
+    RunPlan p;
+    std::memset(&p, 0, sizeof p);
+    p.sim = sim;
+    p.burn_in = c.burn_in;
+    p.interval = c.interval;
+    p.energy_sample_start = c.burn_in - std::min<uint64_t>(c.burn_in, (uint64_t)((double)c.burn_in * 0.25));
+    p.n_samples = (int)std::max<uint64_t>(c.readout / std::max<uint64_t>(c.interval, 1), 1);
+    p.readout_chunks = (uint64_t)p.n_samples;
+    p.write_samples = 1;
+    p.write_lattice = write_lattice ? 1 : 0;
+    return p;
+}
+
+std::string run_many(const std::vector<Config>& configs, const std::vector<Initial>& initials, const ReadoutOptions& ro,
+                     std::vector<Result>& out, int device_grid) {
+    const size_t N = configs.size();
+    out.assign(N, Result());
+    if (N == 0) return "";
+    for (auto& c : configs) {
+        if (c.acceptance != ACC_METROPOLIS) return "acceptance = metropolis_hastings is not supported by the GB300 engine";
+        if (c.proposal != PROP_UNIFORM) return "proposal = edge_list is not supported by the GB300 engine";
+        if (c.active.act) return "the Act energy term is not supported by the GB300 engine";
+    }
+    const bool snapshots = ro.include_lattice || ro.topology;
+    std::vector<RunPlan> plans(N);
+    std::vector<int> ns(N), ne(N), nt(N);
+    for (size_t i = 0; i < N; ++i) {
+        plans[i] = plan_for(configs[i], (int)i, snapshots);
+        nt[i] = trace_points(configs[i].burn_in, configs[i].interval, plans[i].energy_sample_start);
+        ns[i] = plans[i].n_samples;
+        ne[i] = nt[i] + ns[i];
+    }
+    DeviceSims dev;
+    std::string err = dev.create(configs, initials, ns, ne, snapshots);
+    if (!err.empty()) return err;
+    err = dev.run(plans, device_grid);
+    if (!err.empty()) return err;
+    err = dev.sync();
+    if (!err.empty()) return err;
+    // ---- assemble results (host threads over simulations)
+    std::atomic<size_t> next{0};
+    std::vector<std::string> errs(N);
+    auto worker = [&]() {
+        for (;;) {
+            const size_t i = next.fetch_add(1);
+            if (i >= N) return;
+            const Config& c = configs[i];
+            const SimLayout& L = dev.layout(i);
+            Result& R = out[i];
+            R.D = c.D;
+            for (int d = 0; d < c.D; ++d) R.grid.push_back(c.grid[d]);
+            R.used_default = initials[i].used_default;
+            for (auto& t : c.types) R.cell_type_names.push_back(t.name);
+            R.cell_type_index = initials[i].type_of;
+            std::vector<uint32_t> sv, si, slat;
+            std::vector<int64_t> ssp, sso;
+            std::vector<double> energy;
+            std::string e = dev.read_samples(i, ns[i], sv, si, ssp, sso, snapshots ? &slat : nullptr);
+            if (e.empty()) e = dev.read_energy(i, energy);
+            if (e.empty()) e = dev.read_stats(i, R.stats);
+            std::vector<uint32_t> fin;
+            if (e.empty()) e = dev.read_padded(i, fin);
+            if (!e.empty()) { errs[i] = e; continue; }
+            const int n = L.n_cells, D = c.D;
+            const size_t n1 = (size_t)n + 1;
+            std::vector<double> trace(energy.begin(), energy.begin() + nt[i]);
+            R.samples.resize(ns[i]);
+            for (int s = 0; s < ns[i]; ++s) {
+                Sample& S = R.samples[s];
+                S.mcs = c.burn_in + (uint64_t)(s + 1) * c.interval;
+                S.energy = energy[nt[i] + s];
+                S.cells.resize(n);
+                for (int id = 1; id <= n; ++id)
+                    cell_summary(D, (uint32_t)id, sv[s * n1 + id], si[s * n1 + id], &ssp[(s * n1 + id) * D],
+                                 &sso[(s * n1 + id) * D * D], S.cells[id - 1]);
+                if (snapshots) {
+                    std::vector<uint32_t> interior(slat.begin() + (size_t)s * L.g.n_sites,
+                                                   slat.begin() + (size_t)(s + 1) * L.g.n_sites);
+                    if (ro.topology) topology_readouts(c, L.g, pad_lattice(L.g, interior), n, S);
+                    if (ro.include_lattice) { S.lattice = std::move(interior); S.has_lattice = true; }
+                }
+            }
+            R.status = status_of(c, trace, R.samples, n, ro.topology);
+            // metadata (output.rs:66-78): hashes of the final state
+            std::vector<uint32_t> fin_int((size_t)L.g.n_sites);
+            int64_t x[3] = {0, 0, 0};
+            uint64_t occupied = 0;
+            for (int64_t q = 0; q < L.g.n_sites; ++q) {
+                fin_int[q] = fin[L.g.flat(x)];
+                for (int d = D - 1; d >= 0; --d) { if (++x[d] < L.g.dims[d]) break; x[d] = 0; }
+            }
+            std::vector<uint32_t> vol, itf;
+            std::vector<int64_t> sp, so;
+            e = dev.read_cells(i, vol, itf, sp, so);
+            if (!e.empty()) { errs[i] = e; continue; }
+            for (size_t id = 1; id < n1; ++id) occupied += vol[id];
+            R.metadata.cpm_version = "0.2.0+gb300";
+            R.metadata.convention_version = 1;
+            R.metadata.convention_hash = convention_hash(c);
+            R.metadata.model_hash = model_hash(c, fin_int, initials[i].type_of);
+            R.metadata.seed = c.seed;
+            R.metadata.seed_policy = "independent";
+            R.metadata.derived_phi = (double)(uint32_t)occupied / (double)L.g.n_sites;
+            R.metadata.theta_layout_version = 1;
+        }
+    };
+    const unsigned nthreads = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), (unsigned)N));
+    int dev_id = 0;
+    cudaGetDevice(&dev_id);
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nthreads; ++t)
+        th.emplace_back([&, dev_id] { cudaSetDevice(dev_id); worker(); });
+    for (auto& t : th) t.join();
+    for (auto& e : errs) if (!e.empty()) return e;
+    return "";
+}
+
+std::string run_one(const Config& c, const ReadoutOptions& ro, Result& out) {
+    std::string e = validate(c);
+    if (!e.empty()) return e;
+    Initial init;
+    e = initialize(c, init);
+    if (!e.empty()) return e;
+    std::vector<Result> rs;
+    e = run_many({c}, {init}, ro, rs);
+    if (!e.empty()) return e;
+    out = std::move(rs[0]);
+    return "";
+}
+
+std::string run_batch(const Config& base, const std::vector<std::vector<double>>& thetas, uint64_t master_seed,
+                      const ReadoutOptions& ro, std::vector<Result>& out) {
+    const size_t expected = theta_len(base.types.size());
+    for (size_t i = 0; i < thetas.size(); ++i)
+        if (thetas[i].size() != expected)
+            return "theta at index " + std::to_string(i) + " has length " + std::to_string(thetas[i].size()) +
+                   ", expected " + std::to_string(expected);
+    std::vector<Config> cfgs(thetas.size(), base);
+    std::vector<Initial> inits(thetas.size());
+    std::vector<std::string> errs(thetas.size());
+    std::atomic<size_t> next{0};
+    auto worker = [&]() {
+        for (;;) {
+            const size_t i = next.fetch_add(1);
+            if (i >= thetas.size()) return;
+            std::string e = theta_inject(cfgs[i], thetas[i].data());
+            if (e.empty()) { cfgs[i].seed = derive_seed_u64(master_seed, i); e = validate(cfgs[i]); }
+            if (e.empty()) e = initialize(cfgs[i], inits[i]);
+            errs[i] = e;
+        }
+    };
+    const unsigned nthreads = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), (unsigned)std::max<size_t>(thetas.size(), 1)));
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nthreads; ++t) th.emplace_back(worker);
+    for (auto& t : th) t.join();
+    for (auto& e : errs) if (!e.empty()) return e;
+    return run_many(cfgs, inits, ro, out);
+}
+
+}  // namespace cpmhost

@@ -1,0 +1,81 @@
+// Device residency for a set of simulations (internal to the library).
+//
+// `DeviceSims` owns one arena allocation holding, for every simulation, the
+// halo-padded sigma lattice, the per-cell arrays, the parameters and the
+// run-window output buffers, plus the `SimDesc` table the kernels read.
+// Lattices stay resident between calls, so `run_mcs` can be called
+// repeatedly (the reference's `run_mcs` seam) and sampling intervals never
+// re-upload state.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "cpm_common.h"
+#include "cpm_host.h"
+
+namespace cpmhost {
+
+struct SimLayout {
+    Geometry g;
+    int NE = 0;
+    int n_cells = 0;
+    int n_samples = 0;  // capacity of the sample buffers
+    int n_energy = 0;   // capacity of the energy output
+    bool lattice_samples = false;
+};
+
+class DeviceSims {
+   public:
+    DeviceSims() = default;
+    ~DeviceSims();
+    DeviceSims(const DeviceSims&) = delete;
+    DeviceSims& operator=(const DeviceSims&) = delete;
+
+    // Allocates and uploads every simulation. `n_samples[i]`/`n_energy[i]`
+    // size the output buffers of simulation i.
+    std::string create(const std::vector<Config>& configs, const std::vector<Initial>& initials,
+                       const std::vector<int>& n_samples, const std::vector<int>& n_energy, bool lattice_samples,
+                       cudaStream_t stream = 0);
+    // Runs one plan per simulation (plans[i].sim indexes this set); one
+    // persistent launch per (D, energy stencil) group.
+    std::string run(const std::vector<RunPlan>& plans, int grid_override = 0);
+    std::string sync();
+
+    size_t size() const { return layouts_.size(); }
+    const SimLayout& layout(size_t i) const { return layouts_[i]; }
+    const SimDesc& host_desc(size_t i) const { return descs_[i]; }
+    SimDesc* device_desc(size_t i) const { return d_descs_ + i; }
+    cudaStream_t stream() const { return stream_; }
+
+    // Downloads (blocking).
+    std::string read_padded(size_t i, std::vector<uint32_t>& out) const;
+    std::string read_cells(size_t i, std::vector<uint32_t>& vol, std::vector<uint32_t>& itf,
+                           std::vector<int64_t>& sp, std::vector<int64_t>& so) const;
+    std::string read_energy(size_t i, std::vector<double>& e) const;
+    std::string read_samples(size_t i, int n, std::vector<uint32_t>& vol, std::vector<uint32_t>& itf,
+                             std::vector<int64_t>& sp, std::vector<int64_t>& so, std::vector<uint32_t>* lattice) const;
+    std::string read_stats(size_t i, std::vector<uint64_t>& stats) const;
+    std::string read_mcs(size_t i, uint64_t& mcs) const;
+    // Writes sigma/V/I (harness use: set an arbitrary state).
+    std::string write_state(size_t i, const std::vector<uint32_t>& padded, const std::vector<uint32_t>& vol,
+                            const std::vector<uint32_t>& itf, const std::vector<int64_t>* sp = nullptr,
+                            const std::vector<int64_t>* so = nullptr);
+
+   private:
+    std::vector<SimLayout> layouts_;
+    std::vector<SimDesc> descs_;
+    SimDesc* d_descs_ = nullptr;
+    RunPlan* d_plans_ = nullptr;
+    int* d_next_ = nullptr;
+    size_t plans_cap_ = 0;
+    char* arena_ = nullptr;
+    cudaStream_t stream_ = 0;
+};
+
+// The 8 MiB 3D simple-point table of the current device (generated once).
+const uint64_t* device_table3d(std::string& err);
+int energy_count(int D, int kind);
+
+}  // namespace cpmhost

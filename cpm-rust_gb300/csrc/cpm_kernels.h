@@ -1,0 +1,23 @@
+// Internal interface between the host engine (cpm_engine.cpp) and the
+// sm_103a kernels (cpm_kernels.cu). Not part of the public C ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "cpm_common.h"
+
+namespace cpmgpu {
+int sweep_block();
+int sweep_max_smem_cells();
+size_t sweep_smem_bytes(int max_cells);
+cudaError_t launch_sweep(int D, int NE, SimDesc* d_sims, const RunPlan* d_plans, int n_plans, int* d_next,
+                         const uint64_t* d_t3, int max_cells, int grid, cudaStream_t st);
+cudaError_t launch_evaluate(int D, int NE, const SimDesc* d_sim, int64_t n, const int64_t* d_t, const int32_t* d_k,
+                            const double* d_u, MoveOut* d_out, const uint64_t* d_t3, cudaStream_t st);
+cudaError_t launch_commit_moves(int D, int NE, const SimDesc* d_sim, int64_t n, const int64_t* d_t,
+                                const uint32_t* d_g, cudaStream_t st);
+cudaError_t launch_recount(int D, int NE, const SimDesc* d_sim, int64_t n_sites, uint32_t* d_vol, uint32_t* d_itf,
+                           cudaStream_t st);
+cudaError_t launch_energy(int D, int NE, const SimDesc* d_sim, double* d_out, cudaStream_t st);
+cudaError_t launch_table3d(uint64_t* d_words, const uint32_t* d_face, const uint32_t* d_full, uint32_t origin_mask,
+                           cudaStream_t st);
+}  // namespace cpmgpu

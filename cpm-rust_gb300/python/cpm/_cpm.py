@@ -1,0 +1,618 @@
+"""Compiled-surface shim: the GB300 engine's ``_cpm`` module.
+
+Stands in for the reference's PyO3 extension ``cpm._cpm``
+(crates/cpm-py/src/lib.rs:85-94): the same ``CPM`` builder class with the
+same keyword arguments and return tuples (crates/cpm-py/src/builder.rs:
+104-401), and result objects with the reference's attribute names and dtypes
+(crates/cpm-py/src/convert.rs:27-256). Every call goes through the C ABI of
+``libcpm_gpu.so`` (include/cpm_gpu.h); ctypes releases the GIL for the
+duration of each foreign call, so a whole trajectory or batch runs without
+the GIL, as in the reference (builder.rs:452, 509-511).
+
+There is no CPU fallback: if the library is missing this module fails to
+import, and running without a CUDA device raises.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+__version__ = "0.2.0+gb300"
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_PKG = os.path.dirname(os.path.dirname(_HERE))
+_LIB_PATH = os.environ.get("CPM_GPU_LIB", os.path.join(_PKG, "lib", "libcpm_gpu.so"))
+
+CPM_OK = 0
+CPM_E_CONFIG = 1
+CPM_E_INIT = 2
+CPM_E_THETA = 3
+CPM_E_CUDA = 4
+CPM_E_TIMEOUT = 5
+CPM_E_BUDGET = 6
+CPM_E_ARG = 7
+CPM_E_UNSUPPORTED = 8
+
+STAT_NAMES = (
+    "attempts",
+    "nonnull",
+    "topology_rejected",
+    "guard_rejected",
+    "evaluated",
+    "accepted",
+    "rounds",
+    "passes",
+    "spin_timeouts",
+)
+
+
+class CPMRuntimeError(RuntimeError):
+    """A device-side failure (CUDA error, timeout) reported by the engine."""
+
+
+class ResultInfo(ctypes.Structure):
+    _fields_ = [
+        ("dim", ctypes.c_int32),
+        ("n_types", ctypes.c_int32),
+        ("grid", ctypes.c_int64 * 3),
+        ("n_cells", ctypes.c_uint64),
+        ("n_samples", ctypes.c_uint64),
+        ("used_default", ctypes.c_int32),
+        ("pad", ctypes.c_int32),
+    ]
+
+
+class MetadataC(ctypes.Structure):
+    _fields_ = [
+        ("cpm_version", ctypes.c_char * 32),
+        ("convention_hash", ctypes.c_char * 65),
+        ("model_hash", ctypes.c_char * 65),
+        ("seed_policy", ctypes.c_char * 32),
+        ("convention_version", ctypes.c_uint32),
+        ("theta_layout_version", ctypes.c_uint32),
+        ("seed", ctypes.c_uint64),
+        ("derived_phi", ctypes.c_double),
+    ]
+
+
+class StatusC(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_char * 24),
+        ("has_cell", ctypes.c_int32),
+        ("cell_id", ctypes.c_uint32),
+        ("at_mcs", ctypes.c_uint64),
+    ]
+
+
+class SampleSizes(ctypes.Structure):
+    _fields_ = [
+        ("n_contact", ctypes.c_uint64),
+        ("n_fragmented", ctypes.c_uint64),
+        ("n_medium", ctypes.c_uint64),
+        ("has_lattice", ctypes.c_int32),
+        ("pad", ctypes.c_int32),
+    ]
+
+
+_P = ctypes.c_void_p
+
+
+class SampleOut(ctypes.Structure):
+    _fields_ = [(name, _P) for name in (
+        "mcs", "conservative_energy", "ids", "volume", "interface", "centroid", "eigenvalues",
+        "radius_of_gyration_sq", "kappa_sq", "contact_a", "contact_b", "contact_count", "fragmented_cells",
+        "medium_component_volumes", "medium_component_touches_boundary", "lattice",
+    )]
+
+
+class SimInfo(ctypes.Structure):
+    _fields_ = [
+        ("dim", ctypes.c_int32),
+        ("periodic", ctypes.c_int32),
+        ("dims", ctypes.c_int64 * 3),
+        ("padded_dims", ctypes.c_int64 * 3),
+        ("strides", ctypes.c_int64 * 3),
+        ("n_sites", ctypes.c_uint64),
+        ("n_padded", ctypes.c_uint64),
+        ("n_cells", ctypes.c_uint64),
+        ("n_energy", ctypes.c_int32),
+        ("n_colors", ctypes.c_int32),
+    ]
+
+
+MOVE_DTYPE = np.dtype([
+    ("target_flat", np.int64), ("source_flat", np.int64), ("losing", np.uint32), ("gaining", np.uint32),
+    ("null_move", np.int32), ("topology_ok", np.int32), ("volume_guard_ok", np.int32), ("evaluated", np.int32),
+    ("delta_i_losing", np.int32), ("delta_i_gaining", np.int32), ("delta_h", np.float64), ("accepted", np.int32),
+    ("pad", np.int32),
+])
+
+# Every symbol include/cpm_gpu.h declares (checked by the CPU test suite).
+EXPORTED_SYMBOLS = (
+    "cpm_last_error", "cpm_version",
+    "cpm_builder_new", "cpm_builder_register_cell_type", "cpm_builder_add_cells", "cpm_builder_set_adhesion",
+    "cpm_builder_initialize", "cpm_builder_run", "cpm_builder_run_batch", "cpm_builder_theta_len",
+    "cpm_builder_extract_theta", "cpm_builder_theta_name", "cpm_builder_free",
+    "cpm_result_info_get", "cpm_result_metadata_get", "cpm_result_status_get", "cpm_result_cell_type_index",
+    "cpm_result_cell_type_name", "cpm_result_sample_sizes", "cpm_result_sample_read", "cpm_result_stats",
+    "cpm_result_free",
+    "cpm_engine_create", "cpm_engine_size", "cpm_engine_sim_info", "cpm_engine_run_mcs", "cpm_engine_synchronize",
+    "cpm_engine_mcs", "cpm_engine_read_lattice", "cpm_engine_read_padded", "cpm_engine_read_cells",
+    "cpm_engine_energy", "cpm_engine_recount_check", "cpm_engine_stats", "cpm_engine_write_state",
+    "cpm_engine_evaluate_moves", "cpm_engine_commit_moves", "cpm_engine_destroy",
+    "cpm_run_many",
+    "cpm_builder_initial_state", "cpm_builder_hashes", "cpm_derive_seed_u64",
+)
+
+
+def _load():
+    if not os.path.exists(_LIB_PATH):
+        raise ImportError(
+            f"libcpm_gpu.so not found at {_LIB_PATH}: build it with `python cpm-rust_gb300/build.py` "
+            "(the GB300 engine has no CPU fallback)"
+        )
+    L = ctypes.CDLL(_LIB_PATH)
+    I32, U32, U64, SZ, D = ctypes.c_int32, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_size_t, ctypes.c_double
+    L.cpm_last_error.restype = ctypes.c_char_p
+    L.cpm_last_error.argtypes = []
+    L.cpm_version.restype = ctypes.c_char_p
+    L.cpm_builder_new.argtypes = [_P, SZ, ctypes.c_char_p, U64, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p,
+                                  ctypes.c_char_p, ctypes.c_char_p, _P, _P, SZ, ctypes.POINTER(_P)]
+    L.cpm_builder_register_cell_type.argtypes = [_P, ctypes.c_char_p, U32, U32, D, D, D, U32]
+    L.cpm_builder_add_cells.argtypes = [_P, ctypes.c_char_p, U64]
+    L.cpm_builder_set_adhesion.argtypes = [_P, _P, _P, SZ]
+    L.cpm_builder_initialize.argtypes = [_P, _P, SZ, _P, SZ, I32, I32]
+    L.cpm_builder_run.argtypes = [_P, U64, U64, U64, I32, ctypes.POINTER(I32), ctypes.POINTER(_P)]
+    L.cpm_builder_run_batch.argtypes = [_P, _P, _P, SZ, U64, U64, U64, U64, I32, ctypes.POINTER(I32), _P]
+    L.cpm_builder_theta_len.argtypes = [_P, ctypes.POINTER(SZ)]
+    L.cpm_builder_extract_theta.argtypes = [_P, _P, SZ]
+    L.cpm_builder_theta_name.argtypes = [_P, SZ, ctypes.c_char_p, SZ]
+    L.cpm_builder_free.argtypes = [_P]
+    L.cpm_builder_free.restype = None
+    L.cpm_result_info_get.argtypes = [_P, ctypes.POINTER(ResultInfo)]
+    L.cpm_result_metadata_get.argtypes = [_P, ctypes.POINTER(MetadataC)]
+    L.cpm_result_status_get.argtypes = [_P, ctypes.POINTER(StatusC)]
+    L.cpm_result_cell_type_index.argtypes = [_P, _P]
+    L.cpm_result_cell_type_name.argtypes = [_P, SZ, ctypes.c_char_p, SZ]
+    L.cpm_result_sample_sizes.argtypes = [_P, SZ, ctypes.POINTER(SampleSizes)]
+    L.cpm_result_sample_read.argtypes = [_P, SZ, ctypes.POINTER(SampleOut)]
+    L.cpm_result_stats.argtypes = [_P, _P]
+    L.cpm_result_free.argtypes = [_P]
+    L.cpm_result_free.restype = None
+    L.cpm_engine_create.argtypes = [_P, SZ, _P, ctypes.POINTER(_P)]
+    L.cpm_engine_size.argtypes = [_P, ctypes.POINTER(SZ)]
+    L.cpm_engine_sim_info.argtypes = [_P, SZ, ctypes.POINTER(SimInfo)]
+    L.cpm_engine_run_mcs.argtypes = [_P, U64]
+    L.cpm_engine_synchronize.argtypes = [_P]
+    L.cpm_engine_mcs.argtypes = [_P, SZ, ctypes.POINTER(U64)]
+    L.cpm_engine_read_lattice.argtypes = [_P, SZ, _P]
+    L.cpm_engine_read_padded.argtypes = [_P, SZ, _P]
+    L.cpm_engine_read_cells.argtypes = [_P, SZ, _P, _P, _P, _P]
+    L.cpm_engine_energy.argtypes = [_P, SZ, ctypes.POINTER(D)]
+    L.cpm_engine_recount_check.argtypes = [_P, SZ, ctypes.POINTER(I32), _P, _P]
+    L.cpm_engine_stats.argtypes = [_P, SZ, _P]
+    L.cpm_engine_write_state.argtypes = [_P, SZ, _P, _P, _P, _P, _P]
+    L.cpm_engine_evaluate_moves.argtypes = [_P, SZ, SZ, _P, _P, _P, _P]
+    L.cpm_engine_commit_moves.argtypes = [_P, SZ, SZ, _P, _P]
+    L.cpm_engine_destroy.argtypes = [_P]
+    L.cpm_engine_destroy.restype = None
+    L.cpm_run_many.argtypes = [_P, SZ, U64, U64, U64, I32, I32, _P]
+    L.cpm_builder_initial_state.argtypes = [_P, _P, SZ, _P, ctypes.POINTER(SZ), ctypes.POINTER(I32)]
+    L.cpm_builder_hashes.argtypes = [_P, U64, U64, U64, _P, SZ, _P, SZ, ctypes.c_char_p, ctypes.c_char_p]
+    L.cpm_derive_seed_u64.argtypes = [U64, U64]
+    L.cpm_derive_seed_u64.restype = U64
+    return L
+
+
+_lib = _load()
+LIB_PATH = _LIB_PATH
+
+
+def lib():
+    return _lib
+
+
+def _check(rc: int):
+    if rc == CPM_OK:
+        return
+    msg = (_lib.cpm_last_error() or b"").decode("utf-8", "replace")
+    if rc in (CPM_E_CONFIG, CPM_E_INIT, CPM_E_THETA, CPM_E_ARG, CPM_E_UNSUPPORTED, CPM_E_BUDGET):
+        raise ValueError(msg)
+    raise CPMRuntimeError(msg)
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(_P)
+
+
+def _u64(x, name):
+    x = int(x)
+    if x < 0 or x >= 2**64:
+        raise OverflowError(f"{name}: can't convert {x} to an unsigned 64-bit integer")
+    return x
+
+
+def _u32(x, name):
+    x = int(x)
+    if x < 0 or x >= 2**32:
+        raise OverflowError(f"{name}: can't convert {x} to an unsigned 32-bit integer")
+    return x
+
+
+def _enc(s):
+    return None if s is None else str(s).encode("utf-8")
+
+
+# ----------------------------------------------------------------- results
+class RunMetadata:
+    """PyRunMetadata (convert.rs:27-38)."""
+
+    __slots__ = ("cpm_version", "convention_version", "convention_hash", "model_hash", "seed", "seed_policy",
+                 "derived_phi", "theta_layout_version")
+
+    def __repr__(self):
+        return f"RunMetadata(seed={self.seed}, convention_hash={self.convention_hash!r})"
+
+
+class Status:
+    """PyStatus (convert.rs:40-52): kind plus cell_id/at_mcs for CellLost/Fragmented."""
+
+    __slots__ = ("kind", "cell_id", "at_mcs")
+
+    def __repr__(self):
+        return f"Status(kind={self.kind!r}, cell_id={self.cell_id}, at_mcs={self.at_mcs})"
+
+
+class Sample:
+    """PySample (convert.rs:54-95). ``contact`` is the dense
+    ``(n_cells+1, n_cells+1)`` upper-triangular uint32 matrix, built from the
+    engine's sparse pairs on first access."""
+
+    __slots__ = ("mcs", "conservative_energy", "ids", "volume", "interface", "centroid", "eigenvalues",
+                 "radius_of_gyration_sq", "kappa_sq", "fragmented_cells", "medium_component_volumes",
+                 "medium_component_touches_boundary", "lattice", "_contact_pairs", "_contact")
+
+    @property
+    def contact(self):
+        if self._contact is None:
+            a, b, n = self._contact_pairs
+            m = np.zeros((len(self.ids) + 1, len(self.ids) + 1), dtype=np.uint32)
+            m[a.astype(np.int64), b.astype(np.int64)] = n
+            self._contact = m
+        return self._contact
+
+    @property
+    def contact_pairs(self):
+        """Sparse form of ``contact``: (a, b, count) arrays with a < b."""
+        return self._contact_pairs
+
+
+class RunResult:
+    """PyRunResult (convert.rs:97-115)."""
+
+    __slots__ = ("metadata", "status", "samples", "cell_type_index", "cell_type_names", "stats")
+
+
+def _result_from_handle(h) -> RunResult:
+    try:
+        info = ResultInfo()
+        _check(_lib.cpm_result_info_get(h, ctypes.byref(info)))
+        D, n = info.dim, int(info.n_cells)
+        grid = tuple(int(info.grid[d]) for d in range(D))
+        md = MetadataC()
+        _check(_lib.cpm_result_metadata_get(h, ctypes.byref(md)))
+        meta = RunMetadata()
+        meta.cpm_version = md.cpm_version.decode()
+        meta.convention_version = int(md.convention_version)
+        meta.convention_hash = md.convention_hash.decode()
+        meta.model_hash = md.model_hash.decode()
+        meta.seed = int(md.seed)
+        meta.seed_policy = md.seed_policy.decode()
+        meta.derived_phi = float(md.derived_phi)
+        meta.theta_layout_version = int(md.theta_layout_version)
+        st = StatusC()
+        _check(_lib.cpm_result_status_get(h, ctypes.byref(st)))
+        status = Status()
+        status.kind = st.kind.decode()
+        status.cell_id = int(st.cell_id) if st.has_cell else None
+        status.at_mcs = int(st.at_mcs) if st.has_cell else None
+        cti = np.zeros(n, dtype=np.uint32)
+        _check(_lib.cpm_result_cell_type_index(h, _ptr(cti)))
+        names = []
+        buf = ctypes.create_string_buffer(4096)
+        for t in range(info.n_types):
+            _check(_lib.cpm_result_cell_type_name(h, t, buf, 4096))
+            names.append(buf.value.decode("utf-8"))
+        stats = np.zeros(16, dtype=np.uint64)
+        _check(_lib.cpm_result_stats(h, _ptr(stats)))
+        samples = []
+        for s in range(int(info.n_samples)):
+            sz = SampleSizes()
+            _check(_lib.cpm_result_sample_sizes(h, s, ctypes.byref(sz)))
+            mcs = np.zeros(1, dtype=np.uint64)
+            en = np.zeros(1, dtype=np.float64)
+            ids = np.zeros(n, dtype=np.uint32)
+            vol = np.zeros(n, dtype=np.uint32)
+            itf = np.zeros(n, dtype=np.uint32)
+            cen = np.zeros((n, D), dtype=np.float64)
+            eig = np.zeros((n, D), dtype=np.float64)
+            rg2 = np.zeros(n, dtype=np.float64)
+            k2 = np.zeros(n, dtype=np.float64)
+            ca = np.zeros(int(sz.n_contact), dtype=np.uint32)
+            cb = np.zeros(int(sz.n_contact), dtype=np.uint32)
+            cn = np.zeros(int(sz.n_contact), dtype=np.uint32)
+            fr = np.zeros(int(sz.n_fragmented), dtype=np.uint32)
+            mv = np.zeros(int(sz.n_medium), dtype=np.uint32)
+            mt = np.zeros(int(sz.n_medium), dtype=np.uint8)
+            lat = np.zeros(grid, dtype=np.uint32) if sz.has_lattice else None
+            o = SampleOut()
+            for name, arr in (("mcs", mcs), ("conservative_energy", en), ("ids", ids), ("volume", vol),
+                              ("interface", itf), ("centroid", cen), ("eigenvalues", eig),
+                              ("radius_of_gyration_sq", rg2), ("kappa_sq", k2), ("contact_a", ca),
+                              ("contact_b", cb), ("contact_count", cn), ("fragmented_cells", fr),
+                              ("medium_component_volumes", mv), ("medium_component_touches_boundary", mt)):
+                setattr(o, name, arr.ctypes.data if arr.size else None)
+            o.lattice = lat.ctypes.data if lat is not None else None
+            _check(_lib.cpm_result_sample_read(h, s, ctypes.byref(o)))
+            smp = Sample()
+            smp.mcs = int(mcs[0])
+            smp.conservative_energy = float(en[0])
+            smp.ids, smp.volume, smp.interface = ids, vol, itf
+            smp.centroid, smp.eigenvalues = cen, eig
+            smp.radius_of_gyration_sq, smp.kappa_sq = rg2, k2
+            smp.fragmented_cells = fr.tolist()
+            smp.medium_component_volumes = mv.tolist()
+            smp.medium_component_touches_boundary = [bool(x) for x in mt]
+            smp.lattice = lat
+            smp._contact_pairs = (ca, cb, cn)
+            smp._contact = None
+            samples.append(smp)
+        r = RunResult()
+        r.metadata, r.status, r.samples = meta, status, samples
+        r.cell_type_index, r.cell_type_names = cti, names
+        r.stats = {name: int(stats[i]) for i, name in enumerate(STAT_NAMES)}
+        return r
+    finally:
+        _lib.cpm_result_free(h)
+
+
+# ----------------------------------------------------------------- builder
+class CPM:
+    """The compiled builder (builder.rs:104-401), backed by libcpm_gpu.so."""
+
+    def __init__(self, grid, boundary, seed, copy_neighborhood="von_neumann", energy_neighborhood=None,
+                 connectivity_neighborhood="von_neumann", acceptance=None, proposal=None, active_terms=None):
+        g = np.ascontiguousarray([_u64(x, "grid") for x in grid], dtype=np.uint64)
+        keys, vals = [], []
+        for k, v in (active_terms or {}).items():
+            keys.append(str(k).encode("utf-8"))
+            vals.append(1 if v else 0)
+        karr = (ctypes.c_char_p * max(len(keys), 1))(*keys) if keys else None
+        varr = np.ascontiguousarray(vals, dtype=np.int32) if vals else None
+        h = _P()
+        self._h = None
+        _check(_lib.cpm_builder_new(
+            _ptr(g) if g.size else None, g.size, _enc(boundary), _u64(seed, "seed"), _enc(copy_neighborhood),
+            _enc(energy_neighborhood), _enc(connectivity_neighborhood), _enc(acceptance), _enc(proposal),
+            ctypes.cast(karr, _P) if karr is not None else None, _ptr(varr) if varr is not None else None,
+            len(keys), ctypes.byref(h)))
+        self._h = h
+        self._grid = tuple(int(x) for x in grid)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            _lib.cpm_builder_free(h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def register_cell_type(self, name, target_volume, target_interface, lambda_volume, lambda_interface,
+                           lambda_act=0.0, max_act=0):
+        _check(_lib.cpm_builder_register_cell_type(
+            self._h, _enc(name), _u32(target_volume, "target_volume"), _u32(target_interface, "target_interface"),
+            float(lambda_volume), float(lambda_interface), float(lambda_act), _u32(max_act, "max_act")))
+
+    def add_cells(self, cell_type, n):
+        _check(_lib.cpm_builder_add_cells(self._h, _enc(cell_type), _u64(n, "n")))
+
+    def set_adhesion(self, matrix):
+        rows = [[float(x) for x in row] for row in matrix]
+        lens = np.ascontiguousarray([len(r) for r in rows], dtype=np.uintp)
+        vals = np.ascontiguousarray([x for r in rows for x in r], dtype=np.float64)
+        _check(_lib.cpm_builder_set_adhesion(self._h, _ptr(vals) if vals.size else None,
+                                             _ptr(lens) if lens.size else None, len(rows)))
+
+    def initialize(self, lattice=None, cell_type_of=None, warn_on_default_init=True):
+        if lattice is not None:
+            lat = np.ascontiguousarray([_u32(x, "lattice") for x in lattice], dtype=np.uint32)
+            has = cell_type_of is not None
+            cto = np.ascontiguousarray([_u64(x, "cell_type_of") for x in (cell_type_of or [])], dtype=np.uint64)
+            _check(_lib.cpm_builder_initialize(self._h, _ptr(lat) if lat.size else _ptr(np.zeros(1, np.uint32)),
+                                               lat.size, _ptr(cto) if cto.size else None, cto.size, int(has),
+                                               int(bool(warn_on_default_init))))
+        else:
+            _check(_lib.cpm_builder_initialize(self._h, None, 0, None, 0, 0, int(bool(warn_on_default_init))))
+
+    def run(self, burn_in_mcs, readout_mcs, sampling_interval_mcs, include_lattice=False):
+        used = ctypes.c_int32(0)
+        h = _P()
+        _check(_lib.cpm_builder_run(self._h, _u64(burn_in_mcs, "burn_in_mcs"), _u64(readout_mcs, "readout_mcs"),
+                                    _u64(sampling_interval_mcs, "sampling_interval_mcs"), int(bool(include_lattice)),
+                                    ctypes.byref(used), ctypes.byref(h)))
+        return bool(used.value), _result_from_handle(h)
+
+    def run_batch(self, thetas, burn_in_mcs, readout_mcs, sampling_interval_mcs, master_seed, include_lattice=False):
+        rows = [[float(x) for x in th] for th in thetas]
+        lens = np.ascontiguousarray([len(r) for r in rows], dtype=np.uintp)
+        vals = np.ascontiguousarray([x for r in rows for x in r], dtype=np.float64)
+        out = (_P * max(len(rows), 1))()
+        anyd = ctypes.c_int32(0)
+        _check(_lib.cpm_builder_run_batch(
+            self._h, _ptr(vals) if vals.size else None, _ptr(lens) if lens.size else None, len(rows),
+            _u64(burn_in_mcs, "burn_in_mcs"), _u64(readout_mcs, "readout_mcs"),
+            _u64(sampling_interval_mcs, "sampling_interval_mcs"), _u64(master_seed, "master_seed"),
+            int(bool(include_lattice)), ctypes.byref(anyd), ctypes.cast(out, _P)))
+        return bool(anyd.value), [_result_from_handle(_P(out[i])) for i in range(len(rows))]
+
+    def initial_state(self):
+        """Host-only placement (no device work): (lattice, cell_type_of, used_default)."""
+        n_sites = int(np.prod(self._grid))
+        lat = np.zeros(n_sites, dtype=np.uint32)
+        n = ctypes.c_size_t(0)
+        used = ctypes.c_int32(0)
+        _check(_lib.cpm_builder_initial_state(self._h, _ptr(lat), n_sites, None, ctypes.byref(n), ctypes.byref(used)))
+        cap = ctypes.c_size_t(n.value)
+        cto = np.zeros(max(n.value, 1), dtype=np.uint32)
+        _check(_lib.cpm_builder_initial_state(self._h, _ptr(lat), n_sites, _ptr(cto), ctypes.byref(cap),
+                                              ctypes.byref(used)))
+        return lat.reshape(self._grid), cto[: n.value], bool(used.value)
+
+    def hashes(self, burn_in_mcs, readout_mcs, sampling_interval_mcs, lattice, cell_type_of):
+        """(convention_hash, model_hash) for the given windows and lattice."""
+        lat = np.ascontiguousarray(np.asarray(lattice, dtype=np.uint32).ravel())
+        cto = np.ascontiguousarray(np.asarray(cell_type_of, dtype=np.uint32))
+        ch = ctypes.create_string_buffer(65)
+        mh = ctypes.create_string_buffer(65)
+        _check(_lib.cpm_builder_hashes(self._h, burn_in_mcs, readout_mcs, sampling_interval_mcs, _ptr(lat), lat.size,
+                                       _ptr(cto) if cto.size else None, cto.size, ch, mh))
+        return ch.value.decode(), mh.value.decode()
+
+    def theta_names(self):
+        n = ctypes.c_size_t(0)
+        _check(_lib.cpm_builder_theta_len(self._h, ctypes.byref(n)))
+        buf = ctypes.create_string_buffer(4096)
+        names = []
+        for i in range(n.value):
+            _check(_lib.cpm_builder_theta_name(self._h, i, buf, 4096))
+            names.append(buf.value.decode("utf-8"))
+        return names
+
+    def extract_theta(self):
+        n = ctypes.c_size_t(0)
+        _check(_lib.cpm_builder_theta_len(self._h, ctypes.byref(n)))
+        out = np.zeros(n.value, dtype=np.float64)
+        _check(_lib.cpm_builder_extract_theta(self._h, _ptr(out), n.value))
+        return out.tolist()
+
+
+def derive_seed_u64(master_seed: int, index: int) -> int:
+    return int(_lib.cpm_derive_seed_u64(_u64(master_seed, "master_seed"), _u64(index, "index")))
+
+
+def run_many(builders, burn_in_mcs, readout_mcs, sampling_interval_mcs, include_lattice=False, topology=True):
+    """Runs one simulation per builder (each with its own grid, parameters and
+    seed) in one persistent device launch; see ``cpm_run_many``."""
+    hs = (_P * max(len(builders), 1))(*[b.handle for b in builders])
+    out = (_P * max(len(builders), 1))()
+    _check(_lib.cpm_run_many(ctypes.cast(hs, _P), len(builders), _u64(burn_in_mcs, "burn_in_mcs"),
+                             _u64(readout_mcs, "readout_mcs"), _u64(sampling_interval_mcs, "sampling_interval_mcs"),
+                             int(bool(include_lattice)), int(bool(topology)), ctypes.cast(out, _P)))
+    return [_result_from_handle(_P(out[i])) for i in range(len(builders))]
+
+
+class Engine:
+    """Device-resident simulations driven MCS by MCS (the run_mcs seam)."""
+
+    def __init__(self, builders, stream=None):
+        if isinstance(builders, CPM):
+            builders = [builders]
+        self._builders = list(builders)
+        hs = (_P * len(self._builders))(*[b.handle for b in self._builders])
+        h = _P()
+        self._h = None
+        _check(_lib.cpm_engine_create(ctypes.cast(hs, _P), len(self._builders),
+                                      _P(stream) if stream else None, ctypes.byref(h)))
+        self._h = h
+        self.info = []
+        for i in range(len(self._builders)):
+            si = SimInfo()
+            _check(_lib.cpm_engine_sim_info(self._h, i, ctypes.byref(si)))
+            self.info.append(si)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            _lib.cpm_engine_destroy(h)
+            self._h = None
+
+    def __len__(self):
+        return len(self.info)
+
+    def run_mcs(self, n: int):
+        _check(_lib.cpm_engine_run_mcs(self._h, _u64(n, "n")))
+
+    def synchronize(self):
+        _check(_lib.cpm_engine_synchronize(self._h))
+
+    def mcs(self, i=0):
+        v = ctypes.c_uint64(0)
+        _check(_lib.cpm_engine_mcs(self._h, i, ctypes.byref(v)))
+        return v.value
+
+    def lattice(self, i=0):
+        si = self.info[i]
+        out = np.zeros(int(si.n_sites), dtype=np.uint32)
+        _check(_lib.cpm_engine_read_lattice(self._h, i, _ptr(out)))
+        return out.reshape([int(si.dims[d]) for d in range(si.dim)])
+
+    def padded(self, i=0):
+        out = np.zeros(int(self.info[i].n_padded), dtype=np.uint32)
+        _check(_lib.cpm_engine_read_padded(self._h, i, _ptr(out)))
+        return out
+
+    def cells(self, i=0):
+        si = self.info[i]
+        n1, D = int(si.n_cells) + 1, si.dim
+        v = np.zeros(n1, np.uint32)
+        it = np.zeros(n1, np.uint32)
+        sp = np.zeros(n1 * D, np.int64)
+        so = np.zeros(n1 * D * D, np.int64)
+        _check(_lib.cpm_engine_read_cells(self._h, i, _ptr(v), _ptr(it), _ptr(sp), _ptr(so)))
+        return v, it, sp.reshape(n1, D), so.reshape(n1, D, D)
+
+    def energy(self, i=0):
+        e = ctypes.c_double(0.0)
+        _check(_lib.cpm_engine_energy(self._h, i, ctypes.byref(e)))
+        return e.value
+
+    def recount_check(self, i=0):
+        n1 = int(self.info[i].n_cells) + 1
+        okv = ctypes.c_int32(0)
+        v = np.zeros(n1, np.uint32)
+        it = np.zeros(n1, np.uint32)
+        _check(_lib.cpm_engine_recount_check(self._h, i, ctypes.byref(okv), _ptr(v), _ptr(it)))
+        return bool(okv.value), v, it
+
+    def stats(self, i=0):
+        s = np.zeros(16, np.uint64)
+        _check(_lib.cpm_engine_stats(self._h, i, _ptr(s)))
+        return {name: int(s[k]) for k, name in enumerate(STAT_NAMES)}
+
+    def write_state(self, padded, volume, interface, sum_position=None, sum_outer=None, i=0):
+        p = np.ascontiguousarray(padded, dtype=np.uint32)
+        v = np.ascontiguousarray(volume, dtype=np.uint32)
+        it = np.ascontiguousarray(interface, dtype=np.uint32)
+        sp = np.ascontiguousarray(sum_position, dtype=np.int64) if sum_position is not None else None
+        so = np.ascontiguousarray(sum_outer, dtype=np.int64) if sum_outer is not None else None
+        _check(_lib.cpm_engine_write_state(self._h, i, _ptr(p), _ptr(v), _ptr(it),
+                                           _ptr(sp) if sp is not None else None,
+                                           _ptr(so) if so is not None else None))
+
+    def evaluate_moves(self, target, k, u, i=0):
+        t = np.ascontiguousarray(target, dtype=np.int64)
+        kk = np.ascontiguousarray(k, dtype=np.int32)
+        uu = np.ascontiguousarray(u, dtype=np.float64)
+        out = np.zeros(t.size, dtype=MOVE_DTYPE)
+        _check(_lib.cpm_engine_evaluate_moves(self._h, i, t.size, _ptr(t), _ptr(kk), _ptr(uu), _ptr(out)))
+        return out
+
+    def commit_moves(self, target, gaining, i=0):
+        t = np.ascontiguousarray(target, dtype=np.int64)
+        g = np.ascontiguousarray(gaining, dtype=np.uint32)
+        _check(_lib.cpm_engine_commit_moves(self._h, i, t.size, _ptr(t), _ptr(g)))

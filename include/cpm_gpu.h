@@ -1,0 +1,253 @@
+/*
+ * cpm_gpu.h — C ABI of the GB300 Cellular Potts engine (libcpm_gpu.so).
+ *
+ * Drop-in boundary for DebajyotiS/cpm-rust. The reference crosses its only
+ * FFI boundary once per call, from Python into Rust through PyO3
+ * (crates/cpm-py/src/builder.rs:104-401, convert.rs:27-256); this header is
+ * the same surface as plain C: a builder that accumulates the configuration
+ * exactly like the PyO3 pyclass `CPM`, run / run_batch calls that execute a
+ * whole trajectory per call, opaque results with accessors, and the
+ * hot-path seam (`monte_carlo::run_mcs`, crates/cpm-core/src/monte_carlo.rs:
+ * 327-357) for callers that drive the lattice themselves.
+ *
+ * Conventions: every function returns CPM_OK (0) or a CPM_E_* code; the
+ * message of the last failure on the calling thread is cpm_last_error().
+ * Configuration, initialisation and theta messages are the reference's own
+ * texts (config.rs:287-413, initialization.rs:61-277, theta.rs:93-147,
+ * batch.rs:26-45, builder.rs:35-96). The caller owns every buffer it passes;
+ * the library keeps no caller pointer after a call returns. Objects are not
+ * internally synchronised: use one object per thread.
+ */
+#ifndef CPM_GPU_H
+#define CPM_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CPM_OK 0
+#define CPM_E_CONFIG 1      /* ConfigError / CellTypeError / parse errors (-> ValueError) */
+#define CPM_E_INIT 2        /* InitError (-> ValueError) */
+#define CPM_E_THETA 3       /* BatchError::WrongThetaLength / ThetaError (-> ValueError) */
+#define CPM_E_CUDA 4        /* a CUDA call failed; see cpm_last_error() */
+#define CPM_E_TIMEOUT 5     /* a bounded device or host wait gave up */
+#define CPM_E_BUDGET 6      /* serving admission: request exceeds the HBM budget */
+#define CPM_E_ARG 7         /* invalid argument (null pointer, index out of range, short buffer) */
+#define CPM_E_UNSUPPORTED 8 /* valid reference configuration the GB300 engine does not run */
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* cpm_last_error(void);
+/* Library version string, e.g. "0.2.0+gb300". */
+const char* cpm_version(void);
+
+/* ------------------------------------------------------------ builder ---
+ * Replaces the PyO3 pyclass `CPM` (crates/cpm-py/src/builder.rs:104-401). */
+typedef struct cpm_builder cpm_builder;
+
+/* builder.rs:117-195 (`CPM.__new__`). energy_neighborhood, acceptance and
+ * proposal may be NULL (resolved defaults). active_term_keys/values may be
+ * NULL with n_active_terms = 0. */
+int cpm_builder_new(const uint64_t* grid, size_t grid_len, const char* boundary, uint64_t seed,
+                    const char* copy_neighborhood, const char* energy_neighborhood,
+                    const char* connectivity_neighborhood, const char* acceptance, const char* proposal,
+                    const char* const* active_term_keys, const int32_t* active_term_values, size_t n_active_terms,
+                    cpm_builder** out);
+/* builder.rs:197-241 */
+int cpm_builder_register_cell_type(cpm_builder* b, const char* name, uint32_t target_volume,
+                                   uint32_t target_interface, double lambda_volume, double lambda_interface,
+                                   double lambda_act, uint32_t max_act);
+/* builder.rs:243-254 */
+int cpm_builder_add_cells(cpm_builder* b, const char* cell_type, uint64_t n);
+/* builder.rs:256-262: row-major values of n_rows rows with the given lengths
+ * (ragged rows are accepted here and rejected by validation at run time). */
+int cpm_builder_set_adhesion(cpm_builder* b, const double* values, const size_t* row_lengths, size_t n_rows);
+/* builder.rs:270-296: lattice == NULL selects the default scatter-and-grow. */
+int cpm_builder_initialize(cpm_builder* b, const uint32_t* lattice, size_t lattice_len,
+                           const uint64_t* cell_type_of, size_t cell_type_of_len, int32_t has_cell_type_of,
+                           int32_t warn_on_default_init);
+typedef struct cpm_result cpm_result;
+/* builder.rs:304-333 + 432-474: resolve, validate, place, burn in, read out.
+ * *used_default reports whether scatter-and-grow placement was used. */
+int cpm_builder_run(const cpm_builder* b, uint64_t burn_in_mcs, uint64_t readout_mcs, uint64_t sampling_interval_mcs,
+                    int32_t include_lattice, int32_t* used_default, cpm_result** out);
+/* builder.rs:342-381 + 485-525 and batch.rs:110-153: thetas are
+ * concatenated, theta i has theta_lengths[i] entries; per-simulation seeds
+ * are derive_seed_u64(master_seed, i). out must hold n_thetas pointers. All
+ * simulations run in one persistent device launch. */
+int cpm_builder_run_batch(const cpm_builder* b, const double* thetas, const size_t* theta_lengths, size_t n_thetas,
+                          uint64_t burn_in_mcs, uint64_t readout_mcs, uint64_t sampling_interval_mcs,
+                          uint64_t master_seed, int32_t include_lattice, int32_t* any_used_default, cpm_result** out);
+/* builder.rs:386-430 (theta.rs:43-178) */
+int cpm_builder_theta_len(const cpm_builder* b, size_t* out);
+int cpm_builder_extract_theta(const cpm_builder* b, double* out, size_t capacity);
+int cpm_builder_theta_name(const cpm_builder* b, size_t index, char* buf, size_t capacity);
+void cpm_builder_free(cpm_builder* b);
+
+/* ------------------------------------------------------------ results ---
+ * Replaces PyRunResult / PySample / PyRunMetadata / PyStatus
+ * (crates/cpm-py/src/convert.rs:27-256). */
+typedef struct {
+    int32_t dim;
+    int32_t n_types;
+    int64_t grid[3];
+    uint64_t n_cells;
+    uint64_t n_samples;
+    int32_t used_default;
+    int32_t pad;
+} cpm_result_info;
+
+typedef struct {
+    char cpm_version[32];
+    char convention_hash[65];
+    char model_hash[65];
+    char seed_policy[32];
+    uint32_t convention_version;
+    uint32_t theta_layout_version;
+    uint64_t seed;
+    double derived_phi;
+} cpm_metadata;
+
+typedef struct {
+    char kind[24]; /* "Ok", "CellLost", "Fragmented", "NotEquilibrated", "Degenerate" */
+    int32_t has_cell;
+    uint32_t cell_id;
+    uint64_t at_mcs;
+} cpm_status;
+
+typedef struct {
+    uint64_t n_contact;   /* nonzero contact pairs (a < b) */
+    uint64_t n_fragmented;
+    uint64_t n_medium;    /* medium components */
+    int32_t has_lattice;
+    int32_t pad;
+} cpm_sample_sizes;
+
+/* Caller-owned destination buffers for one sample; any pointer may be NULL
+ * to skip that field. Per-cell arrays have n_cells rows in id order. */
+typedef struct {
+    uint64_t* mcs;
+    double* conservative_energy;
+    uint32_t* ids;
+    uint32_t* volume;
+    uint32_t* interface;
+    double* centroid;      /* n_cells x dim */
+    double* eigenvalues;   /* n_cells x dim, descending */
+    double* radius_of_gyration_sq;
+    double* kappa_sq;
+    uint32_t* contact_a;   /* n_contact; canonical (min, max) pairs, medium = 0 */
+    uint32_t* contact_b;
+    uint32_t* contact_count;
+    uint32_t* fragmented_cells;
+    uint32_t* medium_component_volumes;
+    uint8_t* medium_component_touches_boundary;
+    uint32_t* lattice;     /* product(grid), row-major; only if has_lattice */
+} cpm_sample_out;
+
+int cpm_result_info_get(const cpm_result* r, cpm_result_info* out);
+int cpm_result_metadata_get(const cpm_result* r, cpm_metadata* out);
+int cpm_result_status_get(const cpm_result* r, cpm_status* out);
+int cpm_result_cell_type_index(const cpm_result* r, uint32_t* out /* n_cells */);
+int cpm_result_cell_type_name(const cpm_result* r, size_t type_index, char* buf, size_t capacity);
+int cpm_result_sample_sizes(const cpm_result* r, size_t sample, cpm_sample_sizes* out);
+int cpm_result_sample_read(const cpm_result* r, size_t sample, const cpm_sample_out* out);
+/* Device counters of the run (CPM_STAT_* order: attempts, non-null,
+ * topology rejections, guard rejections, evaluated, accepted, conflict
+ * rounds, colour passes, ...); out holds 16 values. */
+int cpm_result_stats(const cpm_result* r, uint64_t* out16);
+void cpm_result_free(cpm_result* r);
+
+/* --------------------------------------------------- hot-path engine ---
+ * The seam the kernels replace: monte_carlo::run_mcs (monte_carlo.rs:
+ * 327-357) on device-resident lattices. An engine holds one or more
+ * simulations, each built and placed from a builder (its grid, types,
+ * adhesion, seed and initialisation); `run_mcs` advances every simulation
+ * by n MCS in one persistent launch. Per-cell arrays are indexed by cell id
+ * (n_cells + 1 entries, entry 0 = medium). */
+typedef struct cpm_engine cpm_engine;
+
+typedef struct {
+    int32_t dim;
+    int32_t periodic;
+    int64_t dims[3];
+    int64_t padded_dims[3];
+    int64_t strides[3];
+    uint64_t n_sites;
+    uint64_t n_padded;
+    uint64_t n_cells;
+    int32_t n_energy;   /* energy-neighbourhood size */
+    int32_t n_colors;   /* checkerboard colours per MCS */
+} cpm_sim_info;
+
+/* Per-move parity record (monte_carlo.rs:52-145 decided with explicit
+ * draws): k indexes the von Neumann copy stencil, u is the uniform draw used
+ * when delta_h > 0. */
+typedef struct {
+    int64_t target_flat, source_flat;
+    uint32_t losing, gaining;
+    int32_t null_move, topology_ok, volume_guard_ok, evaluated;
+    int32_t delta_i_losing, delta_i_gaining;
+    double delta_h;
+    int32_t accepted;
+    int32_t pad;
+} cpm_move;
+
+/* stream: a cudaStream_t to launch on, or NULL for the default stream. */
+int cpm_engine_create(const cpm_builder* const* builders, size_t n, void* stream, cpm_engine** out);
+int cpm_engine_size(const cpm_engine* e, size_t* out);
+int cpm_engine_sim_info(const cpm_engine* e, size_t sim, cpm_sim_info* out);
+/* Advance every simulation by n_mcs MCS (asynchronous on the engine stream). */
+int cpm_engine_run_mcs(cpm_engine* e, uint64_t n_mcs);
+int cpm_engine_synchronize(cpm_engine* e);
+int cpm_engine_mcs(const cpm_engine* e, size_t sim, uint64_t* out);
+int cpm_engine_read_lattice(const cpm_engine* e, size_t sim, uint32_t* out /* n_sites */);
+int cpm_engine_read_padded(const cpm_engine* e, size_t sim, uint32_t* out /* n_padded */);
+int cpm_engine_read_cells(const cpm_engine* e, size_t sim, uint32_t* volume, uint32_t* interface, int64_t* sum_position,
+                          int64_t* sum_position_outer);
+/* Global energy of the current state (energy.rs:104-308), computed on the device. */
+int cpm_engine_energy(const cpm_engine* e, size_t sim, double* out);
+/* Full recount of volume and interface from the lattice on the device
+ * (checker.rs:36-83); *ok = 1 iff it equals the incrementally kept state. */
+int cpm_engine_recount_check(const cpm_engine* e, size_t sim, int32_t* ok, uint32_t* volume, uint32_t* interface);
+int cpm_engine_stats(const cpm_engine* e, size_t sim, uint64_t* out16);
+/* Parity harness: overwrite the dynamic state, decide moves without
+ * committing them, or apply moves in order with the sweep's commit. */
+int cpm_engine_write_state(cpm_engine* e, size_t sim, const uint32_t* padded, const uint32_t* volume,
+                           const uint32_t* interface, const int64_t* sum_position, const int64_t* sum_position_outer);
+int cpm_engine_evaluate_moves(cpm_engine* e, size_t sim, size_t n, const int64_t* target_flat, const int32_t* k,
+                              const double* u, cpm_move* out);
+int cpm_engine_commit_moves(cpm_engine* e, size_t sim, size_t n, const int64_t* target_flat, const uint32_t* gaining);
+void cpm_engine_destroy(cpm_engine* e);
+
+/* ------------------------------------------------------ many-run batch ---
+ * Extension of run_batch for simulations that differ in grid as well as
+ * theta (no counterpart in the reference, whose run_batch shares one grid):
+ * one builder per simulation, all run in one persistent launch. topology=0
+ * skips the contact graph and labelling (samples then carry volume,
+ * interface, centroid and gyration only). */
+int cpm_run_many(const cpm_builder* const* builders, size_t n, uint64_t burn_in_mcs, uint64_t readout_mcs,
+                 uint64_t sampling_interval_mcs, int32_t include_lattice, int32_t topology, cpm_result** out);
+
+/* ---------------------------------------------------- host-only helpers ---
+ * No device work: the placement, hashes and seeds the reference computes on
+ * the host, exposed so callers (and the CPU test suite) can check them. */
+/* Resolves, validates and places (initialization.rs:39-330) without running.
+ * lattice_out holds product(grid) ids, type_of_out n_cells type indices
+ * (capacity in *n_cells on input, count on output). */
+int cpm_builder_initial_state(const cpm_builder* b, uint32_t* lattice_out, size_t lattice_capacity,
+                              uint32_t* type_of_out, size_t* n_cells, int32_t* used_default);
+/* convention_hash and model_hash (config.rs:479-556) of the configuration
+ * resolved with the given windows and the given lattice (product(grid) ids)
+ * and cell types; each out buffer holds 65 bytes. */
+int cpm_builder_hashes(const cpm_builder* b, uint64_t burn_in_mcs, uint64_t readout_mcs, uint64_t sampling_interval_mcs,
+                       const uint32_t* lattice, size_t lattice_len, const uint32_t* type_of, size_t n_cells,
+                       char* convention_hash_out, char* model_hash_out);
+/* rng.rs:37-40: first 8 LE bytes of BLAKE3(master LE || index LE). */
+uint64_t cpm_derive_seed_u64(uint64_t master_seed, uint64_t simulation_index);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CPM_GPU_H */

@@ -1,0 +1,211 @@
+"""Host-side logic of the GB300 engine, checked on the CPU (no device work).
+
+* libcpm_gpu.so loads and exports every symbol include/cpm_gpu.h declares;
+* default placement (scatter-and-grow) equals the oracle's, site for site,
+  so a device run starts from the reference's own initial lattice;
+* derived seeds and the model hash reproduce the reference's known answers;
+* configuration errors surface as ValueError with the reference's messages
+  (tests/python/test_errors.py:8-51) and theta has the canonical layout
+  (tests/python/test_batch.py:26-37).
+"""
+
+import ctypes
+import re
+import warnings
+
+import numpy as np
+import pytest
+
+from helpers import Model, c1_model, organoid_model, sorting_model
+from kat_fixtures import DERIVED_SEEDS_42, FROZEN_ADHESION, FROZEN_MCS, FROZEN_MODEL_HASH, FROZEN_SEED, FROZEN_TYPES, frozen_lattice
+
+
+def test_library_exports_every_declared_symbol():
+    from cpm import _cpm
+
+    header = open(_cpm.__file__.replace("cpm-rust_gb300/python/cpm/_cpm.py", "include/cpm_gpu.h")).read()
+    declared = set(re.findall(r"\b(cpm_[a-z0-9_]+)\s*\(", header))
+    assert declared == set(_cpm.EXPORTED_SYMBOLS)
+    lib = ctypes.CDLL(_cpm.LIB_PATH)
+    for name in declared:
+        assert hasattr(lib, name), name
+
+
+@pytest.mark.parametrize("model_fn", [
+    lambda: c1_model(seed=1),
+    lambda: c1_model(seed=77),
+    lambda: Model((30, 30), "fixed", [("e", 50, 75, 10.0, 2.0)], [[0, 5], [5, 2]], [5], seed=2),
+    lambda: sorting_model(side=64, seed=4),
+    lambda: organoid_model(side=20),
+    lambda: organoid_model(side=15, boundary="fixed", counts=(4, 3)),
+])
+def test_default_placement_matches_oracle(model_fn):
+    m = model_fn()
+    lat, cto, used = m.builder().initial_state()
+    ref = m.oracle()
+    assert used
+    assert np.array_equal(lat, ref.lattice())
+    assert np.array_equal(cto, ref.type_of())
+
+
+def test_explicit_placement_errors_match_reference():
+    m = c1_model()
+    lat = np.zeros((30, 30), dtype=np.uint32)
+    lat[0, 0] = 1
+    lat[5, 5] = 1  # disconnected
+    with pytest.raises(ValueError, match="is not connected"):
+        m.builder(lattice=lat, cell_type_of=[0]).initial_state()
+    with pytest.raises(ValueError, match="has zero volume"):
+        m.builder(lattice=np.zeros((30, 30), np.uint32), cell_type_of=[0]).initial_state()
+    with pytest.raises(ValueError, match="expected N_sites = 900"):
+        m.builder(lattice=np.zeros(10, np.uint32), cell_type_of=[0]).initial_state()
+
+
+def test_crowded_scatter_reports_reference_error():
+    m = Model((10, 10), "periodic", [("a", 50, 75, 1.0, 1.0)], [[0, 1], [1, 1]], [20])
+    with pytest.raises(ValueError, match="could not place all 20 seed points"):
+        m.builder().initial_state()
+
+
+def test_derived_seeds_match_published_values():
+    from cpm import _cpm
+
+    assert [_cpm.derive_seed_u64(42, i) for i in range(5)] == DERIVED_SEEDS_42
+
+
+def test_model_hash_known_answer():
+    import oracle as O
+
+    m = Model((30, 30), "periodic", FROZEN_TYPES, FROZEN_ADHESION, [1, 1], seed=FROZEN_SEED)
+    sim = m.oracle(lattice=frozen_lattice(), cell_type_of=[0, 1], local_halo=False)
+    sim.run_mcs(FROZEN_MCS)
+    b = m.builder(lattice=frozen_lattice(), cell_type_of=[0, 1])
+    _, mh = b.hashes(0, 1, 1, sim.lattice(), [0, 1])
+    assert mh == FROZEN_MODEL_HASH
+
+
+def test_convention_hash_is_theta_independent():
+    m = c1_model()
+    b1 = m.builder()
+    lat, cto, _ = b1.initial_state()
+    m2 = Model((30, 30), "periodic", [("epithelial", 50, 75, 3.0, 9.0)], [[0, 1], [1, 7]], [5])
+    b2 = m2.builder()
+    assert b1.hashes(5, 5, 5, lat, cto)[0] == b2.hashes(5, 5, 5, lat, cto)[0]
+    assert b1.hashes(5, 5, 5, lat, cto)[0] != b1.hashes(6, 5, 5, lat, cto)[0]
+
+
+# ---- reference Python tests that need no device (tests/python/test_errors.py)
+def test_unsupported_grid_length_raises_value_error():
+    import cpm
+
+    with pytest.raises(ValueError, match="length 2 or 3"):
+        cpm.CPM(grid=(1, 2, 3, 4), boundary="periodic", seed=1)
+
+
+def test_unknown_neighborhood_string_raises_value_error():
+    import cpm
+
+    with pytest.raises(ValueError, match="unknown neighbourhood"):
+        cpm.CPM(grid=(10, 10), boundary="periodic", seed=1, copy_neighborhood="hexagonal")
+
+
+def test_unknown_boundary_string_raises_value_error():
+    import cpm
+
+    with pytest.raises(ValueError, match="unknown boundary"):
+        cpm.CPM(grid=(10, 10), boundary="squishy", seed=1)
+
+
+def test_positive_lambda_act_with_zero_max_act_raises_immediately():
+    import cpm
+
+    sim = cpm.CPM(grid=(10, 10), boundary="periodic", seed=1)
+    with pytest.raises(ValueError, match="max_act"):
+        sim.register_cell_type(name="a", target_volume=20, target_interface=50, lambda_volume=1.0,
+                               lambda_interface=1.0, lambda_act=1.0, max_act=0)
+
+
+def test_unknown_cell_type_in_add_cells_raises_value_error():
+    import cpm
+
+    sim = cpm.CPM(grid=(10, 10), boundary="periodic", seed=1)
+    with pytest.raises(ValueError, match="unknown cell type"):
+        sim.add_cells(cell_type="ghost", n=1)
+
+
+def test_negative_lambda_message_matches_reference():
+    import cpm
+
+    sim = cpm.CPM(grid=(10, 10), boundary="periodic", seed=1)
+    with pytest.raises(ValueError, match=r"^lambda_volume must be finite and non-negative, got -1$"):
+        sim.register_cell_type("bad", 20, 50, -1.0, 1.0)
+
+
+def test_non_square_adhesion_matrix_is_rejected_before_any_device_work():
+    import cpm
+
+    sim = cpm.CPM(grid=(10, 10), boundary="periodic", seed=1)
+    sim.register_cell_type(name="a", target_volume=20, target_interface=50, lambda_volume=1.0, lambda_interface=1.0)
+    sim.add_cells(cell_type="a", n=1)
+    sim.set_adhesion([[0.0, 1.0], [1.0, 0.0], [0.0, 0.0]])
+    with pytest.raises(ValueError, match="adhesion matrix"):
+        sim.run(burn_in_mcs=1, readout_mcs=1, sampling_interval_mcs=1)
+
+
+def test_literal_config2_and_config3_neighbourhoods_are_rejected():
+    """Moore / 26-neighbour *copy* is not a subset of the von Neumann
+    connectivity stencil (config.rs:305-323): rejected as the reference does."""
+    import cpm
+
+    for grid, copy in (((32, 32), "moore"), ((8, 8, 8), "twenty_six")):
+        sim = cpm.CPM(grid=grid, boundary="periodic", seed=1, copy_neighborhood=copy)
+        sim.register_cell_type("a", 20, 30, 1.0, 1.0)
+        sim.add_cells("a", 1)
+        sim.set_adhesion([[0, 1], [1, 1]])
+        with pytest.raises(ValueError, match="must be a subset of connectivity_neighborhood"):
+            sim.run(1, 1, 1)
+
+
+def test_theta_names_and_extract_theta_match_canonical_layout():
+    import cpm
+
+    sim = cpm.CPM(grid=(20, 20), boundary="periodic", seed=1)
+    sim.register_cell_type(name="a", target_volume=9, target_interface=20, lambda_volume=1.0, lambda_interface=0.2)
+    sim.register_cell_type(name="b", target_volume=9, target_interface=20, lambda_volume=1.5, lambda_interface=0.3)
+    sim.add_cells("a", 2)
+    sim.add_cells("b", 2)
+    sim.set_adhesion([[0.0, 3.0, 3.0], [3.0, 1.0, 5.0], [3.0, 5.0, 1.0]])
+    names = sim.theta_names()
+    theta = sim.extract_theta()
+    assert len(names) == len(theta) == 14
+    assert names[:4] == ["lambda_volume[a]", "lambda_volume[b]", "lambda_interface[a]", "lambda_interface[b]"]
+    assert theta[:4] == [1.0, 1.5, 0.2, 0.3]
+    assert names[4:10] == ["J[medium][medium]", "J[medium][a]", "J[medium][b]", "J[a][a]", "J[a][b]", "J[b][b]"]
+
+
+def test_wrong_length_theta_raises_a_clean_error():
+    import cpm
+
+    sim = cpm.CPM(grid=(20, 20), boundary="periodic", seed=1)
+    sim.register_cell_type("a", 9, 20, 1.0, 0.2)
+    sim.add_cells("a", 2)
+    sim.set_adhesion([[0.0, 3.0], [3.0, 1.0]])
+    base = sim.extract_theta()
+    with pytest.raises(ValueError, match="theta at index 1 has length"):
+        sim.run_batch([base, base[:-1]], burn_in_mcs=5, readout_mcs=5, sampling_interval_mcs=5, master_seed=1)
+
+
+def test_cells_for_density_matches_reference_helper():
+    import cpm
+    from cpm.warnings import CPMLowResolutionWarning
+
+    n = cpm.cells_for_density(grid=(64, 64), target_volume=100, phi=0.8)
+    assert n * 100 / 4096 == pytest.approx(0.8, abs=0.02)
+    with pytest.warns(CPMLowResolutionWarning):
+        cpm.cells_for_density(grid=(64, 64), target_volume=4, phi=0.8)
+    with warnings.catch_warnings():
+        warnings.simplefilter("error", CPMLowResolutionWarning)
+        cpm.cells_for_density(grid=(64, 64), target_volume=1000, phi=0.8)
+    # the survey's config sizes
+    assert cpm.cells_for_density((512, 512), 50, 0.2) == 1049
+    assert cpm.cells_for_density((128, 128, 128), 1048, 0.8 / 3) == 534
