@@ -62,14 +62,14 @@ __device__ __forceinline__ bool table3d_bit(const uint64_t* t3, uint32_t p) {
     return (__ldg(t3 + (p >> 6)) >> (p & 63u)) & 1ull;
 }
 
-template <int D>
-__device__ __forceinline__ bool preserves_topology(const SimDesc& s, const uint32_t* sig, int64_t t, uint32_t losing,
+template <int D, class SigT>
+__device__ __forceinline__ bool preserves_topology(const SimDesc& s, const SigT* sig, int64_t t, uint32_t losing,
                                                    const uint32_t* t2, const uint64_t* t3) {
     if (losing == 0) return true;  // medium is exempt (connectivity.rs:48-50)
     constexpr int NF = D == 2 ? 8 : 26;
     uint32_t p = 0;
 #pragma unroll
-    for (int i = 0; i < NF; ++i) p |= (uint32_t)(sig[t + s.topo_off[i]] == losing) << i;
+    for (int i = 0; i < NF; ++i) p |= (uint32_t)((uint32_t)sig[t + s.topo_off[i]] == losing) << i;
     return D == 2 ? table2d_bit(t2, p) : table3d_bit(t3, p);
 }
 
@@ -88,8 +88,8 @@ struct DeltaOut {
 // Terms::total_delta = volume + interface + adhesion, each accumulated in the
 // reference's order. Explicit _rn intrinsics forbid FMA contraction, so the
 // result is bit-identical to the reference's separately rounded f64 ops.
-template <int NE>
-__device__ __forceinline__ DeltaOut delta_h(const SimDesc& s, const uint32_t* sig, const uint16_t* adh_of,
+template <int NE, class SigT>
+__device__ __forceinline__ DeltaOut delta_h(const SimDesc& s, const SigT* sig, const uint16_t* adh_of,
                                             const uint32_t* volume, const uint32_t* interface, int64_t t,
                                             uint32_t L, uint32_t G) {
     const int nt1 = s.n_types + 1;
@@ -100,7 +100,7 @@ __device__ __forceinline__ DeltaOut delta_h(const SimDesc& s, const uint32_t* si
     int cl = 0, cg = 0;
 #pragma unroll
     for (int k = 0; k < NE; ++k) {
-        const uint32_t nc = sig[t + s.energy_off[k]];
+        const uint32_t nc = (uint32_t)sig[t + s.energy_off[k]];
         cl += nc == L;
         cg += nc == G;
         const int ni = adh_of[nc];
@@ -160,8 +160,8 @@ __device__ __forceinline__ int64_t nearest_image(int64_t coord, double centroid,
 
 // Writes sigma[t] = v and, under a periodic boundary, every halo cell that
 // mirrors t (the local equivalent of lattice.rs:240-254's full refresh).
-template <int D>
-__device__ __forceinline__ void write_site(const SimDesc& s, uint32_t* sig, const int* x, uint32_t v) {
+template <int D, class SigT>
+__device__ __forceinline__ void write_site(const SimDesc& s, SigT* sig, const int* x, uint32_t v) {
     int alt[3][3], na[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) { na[d] = 1; alt[d][0] = 0; alt[d][1] = 0; alt[d][2] = 0; }
@@ -179,17 +179,17 @@ __device__ __forceinline__ void write_site(const SimDesc& s, uint32_t* sig, cons
                 int64_t f = (int64_t)alt[0][a] * s.strides[0];
                 if (D > 1) f += (int64_t)alt[1][b] * s.strides[1];
                 if (D > 2) f += (int64_t)alt[2][c] * s.strides[2];
-                sig[f] = v;
+                sig[f] = (SigT)v;
             }
 }
 
 // dynamics::commit for an accepted move whose cells this thread owns
 // exclusively (contact is recounted at sample time, not maintained here).
-template <int D>
-__device__ __forceinline__ void commit_move(const SimDesc& s, uint32_t* sig, uint32_t* volume, uint32_t* interface,
+template <int D, class SigT>
+__device__ __forceinline__ void commit_move(const SimDesc& s, SigT* sig, uint32_t* volume, uint32_t* interface,
                                             int64_t* sum_pos, int64_t* sum_outer, const int* x, uint32_t L,
                                             uint32_t G, int dl, int dg) {
-    write_site<D>(s, sig, x, G);
+    write_site<D, SigT>(s, sig, x, G);
     if (L) {
         volume[L] -= 1;
         interface[L] += (uint32_t)dl;

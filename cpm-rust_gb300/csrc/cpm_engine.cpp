@@ -12,11 +12,13 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <map>
 #include <mutex>
 #include <thread>
+#include <tuple>
 
 #include "cpm_kernels.h"
 
@@ -93,6 +95,9 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
                                const std::vector<int>& n_samples, const std::vector<int>& n_energy,
                                bool lattice_samples, cudaStream_t stream) {
     stream_ = stream;
+    // Selects the global-memory sweep for every simulation (used by the
+    // tests to exercise that path on small lattices).
+    force_global_ = std::getenv("CPM_GPU_FORCE_GLOBAL") != nullptr;
     const size_t N = configs.size();
     layouts_.resize(N);
     descs_.resize(N);
@@ -145,7 +150,7 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
     }
     CUDA_TRY(cudaMalloc(&arena_, std::max<size_t>(cv.off, 256)));
     CUDA_TRY(cudaMalloc(&d_descs_, std::max<size_t>(N, 1) * sizeof(SimDesc)));
-    CUDA_TRY(cudaMalloc(&d_next_, sizeof(int) * 8));
+    CUDA_TRY(cudaMalloc(&d_next_, sizeof(int) * 16));
     (void)t3;
     // ---- host staging, then one upload per buffer
     std::vector<char> stage(cv.off, 0);
@@ -250,14 +255,22 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
     return "";
 }
 
+// Whether simulation i runs on the shared-memory-resident path.
+bool DeviceSims::resident(size_t i) const {
+    const SimLayout& L = layouts_[i];
+    if (force_global_) return false;
+    if (L.n_cells >= 65535) return false;
+    return cpmgpu::resident_smem_bytes(L.g.n_padded, L.n_cells) <= cpmgpu::resident_smem_limit();
+}
+
 std::string DeviceSims::run(const std::vector<RunPlan>& plans, int grid_override) {
     std::string err;
     const uint64_t* t3 = nullptr;
-    // group plans by kernel variant
-    std::map<std::pair<int, int>, std::vector<RunPlan>> groups;
+    // group plans by kernel variant: (resident?, D, NE)
+    std::map<std::tuple<int, int, int>, std::vector<RunPlan>> groups;
     for (const RunPlan& p : plans) {
         const SimLayout& L = layouts_[p.sim];
-        groups[{L.g.D, L.NE}].push_back(p);
+        groups[std::make_tuple(resident(p.sim) ? 1 : 0, L.g.D, L.NE)].push_back(p);
         if (L.g.D == 3 && !t3) {
             t3 = device_table3d(err);
             if (!t3) return err;
@@ -282,18 +295,32 @@ std::string DeviceSims::run(const std::vector<RunPlan>& plans, int grid_override
         flat.insert(flat.end(), kv.second.begin(), kv.second.end());
     }
     CUDA_TRY(cudaMemcpyAsync(d_plans_, flat.data(), flat.size() * sizeof(RunPlan), cudaMemcpyHostToDevice, stream_));
-    CUDA_TRY(cudaMemsetAsync(d_next_, 0, sizeof(int) * 8, stream_));
+    CUDA_TRY(cudaMemsetAsync(d_next_, 0, sizeof(int) * 16, stream_));
     int dev = 0, sms = 1;
     CUDA_TRY(cudaGetDevice(&dev));
     CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     size_t gi = 0;
     for (auto& kv : groups) {
         const auto r = ranges[gi];
+        const int res = std::get<0>(kv.first), D = std::get<1>(kv.first), NE = std::get<2>(kv.first);
         int max_cells = 0;
-        for (size_t k = 0; k < r.second; ++k) max_cells = std::max(max_cells, layouts_[flat[r.first + k].sim].n_cells);
-        int grid = grid_override > 0 ? grid_override : std::min<int>((int)r.second, sms * 4);
-        CUDA_TRY(cpmgpu::launch_sweep(kv.first.first, kv.first.second, d_descs_, d_plans_ + r.first, (int)r.second,
-                                      d_next_ + gi, t3, max_cells, std::max(1, grid), stream_));
+        size_t smem = 0;
+        for (size_t k = 0; k < r.second; ++k) {
+            const SimLayout& L = layouts_[flat[r.first + k].sim];
+            max_cells = std::max(max_cells, L.n_cells);
+            smem = std::max(smem, cpmgpu::resident_smem_bytes(L.g.n_padded, L.n_cells));
+        }
+        if (res) {
+            int per_sm = 1;
+            CUDA_TRY(cpmgpu::resident_occupancy(D, NE, smem, &per_sm));
+            int grid = grid_override > 0 ? grid_override : std::min<int>((int)r.second, sms * std::max(1, per_sm));
+            CUDA_TRY(cpmgpu::launch_resident(D, NE, d_descs_, d_plans_ + r.first, (int)r.second, d_next_ + gi, t3, smem,
+                                             std::max(1, grid), stream_));
+        } else {
+            int grid = grid_override > 0 ? grid_override : std::min<int>((int)r.second, sms * 4);
+            CUDA_TRY(cpmgpu::launch_sweep(D, NE, d_descs_, d_plans_ + r.first, (int)r.second, d_next_ + gi, t3, max_cells,
+                                          std::max(1, grid), stream_));
+        }
         ++gi;
     }
     return "";

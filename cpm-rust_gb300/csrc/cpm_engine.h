@@ -42,6 +42,9 @@ class DeviceSims {
     // persistent launch per (D, energy stencil) group.
     std::string run(const std::vector<RunPlan>& plans, int grid_override = 0);
     std::string sync();
+    // Whether simulation i runs shared-memory resident (else the global-memory sweep).
+    bool resident(size_t i) const;
+    void force_global(bool on) { force_global_ = on; }
 
     size_t size() const { return layouts_.size(); }
     const SimLayout& layout(size_t i) const { return layouts_[i]; }
@@ -72,6 +75,7 @@ class DeviceSims {
     size_t plans_cap_ = 0;
     char* arena_ = nullptr;
     cudaStream_t stream_ = 0;
+    bool force_global_ = false;
 };
 
 // The 8 MiB 3D simple-point table of the current device (generated once).

@@ -174,7 +174,7 @@ __device__ void color_pass(const SimDesc& s, const PassInfo& p, uint64_t mcs, ui
             ct.attempts++;
             if (L == G) continue;  // early-out (monte_carlo.rs:60-64)
             ct.nonnull++;
-            if (!preserves_topology<D>(s, sig, t, L, s.table2d, t3)) { ct.topo_reject++; continue; }
+            if (!preserves_topology<D, uint32_t>(s, sig, t, L, s.table2d, t3)) { ct.topo_reject++; continue; }
             pend |= 1ull << i;
             kb0 |= (unsigned long long)(k & 1) << i;
             kb1 |= (unsigned long long)((k >> 1) & 1) << i;
@@ -208,11 +208,11 @@ __device__ void color_pass(const SimDesc& s, const PassInfo& p, uint64_t mcs, ui
                 pend &= ~(1ull << i);
                 if (L != 0 && volume[L] <= s.min_cell_volume) { ct.guard_reject++; continue; }
                 ct.evaluated++;
-                const DeltaOut o = delta_h<NE>(s, sig, adh_of, volume, interface, t, L, G);
+                const DeltaOut o = delta_h<NE, uint32_t>(s, sig, adh_of, volume, interface, t, L, G);
                 bool acc = o.dh <= 0.0;
                 if (!acc) acc = u53(site_draw(s.seed, mcs, (uint32_t)t)) < exp(-o.dh);
                 if (acc) {
-                    commit_move<D>(s, sig, volume, interface, s.sum_pos, s.sum_outer, x, L, G, o.dl, o.dg);
+                    commit_move<D, uint32_t>(s, sig, volume, interface, s.sum_pos, s.sum_outer, x, L, G, o.dl, o.dg);
                     ct.accepted++;
                 }
             }
@@ -361,12 +361,12 @@ __global__ void evaluate_moves_kernel(const SimDesc* simp, int64_t n, const int6
         o.topology_ok = 0; o.volume_guard_ok = 0; o.evaluated = 0;
         o.delta_i_losing = 0; o.delta_i_gaining = 0; o.delta_h = 0.0; o.accepted = 0; o.pad = 0;
         if (!o.null_move) {
-            o.topology_ok = preserves_topology<D>(s, s.sigma, t, o.losing, s.table2d, t3);
+            o.topology_ok = preserves_topology<D, uint32_t>(s, s.sigma, t, o.losing, s.table2d, t3);
             if (o.topology_ok) {
                 o.volume_guard_ok = !(o.losing != 0 && s.volume[o.losing] <= s.min_cell_volume);
                 if (o.volume_guard_ok) {
                     o.evaluated = 1;
-                    const DeltaOut d = delta_h<NE>(s, s.sigma, s.adh_of, s.volume, s.interface, t, o.losing, o.gaining);
+                    const DeltaOut d = delta_h<NE, uint32_t>(s, s.sigma, s.adh_of, s.volume, s.interface, t, o.losing, o.gaining);
                     o.delta_i_losing = d.dl;
                     o.delta_i_gaining = d.dg;
                     o.delta_h = d.dh;
@@ -387,10 +387,10 @@ __global__ void commit_moves_kernel(const SimDesc* simp, int64_t n, const int64_
     for (int64_t i = 0; i < n; ++i) {
         const int t = (int)target[i];
         const uint32_t L = s.sigma[t], G = gaining[i];
-        const DeltaOut d = delta_h<NE>(s, s.sigma, s.adh_of, s.volume, s.interface, t, L, G);
+        const DeltaOut d = delta_h<NE, uint32_t>(s, s.sigma, s.adh_of, s.volume, s.interface, t, L, G);
         int x[3];
         coords_of<D>(s, t, x);
-        commit_move<D>(s, s.sigma, s.volume, s.interface, s.sum_pos, s.sum_outer, x, L, G, d.dl, d.dg);
+        commit_move<D, uint32_t>(s, s.sigma, s.volume, s.interface, s.sum_pos, s.sum_outer, x, L, G, d.dl, d.dg);
     }
 }
 

@@ -20,4 +20,11 @@ cudaError_t launch_recount(int D, int NE, const SimDesc* d_sim, int64_t n_sites,
 cudaError_t launch_energy(int D, int NE, const SimDesc* d_sim, double* d_out, cudaStream_t st);
 cudaError_t launch_table3d(uint64_t* d_words, const uint32_t* d_face, const uint32_t* d_full, uint32_t origin_mask,
                            cudaStream_t st);
+// Shared-memory-resident sweep (cpm_resident.cu): one CTA per simulation.
+size_t resident_smem_bytes(int64_t n_padded, int n_cells);
+size_t resident_smem_limit();
+int resident_block();
+cudaError_t launch_resident(int D, int NE, SimDesc* d_sims, const RunPlan* d_plans, int n_plans, int* d_next,
+                            const uint64_t* d_t3, size_t smem, int grid, cudaStream_t st);
+cudaError_t resident_occupancy(int D, int NE, size_t smem, int* blocks_per_sm);
 }  // namespace cpmgpu

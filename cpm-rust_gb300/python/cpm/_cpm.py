@@ -46,6 +46,7 @@ STAT_NAMES = (
     "rounds",
     "passes",
     "spin_timeouts",
+    "fixpoint_iterations",
 )
 
 

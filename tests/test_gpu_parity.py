@@ -205,3 +205,18 @@ def test_batch_engine_matches_single_engines(cuda_required):
         one.run_mcs(20)
         one.synchronize()
         assert np.array_equal(one.lattice(), many.lattice(i)), i
+
+
+@pytest.mark.parametrize("name", ["c1_periodic", "sorting_moore", "3d_26"])
+def test_global_memory_sweep_keeps_exact_state(name, cuda_required, monkeypatch):
+    """The global-memory sweep (used for lattices too large for shared
+    memory) keeps the same invariants as the resident sweep."""
+    monkeypatch.setenv("CPM_GPU_FORCE_GLOBAL", "1")
+    model = MODELS[name]()
+    eng = _engine(model)
+    eng.run_mcs(20 if model.D == 2 else 4)
+    eng.synchronize()
+    ok, _, _ = eng.recount_check()
+    assert ok
+    st = eng.stats()
+    assert st["accepted"] > 0
