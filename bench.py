@@ -1,0 +1,393 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 Cellular Potts engine (one JSON line on rank 0).
+
+Workload (`config.workload`): the 2D differential-adhesion sorting case,
+512x512 periodic, 4 cell types (V*=50, I*=30, lambda_V=5, lambda_I=1),
+1049 cells per type (phi=0.8 by `cells_for_density`), medium row of J = 16
+and type-type J uniform in [2, 14] drawn from numpy's default_rng(seed).
+The reference rejects the literal "Moore copy" of this case
+(crates/cpm-core/src/config.rs:305-323: copy must be a subset of the von
+Neumann connectivity), so copy = connectivity = von Neumann and energy =
+Moore, the reference's 2D default. A step is `--mcs-per-step` Monte Carlo
+steps of that lattice (one MCS = 262,144 copy attempts); the metric is copy
+attempts per second.
+
+* value: device time of the sweep launches (CUDA events on the engine's
+  stream), lattice already resident in HBM; L2 (129 MB) is flushed by a
+  256 MB write between timed steps.
+* e2e: the same metric through the public API `cpm.CPM(...).run(...)`
+  (host placement, upload, device run, download, host readouts) per step.
+* roofline: algorithmic HBM bytes per attempt = 4 + 4*f_acc (sigma read
+  once, written on accept) times the attempts of one launch, over the
+  launch's average duration, against the measured copy bandwidth.
+* cpu_baseline: the CPU oracle (a restatement of the reference's run_mcs)
+  on one host thread over a bounded sample of the same workload.
+* --impl reference: the oracle on every host core (one replica of the
+  workload per thread, the reference's run_batch parallelism).
+
+Multi-GPU: the path does not shard within one lattice; under torchrun each
+rank runs an independent replica ("replicas only") and `value` sums them.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "cpm-rust_gb300")
+for p in (os.path.join(PKG, "python"), ROOT):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+METRIC = "copy attempts/s"
+GRID = (512, 512)
+TYPES = [(f"t{i}", 50, 30, 5.0, 1.0) for i in range(4)]
+PER_TYPE = 1049  # cells_for_density((512, 512), 50, 0.2)
+SEED = 1
+
+
+def adhesion(seed=SEED):
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    J = np.zeros((5, 5))
+    J[0, 1:] = J[1:, 0] = 16.0
+    tt = rng.uniform(2, 14, size=(4, 4))
+    tt = np.triu(tt) + np.triu(tt, 1).T
+    J[1:, 1:] = tt
+    return J.tolist()
+
+
+def workload_config():
+    return {
+        "workload": "2D sorting 512x512 periodic, 4 types x 1049 cells (phi=0.8), copy=connectivity=von Neumann, "
+                    "energy=Moore, V*=50 I*=30 lambda_V=5 lambda_I=1, J medium 16, J type-type U[2,14]",
+        "grid": list(GRID),
+        "n_cells": 4 * PER_TYPE,
+        "seed": SEED,
+    }
+
+
+def build_raw(seed=SEED):
+    from cpm import _cpm
+
+    b = _cpm.CPM(grid=list(GRID), boundary="periodic", seed=seed)
+    for t in TYPES:
+        b.register_cell_type(*t)
+    for t in TYPES:
+        b.add_cells(t[0], PER_TYPE)
+    b.set_adhesion(adhesion(seed))
+    b.initialize(warn_on_default_init=False)
+    return b
+
+
+def build_public(seed=SEED):
+    import cpm
+
+    sim = cpm.CPM(grid=GRID, boundary="periodic", seed=seed)
+    for t in TYPES:
+        sim.register_cell_type(*t)
+    for t in TYPES:
+        sim.add_cells(t[0], PER_TYPE)
+    sim.set_adhesion(adhesion(seed))
+    sim.initialize(warn_on_default_init=False)
+    return sim
+
+
+def oracle_spec():
+    import oracle as O
+
+    return O.ModelSpec(GRID, True, [t[1:] for t in TYPES], adhesion(SEED), cell_counts=[PER_TYPE] * 4)
+
+
+# --------------------------------------------------------------- clocks ----
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        sm.sort()
+        med = sm[len(sm) // 2] if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def profiled_traffic_per_attempt():
+    """DRAM bytes per attempt of the sweep kernel from the committed ncu summary (or None)."""
+    path = os.path.join(ROOT, "profiles", "sweep_c2_traffic.txt")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("dram_bytes_per_attempt:"):
+                    return float(line.split(":", 1)[1])
+    except Exception:
+        pass
+    return None
+
+
+# ---------------------------------------------------------- reference arm ----
+def run_reference(args, rank, world):
+    import numpy as np
+
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    O.build()
+    spec = oracle_spec()
+    threads = os.cpu_count() or 1
+    mcs = args.ref_mcs
+    seeds = np.arange(1, threads + 1, dtype=np.uint64)
+
+    def step():
+        t0 = time.perf_counter()
+        failed, *_ = O.run_many(spec, seeds, burn_in=mcs, readout=0, threads=threads, local_halo=True)
+        assert failed == 0
+        return time.perf_counter() - t0
+
+    for _ in range(args.warmup):
+        step()
+    times = [step() for _ in range(args.steps)]
+    attempts = threads * mcs * GRID[0] * GRID[1] * args.steps
+    value = attempts / sum(times)
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": "attempts/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1000 * sum(times) / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded scatter-and-grow placement)",
+        "config": dict(workload_config(), sample=f"{threads} replicas x {mcs} MCS per step (incl. placement)"),
+        "cpu_baseline": {"value": value, "unit": "attempts/s", "cores": threads, "kind": "port",
+                         "sample": f"{threads} threads, one replica each, {mcs} MCS per step"},
+        "e2e": {"value": value, "unit": "attempts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------- GPU arm ----
+def cpu_baseline(args):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    O.build()
+    sim = O.OracleSim(oracle_spec(), SEED)
+    sim.set_local_halo(True)
+    sim.init_default()
+    t0 = time.perf_counter()
+    sim.run_mcs(args.cpu_mcs)
+    dt = time.perf_counter() - t0
+    att = args.cpu_mcs * GRID[0] * GRID[1]
+    return {"value": att / dt, "unit": "attempts/s", "cores": 1, "kind": "port",
+            "sample": f"{args.cpu_mcs} MCS of the same 512x512 lattice from the same placement, one thread"}
+
+
+def run_gpu(args, rank, world, dist):
+    import torch
+
+    from cpm import _cpm
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream()
+    eng = _cpm.Engine(build_raw(SEED + rank), stream=stream.cuda_stream)
+    n_sites = GRID[0] * GRID[1]
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    for _ in range(args.warmup):
+        eng.run_mcs(args.mcs_per_step)
+    torch.cuda.synchronize()
+    s0 = eng.stats()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(dev)
+    clocks.start()
+    ms = []
+    launches = 0
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        eng.run_mcs(args.mcs_per_step)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms.append(a.elapsed_time(b))
+        launches += 1
+    clk = clocks.stop()
+    s1 = eng.stats()
+    total_ms = sum(ms)
+    if dist:
+        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    attempts = (s1["attempts"] - s0["attempts"])
+    assert attempts == args.steps * args.mcs_per_step * n_sites, (attempts, s1, s0)
+    ok, _, _ = eng.recount_check()
+    assert ok, "device V/I differ from a full recount"
+    value = attempts * world / (total_ms / 1000.0)
+    f_acc = (s1["accepted"] - s0["accepted"]) / attempts
+    f_nonnull = (s1["nonnull"] - s0["nonnull"]) / attempts
+    bytes_per_attempt = 4.0 + 4.0 * f_acc
+    launch_s = (total_ms / 1000.0) / args.steps
+    achieved = bytes_per_attempt * (attempts / args.steps) / launch_s / 1e9
+    peaks, src = measured_peaks()
+    traffic_pa = profiled_traffic_per_attempt()
+
+    # ---- e2e through the public API (host buffers, copies inside the timed region)
+    e2e = None
+    if rank == 0 and args.e2e_steps > 0:
+        times, h2d, d2h = [], 0, 0
+        for i in range(args.e2e_steps + 1):
+            sim = build_public(SEED + 100 + i)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res = sim.run(burn_in_mcs=0, readout_mcs=args.e2e_mcs, sampling_interval_mcs=args.e2e_mcs)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            if i == 0:
+                continue  # warm-up call
+            times.append(dt)
+            h2d += res.stats["h2d_bytes"]
+            d2h += res.stats["d2h_bytes"]
+        n = len(times)
+        e2e = {"value": n * args.e2e_mcs * n_sites / sum(times), "unit": "attempts/s",
+               "h2d_bytes_per_step": h2d // n, "d2h_bytes_per_step": d2h // n,
+               "step": f"cpm.CPM(...).run(burn_in_mcs=0, readout_mcs={args.e2e_mcs}, sampling_interval_mcs={args.e2e_mcs})"}
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "attempts/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded scatter-and-grow placement, J from default_rng(seed))",
+        "config": dict(workload_config(), mcs_per_step=args.mcs_per_step, l2="flushed (256 MB write) between timed steps",
+                       parallelism="replicas" if world > 1 else "single lattice"),
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "roofline": {
+            "bound": "hbm",
+            "achieved": achieved,
+            "peak": peaks.get("hbm_gbs"),
+            "unit": "GB/s",
+            "frac": achieved / peaks.get("hbm_gbs"),
+            "traffic": traffic_pa * attempts / args.steps if traffic_pa is not None else None,
+            "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)" if src == "measured" else "fallback",
+            "algorithmic_bytes_per_attempt": bytes_per_attempt,
+        },
+        "stats": {"f_nonnull": f_nonnull, "f_acc": f_acc,
+                  "rounds_per_pass": (s1["rounds"] - s0["rounds"]) / max(1, s1["passes"] - s0["passes"])},
+        "clocks": clk,
+    }
+    if world == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(args)
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--mcs-per-step", type=int, default=50)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-mcs", type=int, default=100)
+    ap.add_argument("--cpu-mcs", type=int, default=200)
+    ap.add_argument("--ref-mcs", type=int, default=40)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as tdist
+
+        backend = "gloo" if args.impl == "reference" else "nccl"
+        tdist.init_process_group(backend=backend)
+        dist = tdist
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_gpu(args, rank, world, dist)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -24,6 +24,9 @@ enum CpmStat {
     CPM_STAT_ROUNDS = 6,     // conflict-resolution rounds (summed over passes)
     CPM_STAT_PASSES = 7,
     CPM_STAT_SPIN_TIMEOUTS = 8,  // bounded waits that gave up (must stay 0)
+    CPM_STAT_FIXPOINT_ITERS = 9, // fixpoint iterations summed over threads
+    CPM_STAT_H2D_BYTES = 10,     // host-to-device bytes of the call (host-side count)
+    CPM_STAT_D2H_BYTES = 11,     // device-to-host bytes of the call (host-side count)
     CPM_STAT_COUNT = 16
 };
 

@@ -249,6 +249,7 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
         s.sample_lattice = lattice_samples ? (uint32_t*)(base + o.slat) : nullptr;
         s.error = (int32_t*)(base + o.err);
     }
+    h2d_bytes_ += cv.off + N * sizeof(SimDesc);
     CUDA_TRY(cudaMemcpyAsync(arena_, stage.data(), cv.off, cudaMemcpyHostToDevice, stream_));
     CUDA_TRY(cudaMemcpyAsync(d_descs_, descs_.data(), N * sizeof(SimDesc), cudaMemcpyHostToDevice, stream_));
     CUDA_TRY(cudaStreamSynchronize(stream_));
@@ -333,6 +334,7 @@ std::string DeviceSims::sync() {
 
 std::string DeviceSims::read_padded(size_t i, std::vector<uint32_t>& out) const {
     out.resize((size_t)layouts_[i].g.n_padded);
+    d2h_bytes_ += out.size() * 4;
     CUDA_TRY(cudaMemcpy(out.data(), descs_[i].sigma, out.size() * 4, cudaMemcpyDeviceToHost));
     return "";
 }
@@ -341,16 +343,20 @@ std::string DeviceSims::read_cells(size_t i, std::vector<uint32_t>& vol, std::ve
                                    std::vector<int64_t>& sp, std::vector<int64_t>& so) const {
     const size_t n1 = layouts_[i].n_cells + 1, D = layouts_[i].g.D;
     vol.resize(n1); itf.resize(n1); sp.resize(n1 * D); so.resize(n1 * D * D);
+    d2h_bytes_ += n1 * 4;
     CUDA_TRY(cudaMemcpy(vol.data(), descs_[i].volume, n1 * 4, cudaMemcpyDeviceToHost));
+    d2h_bytes_ += n1 * 4;
     CUDA_TRY(cudaMemcpy(itf.data(), descs_[i].interface, n1 * 4, cudaMemcpyDeviceToHost));
+    d2h_bytes_ += sp.size() * 8;
     CUDA_TRY(cudaMemcpy(sp.data(), descs_[i].sum_pos, sp.size() * 8, cudaMemcpyDeviceToHost));
+    d2h_bytes_ += so.size() * 8;
     CUDA_TRY(cudaMemcpy(so.data(), descs_[i].sum_outer, so.size() * 8, cudaMemcpyDeviceToHost));
     return "";
 }
 
 std::string DeviceSims::read_energy(size_t i, std::vector<double>& e) const {
     e.resize(layouts_[i].n_energy);
-    if (!e.empty()) CUDA_TRY(cudaMemcpy(e.data(), descs_[i].energy_out, e.size() * 8, cudaMemcpyDeviceToHost));
+    if (!e.empty()) { d2h_bytes_ += e.size() * 8; CUDA_TRY(cudaMemcpy(e.data(), descs_[i].energy_out, e.size() * 8, cudaMemcpyDeviceToHost)); }
     return "";
 }
 
@@ -360,12 +366,17 @@ std::string DeviceSims::read_samples(size_t i, int n, std::vector<uint32_t>& vol
     const size_t n1 = layouts_[i].n_cells + 1, D = layouts_[i].g.D;
     vol.resize(n * n1); itf.resize(n * n1); sp.resize(n * n1 * D); so.resize(n * n1 * D * D);
     if (n == 0) return "";
+    d2h_bytes_ += vol.size() * 4;
     CUDA_TRY(cudaMemcpy(vol.data(), descs_[i].sample_volume, vol.size() * 4, cudaMemcpyDeviceToHost));
+    d2h_bytes_ += itf.size() * 4;
     CUDA_TRY(cudaMemcpy(itf.data(), descs_[i].sample_interface, itf.size() * 4, cudaMemcpyDeviceToHost));
+    d2h_bytes_ += sp.size() * 8;
     CUDA_TRY(cudaMemcpy(sp.data(), descs_[i].sample_sum_pos, sp.size() * 8, cudaMemcpyDeviceToHost));
+    d2h_bytes_ += so.size() * 8;
     CUDA_TRY(cudaMemcpy(so.data(), descs_[i].sample_sum_outer, so.size() * 8, cudaMemcpyDeviceToHost));
     if (lattice && descs_[i].sample_lattice) {
         lattice->resize((size_t)n * layouts_[i].g.n_sites);
+        d2h_bytes_ += lattice->size() * 4;
         CUDA_TRY(cudaMemcpy(lattice->data(), descs_[i].sample_lattice, lattice->size() * 4, cudaMemcpyDeviceToHost));
     }
     return "";
@@ -373,11 +384,13 @@ std::string DeviceSims::read_samples(size_t i, int n, std::vector<uint32_t>& vol
 
 std::string DeviceSims::read_stats(size_t i, std::vector<uint64_t>& stats) const {
     stats.resize(CPM_STAT_COUNT);
+    d2h_bytes_ += CPM_STAT_COUNT * 8;
     CUDA_TRY(cudaMemcpy(stats.data(), descs_[i].stats, CPM_STAT_COUNT * 8, cudaMemcpyDeviceToHost));
     return "";
 }
 
 std::string DeviceSims::read_mcs(size_t i, uint64_t& mcs) const {
+    d2h_bytes_ += 8;
     CUDA_TRY(cudaMemcpy(&mcs, &d_descs_[i].mcs, 8, cudaMemcpyDeviceToHost));
     return "";
 }
@@ -730,6 +743,7 @@ std::string run_many(const std::vector<Config>& configs, const std::vector<Initi
             R.metadata.theta_layout_version = 1;
         }
     };
+    (void)0;
     const unsigned nthreads = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), (unsigned)N));
     int dev_id = 0;
     cudaGetDevice(&dev_id);
@@ -738,6 +752,11 @@ std::string run_many(const std::vector<Config>& configs, const std::vector<Initi
         th.emplace_back([&, dev_id] { cudaSetDevice(dev_id); worker(); });
     for (auto& t : th) t.join();
     for (auto& e : errs) if (!e.empty()) return e;
+    for (auto& R : out) {
+        if (R.stats.size() < CPM_STAT_COUNT) R.stats.resize(CPM_STAT_COUNT, 0);
+        R.stats[CPM_STAT_H2D_BYTES] = dev.h2d_bytes();
+        R.stats[CPM_STAT_D2H_BYTES] = dev.d2h_bytes();
+    }
     return "";
 }
 

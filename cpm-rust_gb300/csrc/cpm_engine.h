@@ -9,6 +9,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -45,6 +46,9 @@ class DeviceSims {
     // Whether simulation i runs shared-memory resident (else the global-memory sweep).
     bool resident(size_t i) const;
     void force_global(bool on) { force_global_ = on; }
+    // Bytes this object copied host-to-device / device-to-host so far.
+    uint64_t h2d_bytes() const { return h2d_bytes_; }
+    uint64_t d2h_bytes() const { return d2h_bytes_; }
 
     size_t size() const { return layouts_.size(); }
     const SimLayout& layout(size_t i) const { return layouts_[i]; }
@@ -76,6 +80,8 @@ class DeviceSims {
     char* arena_ = nullptr;
     cudaStream_t stream_ = 0;
     bool force_global_ = false;
+    uint64_t h2d_bytes_ = 0;
+    mutable std::atomic<uint64_t> d2h_bytes_{0};
 };
 
 // The 8 MiB 3D simple-point table of the current device (generated once).

@@ -47,6 +47,8 @@ STAT_NAMES = (
     "passes",
     "spin_timeouts",
     "fixpoint_iterations",
+    "h2d_bytes",
+    "d2h_bytes",
 )
 
 
