@@ -29,6 +29,7 @@ static int fail(int code, const std::string& msg) {
 static int ok() { return CPM_OK; }
 
 extern "C" const char* cpm_last_error(void) { return g_err.c_str(); }
+void cpmhost::set_last_error(const std::string& m) { g_err = m; }
 extern "C" const char* cpm_version(void) { return "0.2.0+gb300"; }
 
 // Rust's `{:?}` of a &str.

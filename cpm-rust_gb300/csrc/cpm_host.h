@@ -164,5 +164,7 @@ std::string run_batch(const Config& base, const std::vector<std::vector<double>>
                       const ReadoutOptions& ro, std::vector<Result>& out);
 
 std::string last_cuda_error();
+// Sets the message cpm_last_error() reports on this thread.
+void set_last_error(const std::string& m);
 
 }  // namespace cpmhost

@@ -148,6 +148,7 @@ EXPORTED_SYMBOLS = (
     "cpm_engine_evaluate_moves", "cpm_engine_commit_moves", "cpm_engine_destroy",
     "cpm_run_many",
     "cpm_builder_initial_state", "cpm_builder_hashes", "cpm_derive_seed_u64",
+    "cpm_run_mcs_noalloc",
 )
 
 

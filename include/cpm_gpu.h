@@ -247,6 +247,49 @@ int cpm_builder_hashes(const cpm_builder* b, uint64_t burn_in_mcs, uint64_t read
 /* rng.rs:37-40: first 8 LE bytes of BLAKE3(master LE || index LE). */
 uint64_t cpm_derive_seed_u64(uint64_t master_seed, uint64_t simulation_index);
 
+/* -------------------------------------------- allocation-free sweep ---
+ * No counterpart in the reference. For callers that cannot call cudaMalloc
+ * while they run — a host framework that owns all device memory through its
+ * own pool, or a service that reserves every byte at start-up and treats a
+ * later allocation as a failure — and that therefore hand over simulations
+ * already resident on the device. cpm_run_mcs_noalloc advances such a
+ * simulation by n_mcs MCS with the same sweep as cpm_engine_run_mcs and
+ * allocates no device memory: its own scratch (descriptor, plan, work-queue
+ * counter, per-cell conflict slots) is a static 1 MiB device array inside
+ * the library, held by every GPU that loads it until the process exits.
+ * Limits: 2D lattices only (3D needs the 8 MiB simple-point table), at most
+ * 130,559 cells. The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress) with that device current, so make it before
+ * any stream capture. Calls share the array: calls that overlap on the GPU
+ * race, so serialise them. On return sim->mcs has advanced by n_mcs (the RNG
+ * counter base of the next call). */
+typedef struct {
+    int32_t dim;                  /* must be 2 */
+    int32_t periodic;             /* 1 periodic, 0 fixed */
+    int64_t dims[3];              /* interior extent; dims[2] ignored */
+    int32_t energy_neighborhood;  /* 0 von Neumann, 1 Moore */
+    int32_t n_types;
+    uint32_t n_cells;
+    uint32_t min_cell_volume;     /* 1 in the reference */
+    uint64_t seed;
+    uint64_t mcs;                 /* MCS already performed */
+    /* device pointers, caller-owned; per-cell arrays are indexed by id (n_cells + 1) */
+    uint32_t* sigma;              /* halo-padded lattice ((dims+2) per axis), halo consistent */
+    const uint16_t* type_plus_one;/* cell type + 1 per id, entry 0 = 0 (medium) */
+    uint32_t* volume;
+    uint32_t* interface;
+    int64_t* sum_position;        /* (n_cells + 1) x 2 */
+    int64_t* sum_position_outer;  /* (n_cells + 1) x 2 x 2 */
+    const double* adhesion;       /* (n_types + 1)^2, row-major, 0 = medium */
+    const double* lambda_volume;  /* n_types */
+    const double* lambda_interface;
+    const uint32_t* target_volume;
+    const uint32_t* target_interface;
+    uint64_t* stats;              /* optional: 16 device counters accumulated by the sweep */
+} cpm_device_sim;
+
+int cpm_run_mcs_noalloc(cpm_device_sim* sim, uint64_t n_mcs, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
