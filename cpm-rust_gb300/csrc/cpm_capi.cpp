@@ -418,10 +418,10 @@ extern "C" int cpm_result_sample_read(const cpm_result* r, size_t s, const cpm_s
     return ok();
 }
 
-extern "C" int cpm_result_stats(const cpm_result* r, uint64_t* out16) {
-    if (!r || !out16) return fail(CPM_E_ARG, "null argument");
-    std::memset(out16, 0, 16 * sizeof(uint64_t));
-    for (size_t i = 0; i < r->r.stats.size() && i < 16; ++i) out16[i] = r->r.stats[i];
+extern "C" int cpm_result_stats(const cpm_result* r, uint64_t* out32) {
+    if (!r || !out32) return fail(CPM_E_ARG, "null argument");
+    std::memset(out32, 0, 32 * sizeof(uint64_t));
+    for (size_t i = 0; i < r->r.stats.size() && i < 32; ++i) out32[i] = r->r.stats[i];
     return ok();
 }
 
@@ -605,12 +605,13 @@ extern "C" int cpm_engine_recount_check(const cpm_engine* ec, size_t i, int32_t*
     return ok();
 }
 
-extern "C" int cpm_engine_stats(const cpm_engine* e, size_t i, uint64_t* out16) {
-    if (bad_sim(e, i) || !out16) return fail(CPM_E_ARG, "bad engine or simulation index");
+extern "C" int cpm_engine_stats(const cpm_engine* e, size_t i, uint64_t* out32) {
+    if (bad_sim(e, i) || !out32) return fail(CPM_E_ARG, "bad engine or simulation index");
     std::vector<uint64_t> s;
     const std::string msg = e->sims.read_stats(i, s);
     if (!msg.empty()) return fail(CPM_E_CUDA, msg);
-    std::memcpy(out16, s.data(), 16 * 8);
+    std::memset(out32, 0, 32 * 8);
+    std::memcpy(out32, s.data(), std::min<size_t>(s.size(), 32) * 8);
     return ok();
 }
 

@@ -27,7 +27,16 @@ enum CpmStat {
     CPM_STAT_FIXPOINT_ITERS = 9, // fixpoint iterations summed over threads
     CPM_STAT_H2D_BYTES = 10,     // host-to-device bytes of the call (host-side count)
     CPM_STAT_D2H_BYTES = 11,     // device-to-host bytes of the call (host-side count)
-    CPM_STAT_COUNT = 16
+    CPM_STAT_DEFERRED = 12,      // tiled sweep: moves skipped because a cell was owned by another tile
+    CPM_STAT_CYC_PASSES = 13,    // tiled sweep: SM cycles in the site-colour passes (thread 0 of each CTA)
+    CPM_STAT_CYC_STAGE = 14,     // tiled sweep: SM cycles staging boxes and writing them back
+    CPM_STAT_CYC_SYNC = 15,      // tiled sweep: SM cycles in claims and grid barriers
+    CPM_STAT_CYC_BUILD = 16,     // tiled sweep: cycles building candidate lists
+    CPM_STAT_CYC_EVAL = 17,      // tiled sweep: cycles in speculative evaluation
+    CPM_STAT_CYC_FIX = 18,       // tiled sweep: cycles in the fixpoint iterations
+    CPM_STAT_CYC_APPLY = 19,     // tiled sweep: cycles applying and re-evaluating
+    CPM_STAT_WIDE_PASSES = 20,   // tiled sweep: tile passes with more than 32 candidates (block-wide resolve)
+    CPM_STAT_COUNT = 32
 };
 
 struct SimDesc {
@@ -52,6 +61,8 @@ struct SimDesc {
     int64_t energy_off[CPM_MAX_STENCIL];
     int64_t topo_off[CPM_MAX_STENCIL];
     int8_t energy_vec[CPM_MAX_STENCIL][3];  // integer offset of each energy neighbour
+    int8_t copy_vec[6][3];                  // integer offset of each copy neighbour
+    int8_t topo_vec[CPM_MAX_STENCIL][3];    // integer offset of each simple-point neighbour
     uint32_t energy_pos_mask;               // offsets whose first nonzero component is > 0
     uint32_t table2d[8];                    // 2D simple-point table (256 bits)
     // ---- parameters ----
@@ -63,6 +74,15 @@ struct SimDesc {
     const double* lambda_i;
     const uint32_t* target_v;
     const uint32_t* target_i;
+    // Exact FP64 tables built on the host with the reference's operations:
+    // vterm[t*tab_n + x] = lambda_V[t] * ((x - V*[t])^2),
+    // iterm[t*tab_n + x] = lambda_I[t] * ((x - I*[t])^2) for 0 <= x < tab_n,
+    // dj[(l*(n+1) + g)*(n+1) + k] = J[g][k] - J[l][k] (adhesion difference).
+    const double* vterm;
+    const double* iterm;
+    const double* dj;
+    int32_t tab_n;
+    int32_t pad1;
     // ---- state ----
     int32_t n_cells;
     int32_t pad0;

@@ -85,28 +85,55 @@ struct DeltaOut {
     int dl, dg;  // integer interface deltas (every weight is 1.0)
 };
 
+// lambda * (x - target)^2 for an integer-valued x: the exact host-built
+// table when x is in range (same IEEE operations), else computed here.
+__device__ __forceinline__ double term_of(const double* tab, int tab_n, int ty, double lambda, uint32_t target,
+                                          int64_t x) {
+    if (tab != nullptr && x >= 0 && x < tab_n) return __ldg(tab + (int64_t)ty * tab_n + x);
+    return quad_term(lambda, target, (double)x);
+}
+
 // Terms::total_delta = volume + interface + adhesion, each accumulated in the
-// reference's order. Explicit _rn intrinsics forbid FMA contraction, so the
-// result is bit-identical to the reference's separately rounded f64 ops.
+// reference's order (energy.rs:92-103, 190-202, 242-264, 521-523). Every
+// operation is the reference's f64 operation, rounded to nearest, never
+// fused: explicit _rn intrinsics, and the tables hold values computed with
+// the same operations on the host. Adding a zero to the running sums is
+// skipped: a sum that starts at +0.0 can never become -0.0 under
+// round-to-nearest, so x + (+-0.0) == x bit for bit.
 template <int NE, class SigT>
 __device__ __forceinline__ DeltaOut delta_h(const SimDesc& s, const SigT* sig, const uint16_t* adh_of,
                                             const uint32_t* volume, const uint32_t* interface, int64_t t,
                                             uint32_t L, uint32_t G) {
     const int nt1 = s.n_types + 1;
     const int li = adh_of[L], gi = adh_of[G];
-    const double* JL = s.J + li * nt1;
-    const double* JG = s.J + gi * nt1;
     double adh = 0.0;
     int cl = 0, cg = 0;
+    if (s.dj != nullptr) {
+        const double* D = s.dj + (int64_t)(li * nt1 + gi) * nt1;
+        const double jgl = __ldg(s.J + gi * nt1 + li);   // neighbour == losing: after - 0.0
+        const double jlg = -__ldg(s.J + li * nt1 + gi);  // neighbour == gaining: 0.0 - before
 #pragma unroll
-    for (int k = 0; k < NE; ++k) {
-        const uint32_t nc = (uint32_t)sig[t + s.energy_off[k]];
-        cl += nc == L;
-        cg += nc == G;
-        const int ni = adh_of[nc];
-        const double before = nc != L ? JL[ni] : 0.0;
-        const double after = nc != G ? JG[ni] : 0.0;
-        adh = __dadd_rn(adh, __dsub_rn(after, before));  // w == 1.0: w*x == x
+        for (int k = 0; k < NE; ++k) {
+            const uint32_t nc = (uint32_t)sig[t + s.energy_off[k]];
+            const bool isl = nc == L, isg = nc == G;
+            cl += isl;
+            cg += isg;
+            const double d = isl ? jgl : (isg ? jlg : __ldg(D + adh_of[nc]));
+            adh = __dadd_rn(adh, d);
+        }
+    } else {
+        const double* JL = s.J + li * nt1;
+        const double* JG = s.J + gi * nt1;
+#pragma unroll
+        for (int k = 0; k < NE; ++k) {
+            const uint32_t nc = (uint32_t)sig[t + s.energy_off[k]];
+            cl += nc == L;
+            cg += nc == G;
+            const int ni = adh_of[nc];
+            const double before = nc != L ? JL[ni] : 0.0;
+            const double after = nc != G ? JG[ni] : 0.0;
+            adh = __dadd_rn(adh, __dsub_rn(after, before));  // w == 1.0: w*x == x
+        }
     }
     DeltaOut o;
     o.dl = 2 * cl - NE;  // sum_k (n == L ? +1 : -1)
@@ -114,35 +141,51 @@ __device__ __forceinline__ DeltaOut delta_h(const SimDesc& s, const SigT* sig, c
     double vol = 0.0, itf = 0.0;
     if (L) {
         const int ty = li - 1;
-        const double v = (double)volume[L];
-        vol = __dadd_rn(vol, __dsub_rn(quad_term(s.lambda_v[ty], s.target_v[ty], __dsub_rn(v, 1.0)),
-                                       quad_term(s.lambda_v[ty], s.target_v[ty], v)));
+        const int64_t v = volume[L];
+        vol = __dadd_rn(vol, __dsub_rn(term_of(s.vterm, s.tab_n, ty, s.lambda_v[ty], s.target_v[ty], v - 1),
+                                       term_of(s.vterm, s.tab_n, ty, s.lambda_v[ty], s.target_v[ty], v)));
     }
     if (G) {
         const int ty = gi - 1;
-        const double v = (double)volume[G];
-        vol = __dadd_rn(vol, __dsub_rn(quad_term(s.lambda_v[ty], s.target_v[ty], __dadd_rn(v, 1.0)),
-                                       quad_term(s.lambda_v[ty], s.target_v[ty], v)));
+        const int64_t v = volume[G];
+        vol = __dadd_rn(vol, __dsub_rn(term_of(s.vterm, s.tab_n, ty, s.lambda_v[ty], s.target_v[ty], v + 1),
+                                       term_of(s.vterm, s.tab_n, ty, s.lambda_v[ty], s.target_v[ty], v)));
     }
     if (L) {
         const int ty = li - 1;
-        const double i = (double)interface[L];
-        itf = __dadd_rn(itf, __dsub_rn(quad_term(s.lambda_i[ty], s.target_i[ty], __dadd_rn(i, (double)o.dl)),
-                                       quad_term(s.lambda_i[ty], s.target_i[ty], i)));
+        const int64_t i = interface[L];
+        itf = __dadd_rn(itf, __dsub_rn(term_of(s.iterm, s.tab_n, ty, s.lambda_i[ty], s.target_i[ty], i + o.dl),
+                                       term_of(s.iterm, s.tab_n, ty, s.lambda_i[ty], s.target_i[ty], i)));
     }
     if (G) {
         const int ty = gi - 1;
-        const double i = (double)interface[G];
-        itf = __dadd_rn(itf, __dsub_rn(quad_term(s.lambda_i[ty], s.target_i[ty], __dadd_rn(i, (double)o.dg)),
-                                       quad_term(s.lambda_i[ty], s.target_i[ty], i)));
+        const int64_t i = interface[G];
+        itf = __dadd_rn(itf, __dsub_rn(term_of(s.iterm, s.tab_n, ty, s.lambda_i[ty], s.target_i[ty], i + o.dg),
+                                       term_of(s.iterm, s.tab_n, ty, s.lambda_i[ty], s.target_i[ty], i)));
     }
     o.dh = __dadd_rn(__dadd_rn(vol, itf), adh);
     return o;
 }
 
-// Metropolis arm of decide_acceptance (monte_carlo.rs:158).
+// Metropolis arm of decide_acceptance (monte_carlo.rs:158):
+// dh <= 0 || u < exp(-dh), with exp the FP64 exponential. The FP64 exp is
+// only evaluated near the decision threshold: expf(x) has at most 2 ulp
+// error (relative 2.4e-7), rounding -dh to float moves exp by at most
+// |dh| * 2^-24 relative (<= 3.9e-6 for dh <= 64), and rounding u to float
+// 2^-24; a relative band of 2e-5 around expf therefore contains the exact
+// threshold, and outside the band the FP32 comparison gives the FP64 answer.
+// For dh > 64, exp(-dh) < 1.7e-28 while u is 0 or >= 2^-53.
 __device__ __forceinline__ bool metropolis(double dh, double u) {
-    return dh <= 0.0 || u < exp(-dh);
+    if (dh <= 0.0) return true;
+    if (dh > 64.0) {
+        if (u > 1e-20) return false;
+        return u < exp(-dh);
+    }
+    const float ef = expf(-(float)dh);
+    const float uf = (float)u;
+    if (uf < ef * 0.99998f) return true;
+    if (uf > ef * 1.00002f) return false;
+    return u < exp(-dh);
 }
 
 // ------------------------------------------------------------- commit ----

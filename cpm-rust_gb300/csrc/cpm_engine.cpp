@@ -74,6 +74,7 @@ const uint64_t* device_table3d(std::string& err) {
 
 // --------------------------------------------------------- DeviceSims ----
 DeviceSims::~DeviceSims() {
+    if (d_bar_) cudaFree(d_bar_);
     if (arena_) cudaFree(arena_);
     if (d_descs_) cudaFree(d_descs_);
     if (d_plans_) cudaFree(d_plans_);
@@ -98,6 +99,9 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
     // Selects the global-memory sweep for every simulation (used by the
     // tests to exercise that path on small lattices).
     force_global_ = std::getenv("CPM_GPU_FORCE_GLOBAL") != nullptr;
+    // Selects the tiled sweep wherever it applies (tests use it on lattices
+    // small enough for the resident sweep).
+    force_tiled_ = std::getenv("CPM_GPU_FORCE_TILED") != nullptr;
     const size_t N = configs.size();
     layouts_.resize(N);
     descs_.resize(N);
@@ -105,7 +109,8 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
     table2d(t2);
     bool need_t3 = false;
     // ---- sizes
-    struct Offs { size_t sigma, adh, vol, itf, sp, so, slots, stats, J, lv, li, tv, ti, energy, svol, sitf, ssp, sso, slat, err; };
+    struct Offs { size_t sigma, adh, vol, itf, sp, so, slots, stats, J, lv, li, tv, ti, vt, it, dj, energy, svol, sitf, ssp, sso, slat, err; };
+    std::vector<int> tab_n(N);
     std::vector<Offs> offs(N);
     Carve cv;
     for (size_t i = 0; i < N; ++i) {
@@ -134,6 +139,12 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
         o.li = cv.take(nt * 8);
         o.tv = cv.take(nt * 4);
         o.ti = cv.take(nt * 4);
+        uint32_t tmax = 0;
+        for (auto& t : c.types) tmax = std::max({tmax, t.target_volume, t.target_interface});
+        tab_n[i] = (int)std::min<uint64_t>(8192, 2 * (uint64_t)tmax + 128);
+        o.vt = cv.take(nt * (size_t)tab_n[i] * 8);
+        o.it = cv.take(nt * (size_t)tab_n[i] * 8);
+        o.dj = cv.take((nt + 1) * (nt + 1) * (nt + 1) * 8);
         o.energy = cv.take((size_t)std::max(1, L.n_energy) * 8);
         o.svol = cv.take((size_t)L.n_samples * n1 * 4);
         o.sitf = cv.take((size_t)L.n_samples * n1 * 4);
@@ -169,6 +180,7 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
         std::memcpy(stage.data() + o.itf, dv.interface.data(), n1 * 4);
         std::memcpy(stage.data() + o.sp, dv.sum_pos.data(), dv.sum_pos.size() * 8);
         std::memcpy(stage.data() + o.so, dv.sum_outer.data(), dv.sum_outer.size() * 8);
+        std::memset(stage.data() + o.slots, 0xFF, n1 * 8);
         std::vector<double> J((nt + 1) * (nt + 1));
         for (size_t a = 0; a <= nt; ++a)
             for (size_t b = 0; b <= nt; ++b) J[a * (nt + 1) + b] = c.adhesion[a][b];
@@ -179,6 +191,31 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
             std::memcpy(stage.data() + o.li + t * 8, &li, 8);
             std::memcpy(stage.data() + o.tv + t * 4, &c.types[t].target_volume, 4);
             std::memcpy(stage.data() + o.ti + t * 4, &c.types[t].target_interface, 4);
+        }
+        // Exact term tables: the device adds these values where it would
+        // otherwise compute lambda * ((x - target) * (x - target)) and
+        // J[g][k] - J[l][k]; -ffp-contract=off keeps every operation a
+        // separately rounded f64 operation, as on the device.
+        {
+            const int tn = tab_n[i];
+            std::vector<double> vt(nt * (size_t)tn), it(nt * (size_t)tn);
+            for (size_t t = 0; t < nt; ++t) {
+                const double lv = c.types[t].lambda_volume, li = c.types[t].lambda_interface;
+                const double tv = (double)c.types[t].target_volume, ti = (double)c.types[t].target_interface;
+                for (int x = 0; x < tn; ++x) {
+                    const double dv = (double)x - tv, di = (double)x - ti;
+                    vt[t * tn + x] = lv * (dv * dv);
+                    it[t * tn + x] = li * (di * di);
+                }
+            }
+            std::memcpy(stage.data() + o.vt, vt.data(), vt.size() * 8);
+            std::memcpy(stage.data() + o.it, it.data(), it.size() * 8);
+            const size_t n1t = nt + 1;
+            std::vector<double> dj(n1t * n1t * n1t);
+            for (size_t l = 0; l < n1t; ++l)
+                for (size_t g = 0; g < n1t; ++g)
+                    for (size_t k = 0; k < n1t; ++k) dj[(l * n1t + g) * n1t + k] = J[g * n1t + k] - J[l * n1t + k];
+            std::memcpy(stage.data() + o.dj, dj.data(), dj.size() * 8);
         }
         // descriptor
         SimDesc& s = descs_[i];
@@ -205,8 +242,10 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
         }
         auto cs = stencil(NBH_VON_NEUMANN, c.D);
         s.n_copy = (int)cs.size();
-        for (size_t k = 0; k < cs.size(); ++k)
+        for (size_t k = 0; k < cs.size(); ++k) {
             s.copy_off[k] = cs[k][0] * L.g.strides[0] + cs[k][1] * L.g.strides[1] + cs[k][2] * L.g.strides[2];
+            for (int d = 0; d < 3; ++d) s.copy_vec[k][d] = (int8_t)cs[k][d];
+        }
         auto es = stencil(c.energy_nbh, c.D);
         s.n_energy = (int)es.size();
         s.energy_pos_mask = 0;
@@ -219,8 +258,10 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
             }
         }
         auto ts = stencil(c.D == 2 ? NBH_MOORE : NBH_TWENTY_SIX, c.D);
-        for (size_t k = 0; k < ts.size(); ++k)
+        for (size_t k = 0; k < ts.size(); ++k) {
             s.topo_off[k] = ts[k][0] * L.g.strides[0] + ts[k][1] * L.g.strides[1] + ts[k][2] * L.g.strides[2];
+            for (int d = 0; d < 3; ++d) s.topo_vec[k][d] = (int8_t)ts[k][d];
+        }
         std::memcpy(s.table2d, t2, sizeof t2);
         s.n_types = (int)nt;
         s.min_cell_volume = c.min_cell_volume;
@@ -240,6 +281,10 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
         s.lambda_i = (const double*)(base + o.li);
         s.target_v = (const uint32_t*)(base + o.tv);
         s.target_i = (const uint32_t*)(base + o.ti);
+        s.vterm = (const double*)(base + o.vt);
+        s.iterm = (const double*)(base + o.it);
+        s.dj = (const double*)(base + o.dj);
+        s.tab_n = tab_n[i];
         s.mcs = 0;
         s.energy_out = (double*)(base + o.energy);
         s.sample_volume = (uint32_t*)(base + o.svol);
@@ -256,27 +301,87 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
     return "";
 }
 
-// Whether simulation i runs on the shared-memory-resident path.
-bool DeviceSims::resident(size_t i) const {
+DeviceSims::Path DeviceSims::path(size_t i) const {
     const SimLayout& L = layouts_[i];
-    if (force_global_) return false;
-    if (L.n_cells >= 65535) return false;
-    return cpmgpu::resident_smem_bytes(L.g.n_padded, L.n_cells) <= cpmgpu::resident_smem_limit();
+    if (force_global_) return GLOBAL;
+    if (L.n_cells >= 65535) return GLOBAL;
+    if (!force_tiled_ && cpmgpu::resident_smem_bytes(L.g.n_padded, L.n_cells) <= cpmgpu::resident_smem_limit())
+        return RESIDENT;
+    int dims[3] = {(int)L.g.dims[0], (int)L.g.dims[1], (int)L.g.dims[2]}, nt[3], max_box = 0;
+    if (cpmgpu::tiled_plan(L.g.D, dims, L.g.periodic, nt, &max_box) &&
+        cpmgpu::tiled_smem_bytes(max_box, L.n_cells) <= cpmgpu::resident_smem_limit())
+        return TILED;
+    return GLOBAL;
+}
+
+// One simulation on the tiled sweep: the run window is replayed from the
+// host, one cooperative launch per chunk plus energy and sample launches.
+std::string DeviceSims::run_tiled(const RunPlan& p, const uint64_t* t3) {
+    const SimLayout& L = layouts_[p.sim];
+    int dims[3] = {(int)L.g.dims[0], (int)L.g.dims[1], (int)L.g.dims[2]}, nt[3], max_box = 0;
+    cpmgpu::tiled_plan(L.g.D, dims, L.g.periodic, nt, &max_box);
+    const size_t smem = cpmgpu::tiled_smem_bytes(max_box, L.n_cells);
+    int per_sm = 0, dev = 0, sms = 1;
+    CUDA_TRY(cpmgpu::tiled_occupancy(L.g.D, L.NE, smem, &per_sm));
+    CUDA_TRY(cudaGetDevice(&dev));
+    CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    int tiles = 1;
+    for (int d = 0; d < L.g.D; ++d) tiles *= nt[d];
+    const int grid = std::max(1, std::min(tiles >> L.g.D, std::max(1, per_sm) * sms));
+    if (!d_bar_) CUDA_TRY(cudaMalloc(&d_bar_, 64));
+    SimDesc* d_sim = d_descs_ + p.sim;
+    unsigned long long* claims = descs_[p.sim].slots;
+    auto chunk = [&](uint64_t n) -> std::string {
+        if (n == 0) return "";
+        CUDA_TRY(cudaMemsetAsync(d_bar_, 0, 64, stream_));
+        CUDA_TRY(cpmgpu::launch_tiled(L.g.D, L.NE, d_sim, n, nt, d_bar_, claims, t3, max_box, smem, grid, stream_));
+        return "";
+    };
+    std::string e;
+    uint64_t burned = 0;
+    int e_idx = 0;
+    while (burned < p.burn_in) {
+        const uint64_t c = std::min(p.interval, p.burn_in - burned);
+        if (!(e = chunk(c)).empty()) return e;
+        burned += c;
+        if (burned >= p.energy_sample_start) {
+            if (descs_[p.sim].energy_out && e_idx < L.n_energy)
+                CUDA_TRY(cpmgpu::launch_energy(L.g.D, L.NE, d_sim, descs_[p.sim].energy_out + e_idx, stream_));
+            ++e_idx;
+        }
+    }
+    for (int smp = 0; smp < p.n_samples; ++smp) {
+        if (!(e = chunk(p.interval)).empty()) return e;
+        if (descs_[p.sim].energy_out && e_idx + smp < L.n_energy)
+            CUDA_TRY(cpmgpu::launch_energy(L.g.D, L.NE, d_sim, descs_[p.sim].energy_out + e_idx + smp, stream_));
+        if (p.write_samples)
+            CUDA_TRY(cpmgpu::launch_sample(L.g.D, d_sim, smp, p.write_lattice, L.g.n_sites, stream_));
+    }
+    tiled_ran_.push_back(p.sim);
+    return "";
 }
 
 std::string DeviceSims::run(const std::vector<RunPlan>& plans, int grid_override) {
     std::string err;
     const uint64_t* t3 = nullptr;
-    // group plans by kernel variant: (resident?, D, NE)
+    // group plans by kernel variant: (resident?, D, NE); tiled plans run one by one
     std::map<std::tuple<int, int, int>, std::vector<RunPlan>> groups;
+    std::vector<RunPlan> tiled;
     for (const RunPlan& p : plans) {
         const SimLayout& L = layouts_[p.sim];
-        groups[std::make_tuple(resident(p.sim) ? 1 : 0, L.g.D, L.NE)].push_back(p);
         if (L.g.D == 3 && !t3) {
             t3 = device_table3d(err);
             if (!t3) return err;
         }
+        const Path pa = path(p.sim);
+        if (pa == TILED) { tiled.push_back(p); continue; }
+        groups[std::make_tuple(pa == RESIDENT ? 1 : 0, L.g.D, L.NE)].push_back(p);
     }
+    for (const RunPlan& p : tiled) {
+        err = run_tiled(p, t3);
+        if (!err.empty()) return err;
+    }
+    if (groups.empty()) return "";
     size_t total = 0;
     for (auto& kv : groups) total += kv.second.size();
     if (total > plans_cap_) {
@@ -329,6 +434,13 @@ std::string DeviceSims::run(const std::vector<RunPlan>& plans, int grid_override
 
 std::string DeviceSims::sync() {
     CUDA_TRY(cudaStreamSynchronize(stream_));
+    // bounded device waits record a timeout instead of hanging
+    for (size_t i : tiled_ran_) {
+        int32_t err = 0;
+        CUDA_TRY(cudaMemcpy(&err, descs_[i].error, 4, cudaMemcpyDeviceToHost));
+        if (err) return "CUDA error: device wait timed out in the tiled sweep (error " + std::to_string(err) + ")";
+    }
+    tiled_ran_.clear();
     return "";
 }
 

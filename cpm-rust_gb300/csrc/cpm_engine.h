@@ -43,8 +43,11 @@ class DeviceSims {
     // persistent launch per (D, energy stencil) group.
     std::string run(const std::vector<RunPlan>& plans, int grid_override = 0);
     std::string sync();
-    // Whether simulation i runs shared-memory resident (else the global-memory sweep).
-    bool resident(size_t i) const;
+    // Which sweep simulation i runs: shared-memory resident, tiled
+    // (cooperative, all SMs on one lattice) or the global-memory sweep.
+    enum Path { RESIDENT = 0, TILED = 1, GLOBAL = 2 };
+    Path path(size_t i) const;
+    bool resident(size_t i) const { return path(i) == RESIDENT; }
     void force_global(bool on) { force_global_ = on; }
     // Bytes this object copied host-to-device / device-to-host so far.
     uint64_t h2d_bytes() const { return h2d_bytes_; }
@@ -80,6 +83,10 @@ class DeviceSims {
     char* arena_ = nullptr;
     cudaStream_t stream_ = 0;
     bool force_global_ = false;
+    bool force_tiled_ = false;
+    void* d_bar_ = nullptr;
+    std::vector<size_t> tiled_ran_;
+    std::string run_tiled(const RunPlan& p, const uint64_t* t3);
     uint64_t h2d_bytes_ = 0;
     mutable std::atomic<uint64_t> d2h_bytes_{0};
 };

@@ -209,8 +209,7 @@ __device__ void color_pass(const SimDesc& s, const PassInfo& p, uint64_t mcs, ui
                 if (L != 0 && volume[L] <= s.min_cell_volume) { ct.guard_reject++; continue; }
                 ct.evaluated++;
                 const DeltaOut o = delta_h<NE, uint32_t>(s, sig, adh_of, volume, interface, t, L, G);
-                bool acc = o.dh <= 0.0;
-                if (!acc) acc = u53(site_draw(s.seed, mcs, (uint32_t)t)) < exp(-o.dh);
+                const bool acc = metropolis(o.dh, o.dh > 0.0 ? u53(site_draw(s.seed, mcs, (uint32_t)t)) : 0.0);
                 if (acc) {
                     commit_move<D, uint32_t>(s, sig, volume, interface, s.sum_pos, s.sum_outer, x, L, G, o.dl, o.dg);
                     ct.accepted++;
@@ -423,6 +422,34 @@ __global__ void energy_kernel(const SimDesc* simp, double* out) {
     if (threadIdx.x == 0) *out = e;
 }
 
+// One readout sample of a simulation whose state lives in HBM (the tiled
+// path): V, I and the position sums into sample `smp`, and optionally the
+// unpadded lattice.
+template <int D>
+__global__ void sample_kernel(const SimDesc* simp, int smp, int write_lattice) {
+    const SimDesc& s = *simp;
+    const int64_t n1 = s.n_cells + 1;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t id = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; id < n1; id += stride) {
+        s.sample_volume[smp * n1 + id] = __ldcg(s.volume + id);
+        s.sample_interface[smp * n1 + id] = __ldcg(s.interface + id);
+        for (int d = 0; d < D; ++d)
+            s.sample_sum_pos[(smp * n1 + id) * D + d] = __ldcg((const long long*)s.sum_pos + id * D + d);
+        for (int d = 0; d < D * D; ++d)
+            s.sample_sum_outer[(smp * n1 + id) * D * D + d] = __ldcg((const long long*)s.sum_outer + id * D * D + d);
+    }
+    if (write_lattice && s.sample_lattice) {
+        for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < s.n_sites; q += stride) {
+            int64_t r = q, f = 0;
+            for (int d = D - 1; d >= 0; --d) {
+                f += (r % s.dims[d] + 1) * s.strides[d];
+                r /= s.dims[d];
+            }
+            s.sample_lattice[(int64_t)smp * s.n_sites + q] = __ldcg(s.sigma + f);
+        }
+    }
+}
+
 // 3D simple-point table: bit p set iff pattern p is simple (FastChecker).
 __global__ void table3d_kernel(uint64_t* words, const uint32_t* face_adj, const uint32_t* full_adj,
                                uint32_t origin_face_mask) {
@@ -536,6 +563,15 @@ cudaError_t launch_recount(int Dd, int NEd, const SimDesc* d_sim, int64_t n_site
 
 cudaError_t launch_energy(int Dd, int NEd, const SimDesc* d_sim, double* d_out, cudaStream_t st) {
     CPM_DISPATCH(Dd, NEd, { energy_kernel<D, NE><<<1, 256, 0, st>>>(d_sim, d_out); });
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sample(int Dd, const SimDesc* d_sim, int sample, int write_lattice, int64_t n_sites, cudaStream_t st) {
+    int grid = (int)((n_sites + 255) / 256);
+    if (grid > 4096) grid = 4096;
+    if (grid < 1) grid = 1;
+    if (Dd == 2) sample_kernel<2><<<grid, 256, 0, st>>>(d_sim, sample, write_lattice);
+    else sample_kernel<3><<<grid, 256, 0, st>>>(d_sim, sample, write_lattice);
     return cudaGetLastError();
 }
 

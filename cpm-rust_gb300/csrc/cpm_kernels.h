@@ -27,4 +27,14 @@ int resident_block();
 cudaError_t launch_resident(int D, int NE, SimDesc* d_sims, const RunPlan* d_plans, int n_plans, int* d_next,
                             const uint64_t* d_t3, size_t smem, int grid, cudaStream_t st);
 cudaError_t resident_occupancy(int D, int NE, size_t smem, int* blocks_per_sm);
+// Tiled cooperative sweep for large lattices (cpm_tiled.cu).
+bool tiled_plan(int D, const int* dims, int periodic, int* nt, int* max_box);
+size_t tiled_smem_bytes(int max_box, int n_cells);
+int tiled_block();
+cudaError_t tiled_occupancy(int D, int NE, size_t smem, int* per_sm);
+cudaError_t launch_tiled(int D, int NE, SimDesc* d_sim, uint64_t n_mcs, const int* nt, void* d_barrier,
+                         unsigned long long* d_claims, const uint64_t* d_t3, int max_box, size_t smem, int grid,
+                         cudaStream_t st);
+// Copies one sample (V, I, position sums, optional lattice) of simulation d_sim.
+cudaError_t launch_sample(int D, const SimDesc* d_sim, int sample, int write_lattice, int64_t n_sites, cudaStream_t st);
 }  // namespace cpmgpu

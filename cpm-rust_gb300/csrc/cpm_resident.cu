@@ -198,9 +198,7 @@ struct Resident {
             fl |= F_GUARD;
         } else {
             const DeltaOut o = delta_h<NE, uint16_t>(s, sig, adh, vol, itf, t, L, G);
-            bool acc = o.dh <= 0.0;
-            if (!acc) acc = u53(site_draw(s.seed, mcs, (uint32_t)t)) < exp(-o.dh);
-            if (acc) fl |= F_ACC;
+            if (metropolis(o.dh, o.dh > 0.0 ? u53(site_draw(s.seed, mcs, (uint32_t)t)) : 0.0)) fl |= F_ACC;
             c_dl[c] = (int16_t)((o.dl & 0xFF) | ((o.dg & 0xFF) << 8));
         }
         c_flags[c] = fl;

@@ -1,0 +1,775 @@
+// Tiled sweep for lattices too large for one CTA's shared memory.
+//
+// Every MCS the lattice is cut into an even number of tiles per axis, at a
+// random offset (periodic lattices), and the tiles are coloured by the
+// parity of their tile coordinates (4 colours in 2D, 8 in 3D). A sub-phase
+// processes all tiles of one colour at once, one CTA per tile: same-colour
+// tiles are a whole tile apart, so no attempt in one reads a site another
+// writes. A cell that reaches into two tiles of the same colour would couple
+// them through its volume and interface; each sub-phase therefore starts
+// with a claim step: every active tile registers the cells of its box with
+// a 64-bit atomicMin of (sub-phase epoch, tile id), a grid barrier follows,
+// and a tile only changes cells it owns (the lowest claiming tile). Moves
+// that involve a cell owned by another tile are counted and skipped (for
+// compact cells this needs a cell wider than a tile, ~21 sites).
+//
+// Inside its tile a CTA stages the box (tile + 1-site rim) into shared
+// memory, runs the site-colour passes of the tile in random order, and
+// resolves each pass exactly as the resident sweep does (speculative FP64
+// evaluation, then the fixpoint that finalises rejection chains, then
+// parallel commits of cell-disjoint accepts). It then writes the tile's
+// sites (plus their periodic halo mirrors), the owned cells' V/I and
+// nothing else back to HBM; the position sums are updated in place with
+// L2-coherent accesses.
+//
+// All CTAs are co-resident (cooperative launch); the grid barrier is a
+// counter/generation pair with a bounded spin that records a timeout and
+// returns instead of hanging.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "cpm_common.h"
+#include "cpm_device.cuh"
+#include "cpm_kernels.h"
+
+namespace cpmgpu {
+
+constexpr int TB = 256;          // threads per CTA
+constexpr int TCMAX = 1024;      // candidate slots per tile pass
+constexpr int TMAX_BOX = 48 * 48 * 48;  // largest shared box (sites)
+enum : uint32_t {
+    T_ACC = 1u << 3, T_PEND = 1u << 4, T_FIN = 1u << 5, T_GUARD = 1u << 6, T_DONE = 1u << 7,
+};
+enum : uint32_t { TAG_TILE = 3u };
+
+struct TileGrid {
+    int nt[3];        // tiles per axis (even)
+    int off[3];       // tiling offset per axis (periodic) or 0
+    int colors;       // 2^D
+};
+
+// Tile j on an axis covers global coordinates [off + b_j, off + b_{j+1}) mod L,
+// b_j = floor(j * L / nt).
+__device__ __forceinline__ int tile_begin(int j, int L, int nt) { return (int)(((long long)j * L) / nt); }
+
+struct BarrierState {
+    unsigned int count;
+    unsigned int gen;
+    int error;
+    int pad;
+};
+
+// Grid barrier with a bounded spin (~2 s): returns false after a timeout.
+__device__ bool grid_sync(BarrierState* b, unsigned int n) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned int* vgen = &b->gen;
+        const unsigned int g = *vgen;
+        __threadfence();
+        const unsigned int arrived = atomicAdd(&b->count, 1u);
+        int ok = 1;
+        if (arrived == n - 1) {
+            b->count = 0;
+            __threadfence();
+            atomicAdd(&b->gen, 1u);
+        } else {
+            long long spins = 0;
+            while (*vgen == g) {
+                __nanosleep(64);
+                if (++spins > 20000000LL || *((volatile int*)&b->error)) { ok = 0; break; }
+            }
+        }
+        __threadfence();
+        if (!ok) atomicExch(&b->error, 1);
+        s_ok = ok && !*((volatile int*)&b->error);
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+struct TileCounters {
+    unsigned long long nonnull, topo, guard, evaluated, accepted, rounds, deferred, wide;
+    unsigned long long c_build, c_eval, c_fix, c_apply;
+};
+
+template <int D, int NE>
+struct TileProc {
+    const SimDesc& g;     // global descriptor
+    SimDesc& l;           // box descriptor: local strides/offsets, same parameters
+    uint16_t* sig;        // box sigma
+    int* gx0;             // global interior coordinate of box position 1 on each axis
+    uint32_t *vol, *itf, *b0, *b1;
+    uint16_t* adh;
+    uint8_t *dirty, *own, *mod;
+    uint32_t *c_site, *c_key, *c_cells, *c_flags, *c_gf;
+    int16_t* c_dl;
+    const uint64_t* t3;
+    int* s_n;
+
+    __device__ int gcoord(int d, int local) const {  // box position -> global interior coordinate
+        int x = gx0[d] + local - 1;
+        const int L = g.dims[d];
+        if (g.periodic) { x %= L; if (x < 0) x += L; }
+        return x;
+    }
+    __device__ int gflat_of_box(int lt, int* xg) const {
+        int f = 0, r = lt;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const int q = r / (int)l.strides[d];
+            r -= q * (int)l.strides[d];
+            xg[d] = gcoord(d, q);
+            f += (xg[d] + 1) * (int)g.strides[d];
+        }
+        return f;
+    }
+
+    __device__ void evaluate(int c, uint64_t mcs) {
+        const int t = (int)c_site[c];
+        const uint32_t cells = c_cells[c];
+        const uint32_t L = cells & 0xFFFFu, G = cells >> 16;
+        uint32_t fl = c_flags[c] & ~(T_ACC | T_GUARD);
+        if (L != 0 && vol[L] <= l.min_cell_volume) {
+            fl |= T_GUARD;
+        } else {
+            const DeltaOut o = delta_h<NE, uint16_t>(l, sig, adh, vol, itf, t, L, G);
+            const double u = o.dh > 0.0 ? u53(site_draw(g.seed, mcs, c_gf[c])) : 0.0;
+            if (metropolis(o.dh, u)) fl |= T_ACC;
+            c_dl[c] = (int16_t)((o.dl & 0xFF) | ((o.dg & 0xFF) << 8));
+        }
+        c_flags[c] = fl;
+    }
+
+    // Commit in shared memory; position sums in HBM through L2. `mark` sets
+    // the dirty bytes the block-wide resolve uses to find re-evaluations.
+    __device__ void commit(int c, bool mark = true) {
+        const int t = (int)c_site[c];
+        const uint32_t cells = c_cells[c];
+        const uint32_t L = cells & 0xFFFFu, G = cells >> 16;
+        const int16_t dd = c_dl[c];
+        const int dl = (int)(int8_t)(dd & 0xFF), dg = (int)(int8_t)((dd >> 8) & 0xFF);
+        int xg[3];
+        gflat_of_box(t, xg);
+        sig[t] = (uint16_t)G;
+        if (L) {
+            vol[L] -= 1;
+            itf[L] += (uint32_t)dl;
+            long long* sp = (long long*)g.sum_pos + (long long)L * D;
+            long long* so = (long long*)g.sum_outer + (long long)L * D * D;
+#pragma unroll
+            for (int d = 0; d < D; ++d) __stcg(sp + d, __ldcg(sp + d) - xg[d]);
+#pragma unroll
+            for (int d = 0; d < D; ++d)
+#pragma unroll
+                for (int e = 0; e < D; ++e) __stcg(so + d * D + e, __ldcg(so + d * D + e) - (long long)xg[d] * xg[e]);
+            if (mark) dirty[L] = 1;
+            mod[L] = 1;
+        }
+        if (G) {
+            const uint32_t vnew = vol[G] + 1;
+            vol[G] = vnew;
+            itf[G] += (uint32_t)dg;
+            uint32_t vb = vnew >= 1 ? vnew - 1 : 0;
+            if (vb < 1) vb = 1;
+            long long* sp = (long long*)g.sum_pos + (long long)G * D;
+            long long* so = (long long*)g.sum_outer + (long long)G * D * D;
+            long long img[3];
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                const double cen = (double)__ldcg(sp + d) / (double)vb;
+                img[d] = nearest_image(xg[d], cen, g.dims[d], g.periodic != 0);
+            }
+#pragma unroll
+            for (int d = 0; d < D; ++d) __stcg(sp + d, __ldcg(sp + d) + img[d]);
+#pragma unroll
+            for (int d = 0; d < D; ++d)
+#pragma unroll
+                for (int e = 0; e < D; ++e) __stcg(so + d * D + e, __ldcg(so + d * D + e) + img[d] * img[e]);
+            if (mark) dirty[G] = 1;
+            mod[G] = 1;
+        }
+    }
+
+    // Resolution of a pass with n <= 32 candidates by one warp, candidate =
+    // lane, with the same outcome as resolve(): `lower` holds the
+    // lower-priority candidates that share a cell (the medium is not a
+    // cell); a pending candidate is final once every lower pending one is a
+    // final reject; final accepts are pairwise cell-disjoint and commit; a
+    // pending candidate with a committed lower neighbour re-evaluates (a
+    // committed candidate sharing a cell with a pending one always has the
+    // lower key, or the pending one would have been a final reject).
+    __device__ void resolve_warp(int n, uint64_t mcs, TileCounters& ct) {
+        const unsigned FULL = 0xffffffffu;
+        const int lane = threadIdx.x & 31;
+        const bool have = lane < n;
+        long long t0 = clock64();
+        if (have) evaluate(lane, mcs);
+        const uint32_t cells = have ? c_cells[lane] : 0u;
+        const uint32_t key = have ? c_key[lane] : 0xFFFFFFFFu;
+        const uint32_t L = cells & 0xFFFFu, G = cells >> 16;
+        uint32_t lower = 0;
+        for (int j = 0; j < n; ++j) {
+            const uint32_t cj = __shfl_sync(FULL, cells, j);
+            const uint32_t kj = __shfl_sync(FULL, key, j);
+            const uint32_t Lj = cj & 0xFFFFu, Gj = cj >> 16;
+            const bool share = (L && (L == Lj || L == Gj)) || (G && (G == Lj || G == Gj));
+            if (share && kj < key) lower |= 1u << j;
+        }
+        __syncwarp();
+        uint32_t fl = have ? c_flags[lane] : 0u;
+        uint32_t pending = __ballot_sync(FULL, have);
+        long long t1 = clock64();
+        ct.c_eval += t1 - t0;
+        while (pending) {
+            t0 = clock64();
+            const bool mine = (pending >> lane) & 1u;
+            const bool rej = (fl & T_GUARD) || !(fl & T_ACC);
+            uint32_t fin = 0;
+            for (;;) {
+                const uint32_t frej = __ballot_sync(FULL, ((fin >> lane) & 1u) && rej);
+                const uint32_t nf = __ballot_sync(FULL, mine && (lower & pending & ~frej) == 0);
+                if (nf == fin) break;
+                fin = nf;
+            }
+            t1 = clock64();
+            ct.c_fix += t1 - t0;
+            const bool is_fin = (fin >> lane) & 1u;
+            const bool commit_me = is_fin && !rej;
+            if (is_fin) {
+                if (fl & T_GUARD) ct.guard++;
+                else ct.evaluated++;
+            }
+            if (commit_me) {
+                commit(lane, false);
+                ct.accepted++;
+            }
+            const uint32_t committed = __ballot_sync(FULL, commit_me);
+            pending &= ~fin;
+            ct.rounds++;
+            __syncwarp();
+            if (((pending >> lane) & 1u) && (lower & committed)) {
+                evaluate(lane, mcs);
+                fl = c_flags[lane];
+            }
+            __syncwarp();
+            ct.c_apply += clock64() - t1;
+        }
+    }
+
+    __device__ void resolve(int n, uint64_t mcs, TileCounters& ct) {
+        const int tid = threadIdx.x;
+        long long t0 = clock64();
+        for (int c = tid; c < n; c += TB) evaluate(c, mcs);
+        __syncthreads();
+        long long t1 = clock64();
+        ct.c_eval += t1 - t0;
+        for (;;) {
+            t0 = clock64();
+            for (int c = tid; c < n; c += TB) {
+                c_flags[c] &= ~T_FIN;
+                if (!(c_flags[c] & T_PEND)) continue;
+                const uint32_t cells = c_cells[c];
+                if (cells & 0xFFFFu) b0[cells & 0xFFFFu] = 0xFFFFFFFFu;
+                if (cells >> 16) b0[cells >> 16] = 0xFFFFFFFFu;
+            }
+            __syncthreads();
+            uint32_t* bc = b0;
+            uint32_t* bn = b1;
+            for (;;) {
+                for (int c = tid; c < n; c += TB) {
+                    const uint32_t fl = c_flags[c];
+                    if (!(fl & T_PEND)) continue;
+                    if ((fl & T_FIN) && (!(fl & T_ACC) || (fl & T_GUARD))) continue;
+                    const uint32_t cells = c_cells[c], key = c_key[c];
+                    if (cells & 0xFFFFu) atomicMin(&bc[cells & 0xFFFFu], key);
+                    if (cells >> 16) atomicMin(&bc[cells >> 16], key);
+                }
+                __syncthreads();
+                int changed = 0;
+                for (int c = tid; c < n; c += TB) {
+                    uint32_t fl = c_flags[c];
+                    if (!(fl & T_PEND)) continue;
+                    const uint32_t cells = c_cells[c], key = c_key[c];
+                    const uint32_t L = cells & 0xFFFFu, G = cells >> 16;
+                    if (!(fl & T_FIN) && (!L || key <= bc[L]) && (!G || key <= bc[G])) {
+                        fl |= T_FIN;
+                        c_flags[c] = fl;
+                        changed = 1;
+                    }
+                    if (!(fl & T_FIN) || ((fl & T_ACC) && !(fl & T_GUARD))) {
+                        if (L) bn[L] = 0xFFFFFFFFu;
+                        if (G) bn[G] = 0xFFFFFFFFu;
+                    }
+                }
+                const int any = __syncthreads_or(changed);
+                uint32_t* tmp = bc; bc = bn; bn = tmp;
+                if (!any) break;
+            }
+            t1 = clock64();
+            ct.c_fix += t1 - t0;
+            int left = 0;
+            for (int c = tid; c < n; c += TB) {
+                uint32_t fl = c_flags[c];
+                if (!(fl & T_PEND)) continue;
+                if (!(fl & T_FIN)) { left = 1; continue; }
+                fl &= ~(T_PEND | T_FIN);
+                if (fl & T_GUARD) ct.guard++;
+                else {
+                    ct.evaluated++;
+                    if (fl & T_ACC) { commit(c); fl |= T_DONE; ct.accepted++; }
+                }
+                c_flags[c] = fl;
+            }
+            ct.rounds++;
+            const int more = __syncthreads_or(left);
+            ct.c_apply += clock64() - t1;
+            if (!more) break;
+            t1 = clock64();
+            for (int c = tid; c < n; c += TB) {
+                if (!(c_flags[c] & T_PEND)) continue;
+                const uint32_t cells = c_cells[c];
+                if (dirty[cells & 0xFFFFu] || dirty[cells >> 16]) evaluate(c, mcs);
+            }
+            __syncthreads();
+            for (int c = tid; c < n; c += TB) {
+                const uint32_t fl = c_flags[c];
+                if (!(fl & T_DONE)) continue;
+                const uint32_t cells = c_cells[c];
+                dirty[cells & 0xFFFFu] = 0;
+                dirty[cells >> 16] = 0;
+                c_flags[c] = fl & ~T_DONE;
+            }
+            __syncthreads();
+            ct.c_apply += clock64() - t1;
+        }
+        for (int c = tid; c < n; c += TB) {
+            if (!(c_flags[c] & T_DONE)) continue;
+            const uint32_t cells = c_cells[c];
+            dirty[cells & 0xFFFFu] = 0;
+            dirty[cells >> 16] = 0;
+        }
+        __syncthreads();
+    }
+};
+
+struct TileShared {
+    uint32_t sig, vol, itf, b0, b1, adh, dirty, own, mod, seen, c_site, c_key, c_cells, c_flags, c_gf, c_dl, total;
+};
+
+__host__ __device__ inline uint32_t tl_take(uint32_t& off, uint64_t b) {
+    const uint32_t o = off;
+    off = (uint32_t)((off + b + 15) & ~(uint64_t)15);
+    return o;
+}
+__host__ __device__ inline TileShared tile_shared(int box_sites, int n_cells) {
+    TileShared s;
+    uint32_t off = 0;
+    const uint64_t n1 = (uint64_t)n_cells + 1;
+    s.sig = tl_take(off, (uint64_t)box_sites * 2);
+    s.vol = tl_take(off, n1 * 4);
+    s.itf = tl_take(off, n1 * 4);
+    s.b0 = tl_take(off, n1 * 4);
+    s.b1 = tl_take(off, n1 * 4);
+    s.adh = tl_take(off, n1 * 2);
+    s.dirty = tl_take(off, n1);
+    s.own = tl_take(off, n1);
+    s.mod = tl_take(off, n1);
+    s.seen = tl_take(off, n1 * 4);
+    s.c_site = tl_take(off, TCMAX * 4);
+    s.c_key = tl_take(off, TCMAX * 4);
+    s.c_cells = tl_take(off, TCMAX * 4);
+    s.c_flags = tl_take(off, TCMAX * 4);
+    s.c_gf = tl_take(off, TCMAX * 4);
+    s.c_dl = tl_take(off, TCMAX * 2);
+    s.total = off;
+    return s;
+}
+
+template <int D, int NE>
+__global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_mcs, TileGrid tg_in, BarrierState* bar,
+                                                   unsigned long long* claims, const uint64_t* t3, int max_box) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    __shared__ SimDesc gsd, lsd;
+    __shared__ int s_n, s_tile, s_box_dims[3], s_gx0[3], s_tcnt[3];
+    __shared__ int perm[8], sperm[27];
+    __shared__ unsigned long long sstat[8];
+    const int tid = threadIdx.x;
+    if (tid == 0) gsd = *simp;
+    if (tid < 8) sstat[tid] = 0;
+    __syncthreads();
+    const SimDesc& g = gsd;
+    const int nblk = gridDim.x;
+    {
+        uint32_t* seen0 = (uint32_t*)(sm + tile_shared(max_box, g.n_cells).seen);
+        for (int id = tid; id <= g.n_cells; id += TB) seen0[id] = 0u;
+        __syncthreads();
+    }
+    TileCounters ct = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    unsigned long long attempts = 0;
+    unsigned long long cyc_pass = 0, cyc_stage = 0, cyc_sync = 0;
+    const uint64_t mcs0 = g.mcs;
+    bool alive = true;
+    for (uint64_t m = 0; m < n_mcs && alive; ++m) {
+        const uint64_t mcs = mcs0 + m;
+        // ---- tiling of this MCS: random offset (periodic), random tile-colour order
+        TileGrid tg = tg_in;
+        {
+            const uint4 r = aux_draw(g.seed, mcs, TAG_TILE, 0u, 0u);
+            const uint32_t rr[3] = {r.x, r.y, r.z};
+            for (int d = 0; d < D; ++d) tg.off[d] = g.periodic ? (int)(((unsigned long long)rr[d] * (unsigned)g.dims[d]) >> 32) : 0;
+        }
+        if (tid == 0) {
+            for (int c = 0; c < tg.colors; ++c) perm[c] = c;
+            for (int c = tg.colors - 1; c > 0; --c) {
+                const uint4 r = aux_draw(g.seed, mcs, TAG_TILE, 1u, (uint32_t)c);
+                const int j = (int)(((unsigned long long)r.x * (unsigned)(c + 1)) >> 32);
+                const int t = perm[c]; perm[c] = perm[j]; perm[j] = t;
+            }
+        }
+        __syncthreads();
+        int n_tiles = 1;
+        for (int d = 0; d < D; ++d) n_tiles *= tg.nt[d];
+        const int per_color = n_tiles / tg.colors;
+        for (int ci = 0; ci < tg.colors && alive; ++ci) {
+            const int color = perm[ci];
+            const uint64_t epoch = mcs * 8 + (uint64_t)ci;
+            const unsigned long long base_key = (unsigned long long)(0xFFFFFFFFull - (epoch & 0xFFFFFFFFull)) << 32;
+            // tile k of this colour -> tile coordinates: colour bits are the parities
+            auto tile_coords = [&](int k, int* tc) {
+                int rem = k;
+                for (int d = D - 1; d >= 0; --d) {
+                    const int half = tg.nt[d] / 2;
+                    const int q = rem % half;
+                    rem /= half;
+                    tc[d] = 2 * q + ((color >> d) & 1);
+                }
+            };
+            // ---- claim the cells of every box this CTA will process
+            long long t_c0 = clock64();
+            for (int k = blockIdx.x; k < per_color; k += nblk) {
+                int tc[3];
+                tile_coords(k, tc);
+                int bdim[3], x0[3];
+                int box = 1;
+                for (int d = 0; d < D; ++d) {
+                    const int L = g.dims[d];
+                    const int b0 = tile_begin(tc[d], L, tg.nt[d]), b1 = tile_begin(tc[d] + 1, L, tg.nt[d]);
+                    x0[d] = b0 + tg.off[d];
+                    bdim[d] = b1 - b0 + 2;
+                    box *= bdim[d];
+                }
+                const int tile_id = k;
+                const unsigned long long key = base_key | (unsigned long long)tile_id;
+                uint32_t* seen = (uint32_t*)(sm + tile_shared(max_box, g.n_cells).seen);
+                const uint32_t stamp = (uint32_t)(epoch * 1024u + (uint32_t)(k / nblk)) + 1u;
+                for (int q = tid; q < box; q += TB) {
+                    int r = q, gf = 0;
+                    for (int d = D - 1; d >= 0; --d) {
+                        const int i = r % bdim[d];
+                        r /= bdim[d];
+                        int x = x0[d] + i - 1;
+                        if (g.periodic) { x %= g.dims[d]; if (x < 0) x += g.dims[d]; gf += (x + 1) * (int)g.strides[d]; }
+                        else gf += (x + 1) * (int)g.strides[d];
+                    }
+                    const uint32_t id = __ldcg(g.sigma + gf);
+                    if (id && atomicExch(&seen[id], stamp) != stamp) atomicMin(claims + id, key);
+                }
+                __syncthreads();
+            }
+            if (!grid_sync(bar, nblk)) { alive = false; break; }
+            cyc_sync += clock64() - t_c0;
+            // ---- process the tiles
+            for (int k = blockIdx.x; k < per_color; k += nblk) {
+                int tc[3];
+                tile_coords(k, tc);
+                if (tid == 0) {
+                    lsd = gsd;
+                    for (int d = 0; d < D; ++d) {
+                        const int L = g.dims[d];
+                        const int b0 = tile_begin(tc[d], L, tg.nt[d]), b1 = tile_begin(tc[d] + 1, L, tg.nt[d]);
+                        s_gx0[d] = b0 + tg.off[d];
+                        s_tcnt[d] = b1 - b0;
+                        s_box_dims[d] = b1 - b0 + 2;
+                        lsd.dims[d] = b1 - b0;
+                        lsd.pdims[d] = b1 - b0 + 2;
+                    }
+                    int64_t st = 1;
+                    for (int d = D - 1; d >= 0; --d) { lsd.strides[d] = st; st *= lsd.pdims[d]; }
+                    lsd.n_padded = st;
+                    s_tile = k;
+                }
+                __syncthreads();
+                // local stencil offsets from the integer offset vectors (one thread each)
+                if (tid < CPM_MAX_STENCIL) {
+                    const int kk = tid;
+                    int64_t e = 0, t = 0, c = 0;
+                    for (int d = 0; d < D; ++d) {
+                        e += (int64_t)g.energy_vec[kk][d] * lsd.strides[d];
+                        t += (int64_t)g.topo_vec[kk][d] * lsd.strides[d];
+                        if (kk < 6) c += (int64_t)g.copy_vec[kk][d] * lsd.strides[d];
+                    }
+                    if (kk < g.n_energy) lsd.energy_off[kk] = e;
+                    lsd.topo_off[kk] = t;
+                    if (kk < g.n_copy) lsd.copy_off[kk] = c;
+                }
+                __syncthreads();
+                long long t_s0 = clock64();
+                const TileShared ts = tile_shared(max_box, g.n_cells);
+                TileProc<D, NE> P{g, lsd, (uint16_t*)(sm + ts.sig), s_gx0, (uint32_t*)(sm + ts.vol),
+                                  (uint32_t*)(sm + ts.itf), (uint32_t*)(sm + ts.b0), (uint32_t*)(sm + ts.b1),
+                                  (uint16_t*)(sm + ts.adh), (uint8_t*)(sm + ts.dirty), (uint8_t*)(sm + ts.own),
+                                  (uint8_t*)(sm + ts.mod), (uint32_t*)(sm + ts.c_site), (uint32_t*)(sm + ts.c_key),
+                                  (uint32_t*)(sm + ts.c_cells), (uint32_t*)(sm + ts.c_flags), (uint32_t*)(sm + ts.c_gf),
+                                  (int16_t*)(sm + ts.c_dl), t3, &s_n};
+                const unsigned long long key = base_key | (unsigned long long)k;
+                int box = 1;
+                for (int d = 0; d < D; ++d) box *= s_box_dims[d];
+                // stage the box and its cells
+                for (int q = tid; q < box; q += TB) {
+                    int xg[3];
+                    // a fixed lattice's rim outside the box maps to its medium halo
+                    const int gf = P.gflat_of_box(q, xg);
+                    const uint32_t id = __ldcg(g.sigma + gf);
+                    P.sig[q] = (uint16_t)id;
+                    P.vol[id] = __ldcg(g.volume + id);
+                    P.itf[id] = __ldcg(g.interface + id);
+                    P.adh[id] = g.adh_of[id];
+                    P.dirty[id] = 0;
+                    P.mod[id] = 0;
+                    P.own[id] = id == 0 || __ldcg(claims + id) == key;
+                }
+                __syncthreads();
+                long long t_p0 = clock64();
+                cyc_stage += t_p0 - t_s0;
+                // site-colour passes of this tile, random order
+                int ncol = 1;
+                for (int d = 0; d < D; ++d) ncol *= 2;
+                if (tid == 0) {
+                    for (int c = 0; c < ncol; ++c) sperm[c] = c;
+                    for (int c = ncol - 1; c > 0; --c) {
+                        const uint4 r = aux_draw(g.seed, mcs, TAG_TILE, 2u + (uint32_t)k, (uint32_t)c);
+                        const int j = (int)(((unsigned long long)r.x * (unsigned)(c + 1)) >> 32);
+                        const int t = sperm[c]; sperm[c] = sperm[j]; sperm[j] = t;
+                    }
+                }
+                __syncthreads();
+                for (int pi = 0; pi < ncol; ++pi) {
+                    const int sc = sperm[pi];
+                    // local sites with global coordinate parity == colour bit
+                    int cnt[3], base[3];
+                    int n_class = 1;
+                    for (int d = 0; d < D; ++d) {
+                        const int want = (sc >> d) & 1;
+                        const int g0 = ((s_gx0[d] % g.dims[d]) + g.dims[d]) % g.dims[d];
+                        const int first = (want - (g0 & 1)) & 1;  // first local offset with that parity
+                        base[d] = first;
+                        cnt[d] = s_tcnt[d] > first ? (s_tcnt[d] - first + 1) / 2 : 0;
+                        n_class *= cnt[d];
+                    }
+                    const uint32_t pass_key = aux_draw(g.seed, mcs, TAG_PASS, (uint32_t)(pi * 64 + ci), (uint32_t)k).x;
+                    const long long tb0 = clock64();
+                    if (tid == 0) s_n = 0;
+                    __syncthreads();
+                    for (int j0 = 0; j0 < n_class; j0 += TB) {
+                        const int j = j0 + tid;
+                        bool cand = false;
+                        int t = 0, kd = 0, gf = 0;
+                        uint32_t L = 0, G = 0;
+                        if (j < n_class) {
+                            int r = j;
+                            t = 0;
+                            for (int d = D - 1; d >= 0; --d) {
+                                const int i = r % cnt[d];
+                                r /= cnt[d];
+                                t += (base[d] + 2 * i + 1) * (int)lsd.strides[d];
+                            }
+                            int xg[3];
+                            gf = P.gflat_of_box(t, xg);
+                            const uint4 rd = site_draw(g.seed, mcs, (uint32_t)gf);
+                            kd = (int)(((unsigned long long)rd.x * (unsigned)g.n_copy) >> 32);
+                            L = P.sig[t];
+                            G = P.sig[t + (int)lsd.copy_off[kd]];
+                            if (L != G) {
+                                ct.nonnull++;
+                                if (!P.own[L] || !P.own[G]) ct.deferred++;
+                                else if (preserves_topology<D, uint16_t>(lsd, P.sig, t, L, g.table2d, t3)) cand = true;
+                                else ct.topo++;
+                            }
+                        }
+                        const unsigned msk = __ballot_sync(0xffffffffu, cand);
+                        int basepos = 0;
+                        if ((tid & 31) == 0 && msk) basepos = atomicAdd(&s_n, __popc(msk));
+                        basepos = __shfl_sync(0xffffffffu, basepos, 0);
+                        if (cand) {
+                            const int pos = basepos + __popc(msk & ((1u << (tid & 31)) - 1));
+                            if (pos < TCMAX) {
+                                P.c_site[pos] = (uint32_t)t;
+                                P.c_cells[pos] = L | (G << 16);
+                                P.c_key[pos] = (mix32((uint32_t)j * 0x9E3779B9u ^ pass_key) & 0xFFFFC000u) | (uint32_t)j;
+                                P.c_flags[pos] = (uint32_t)kd | T_PEND;
+                                P.c_gf[pos] = (uint32_t)gf;
+                            }
+                        }
+                    }
+                    __syncthreads();
+                    const int n = min(s_n, TCMAX);
+                    __syncthreads();
+                    ct.c_build += clock64() - tb0;
+                    if (n > 32) {
+                        P.resolve(n, mcs, ct);
+                        ct.wide++;
+                    } else if (n > 0) {
+                        if (tid < 32) P.resolve_warp(n, mcs, ct);
+                        __syncthreads();
+                    }
+                    attempts += tid == 0 ? (unsigned long long)n_class : 0ull;
+                }
+                long long t_w0 = clock64();
+                cyc_pass += t_w0 - t_p0;
+                // write back the tile's sites (and periodic mirrors) and the owned cells
+                for (int q = tid; q < box; q += TB) {
+                    int r = q;
+                    int li[3];
+                    bool interior = true;
+                    for (int d = D - 1; d >= 0; --d) {
+                        li[d] = r % s_box_dims[d];
+                        r /= s_box_dims[d];
+                        if (li[d] == 0 || li[d] == s_box_dims[d] - 1) interior = false;
+                    }
+                    const uint32_t id = P.sig[q];
+                    if (interior) {
+                        int xg[3];
+                        P.gflat_of_box(q, xg);
+                        write_site<D, uint32_t>(g, g.sigma, xg, id);
+                    }
+                }
+                __syncthreads();
+                for (int q = tid; q < box; q += TB) {
+                    const uint32_t id = P.sig[q];
+                    if (id && P.own[id] && P.mod[id]) {
+                        __stcg(g.volume + id, P.vol[id]);
+                        __stcg(g.interface + id, P.itf[id]);
+                    }
+                }
+                __syncthreads();
+                cyc_stage += clock64() - t_w0;
+            }
+            __threadfence();
+            long long t_b0 = clock64();
+            if (!grid_sync(bar, nblk)) { alive = false; break; }
+            cyc_sync += clock64() - t_b0;
+        }
+    }
+    // statistics: every site was attempted once per completed MCS
+    atomicAdd(&sstat[1], ct.nonnull);
+    atomicAdd(&sstat[2], ct.topo);
+    atomicAdd(&sstat[3], ct.guard);
+    atomicAdd(&sstat[4], ct.evaluated);
+    atomicAdd(&sstat[5], ct.accepted);
+    atomicAdd(&sstat[6], ct.deferred);
+    atomicAdd(&sstat[0], attempts);
+    __syncthreads();
+    if (tid < 6) atomicAdd(&g.stats[tid], sstat[tid]);
+    if (tid == 0) {
+        atomicAdd(&g.stats[CPM_STAT_ROUNDS], ct.rounds);
+        atomicAdd(&g.stats[CPM_STAT_DEFERRED], sstat[6]);
+        atomicAdd(&g.stats[CPM_STAT_CYC_PASSES], cyc_pass);
+        atomicAdd(&g.stats[CPM_STAT_CYC_STAGE], cyc_stage);
+        atomicAdd(&g.stats[CPM_STAT_CYC_SYNC], cyc_sync);
+        atomicAdd(&g.stats[CPM_STAT_CYC_BUILD], ct.c_build);
+        atomicAdd(&g.stats[CPM_STAT_CYC_EVAL], ct.c_eval);
+        atomicAdd(&g.stats[CPM_STAT_CYC_FIX], ct.c_fix);
+        atomicAdd(&g.stats[CPM_STAT_CYC_APPLY], ct.c_apply);
+        atomicAdd(&g.stats[CPM_STAT_WIDE_PASSES], ct.wide);
+        if (blockIdx.x == 0) {
+            atomicAdd(&g.stats[CPM_STAT_PASSES], (unsigned long long)n_mcs * (D == 2 ? 16 : 64));
+            if (alive) simp->mcs = mcs0 + n_mcs;
+        }
+        if (!alive) {
+            atomicAdd(&g.stats[CPM_STAT_SPIN_TIMEOUTS], 1ull);
+            if (g.error) atomicExch(g.error, 5);
+        }
+    }
+}
+
+// ---- host side -------------------------------------------------------
+static int tiled_index(int D, int NE) {
+    if (D == 2 && NE == 4) return 0;
+    if (D == 2 && NE == 8) return 1;
+    if (D == 3 && NE == 6) return 2;
+    if (D == 3 && NE == 18) return 3;
+    if (D == 3 && NE == 26) return 4;
+    return -1;
+}
+
+bool tiled_plan(int D, const int* dims, int periodic, int* nt, int* max_box) {
+    int box = 1, klass = 1;
+    const int target = D == 2 ? 21 : 16;
+    for (int d = 0; d < D; ++d) {
+        const int L = dims[d];
+        if (periodic && (L & 1)) return false;  // odd periodic axes need a third site colour
+        int n = L / target;
+        if (n & 1) n -= 1;
+        if (n < 2) return false;
+        nt[d] = n;
+        const int tmax = (L + n - 1) / n;
+        box *= tmax + 2;
+        klass *= (tmax + 1) / 2;
+    }
+    *max_box = box;
+    return box <= TMAX_BOX && klass <= TCMAX;
+}
+
+size_t tiled_smem_bytes(int max_box, int n_cells) { return tile_shared(max_box, n_cells).total; }
+int tiled_block() { return TB; }
+
+cudaError_t tiled_occupancy(int D, int NE, size_t smem, int* per_sm) {
+    *per_sm = 0;
+#define TOCC(I, D_, NE_)                                                                                   \
+    case I: {                                                                                              \
+        auto k = tiled_kernel<D_, NE_>;                                                                     \
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);     \
+        if (e != cudaSuccess) return e;                                                                    \
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k, TB, smem);                         \
+    }
+    switch (tiled_index(D, NE)) {
+        TOCC(0, 2, 4)
+        TOCC(1, 2, 8)
+        TOCC(2, 3, 6)
+        TOCC(3, 3, 18)
+        TOCC(4, 3, 26)
+        default: return cudaErrorInvalidValue;
+    }
+#undef TOCC
+}
+
+cudaError_t launch_tiled(int D, int NE, SimDesc* d_sim, uint64_t n_mcs, const int* nt, void* d_barrier,
+                         unsigned long long* d_claims, const uint64_t* d_t3, int max_box, size_t smem, int grid,
+                         cudaStream_t st) {
+    TileGrid tg;
+    for (int d = 0; d < 3; ++d) { tg.nt[d] = d < D ? nt[d] : 1; tg.off[d] = 0; }
+    tg.colors = 1 << D;
+    BarrierState* bar = (BarrierState*)d_barrier;
+#define TLAUNCH(I, D_, NE_)                                                                                 \
+    case I: {                                                                                               \
+        auto k = tiled_kernel<D_, NE_>;                                                                      \
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);      \
+        if (e != cudaSuccess) return e;                                                                     \
+        void* args[] = {(void*)&d_sim, (void*)&n_mcs, (void*)&tg, (void*)&bar, (void*)&d_claims, (void*)&d_t3, \
+                        (void*)&max_box};                                                                   \
+        return cudaLaunchCooperativeKernel((const void*)k, dim3(grid), dim3(TB), args, smem, st);            \
+    }
+    switch (tiled_index(D, NE)) {
+        TLAUNCH(0, 2, 4)
+        TLAUNCH(1, 2, 8)
+        TLAUNCH(2, 3, 6)
+        TLAUNCH(3, 3, 18)
+        TLAUNCH(4, 3, 26)
+        default: return cudaErrorInvalidValue;
+    }
+#undef TLAUNCH
+}
+
+}  // namespace cpmgpu

@@ -49,6 +49,15 @@ STAT_NAMES = (
     "fixpoint_iterations",
     "h2d_bytes",
     "d2h_bytes",
+    "deferred",
+    "cycles_passes",
+    "cycles_stage",
+    "cycles_sync",
+    "cycles_build",
+    "cycles_eval",
+    "cycles_fixpoint",
+    "cycles_apply",
+    "wide_passes",
 )
 
 
@@ -330,7 +339,7 @@ def _result_from_handle(h) -> RunResult:
         for t in range(info.n_types):
             _check(_lib.cpm_result_cell_type_name(h, t, buf, 4096))
             names.append(buf.value.decode("utf-8"))
-        stats = np.zeros(16, dtype=np.uint64)
+        stats = np.zeros(32, dtype=np.uint64)
         _check(_lib.cpm_result_stats(h, _ptr(stats)))
         samples = []
         for s in range(int(info.n_samples)):
@@ -594,7 +603,7 @@ class Engine:
         return bool(okv.value), v, it
 
     def stats(self, i=0):
-        s = np.zeros(16, np.uint64)
+        s = np.zeros(32, np.uint64)
         _check(_lib.cpm_engine_stats(self._h, i, _ptr(s)))
         return {name: int(s[k]) for k, name in enumerate(STAT_NAMES)}
 

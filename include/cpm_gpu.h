@@ -153,10 +153,11 @@ int cpm_result_cell_type_index(const cpm_result* r, uint32_t* out /* n_cells */)
 int cpm_result_cell_type_name(const cpm_result* r, size_t type_index, char* buf, size_t capacity);
 int cpm_result_sample_sizes(const cpm_result* r, size_t sample, cpm_sample_sizes* out);
 int cpm_result_sample_read(const cpm_result* r, size_t sample, const cpm_sample_out* out);
-/* Device counters of the run (CPM_STAT_* order: attempts, non-null,
- * topology rejections, guard rejections, evaluated, accepted, conflict
- * rounds, colour passes, ...); out holds 16 values. */
-int cpm_result_stats(const cpm_result* r, uint64_t* out16);
+/* Device counters of the run (order: attempts, non-null, topology
+ * rejections, guard rejections, evaluated, accepted, conflict rounds, colour
+ * passes, timeouts, fixpoint iterations, h2d bytes, d2h bytes, deferred
+ * moves, then cycle counters of the tiled sweep); out holds 32 values. */
+int cpm_result_stats(const cpm_result* r, uint64_t* out32);
 void cpm_result_free(cpm_result* r);
 
 /* --------------------------------------------------- hot-path engine ---
@@ -211,7 +212,7 @@ int cpm_engine_energy(const cpm_engine* e, size_t sim, double* out);
 /* Full recount of volume and interface from the lattice on the device
  * (checker.rs:36-83); *ok = 1 iff it equals the incrementally kept state. */
 int cpm_engine_recount_check(const cpm_engine* e, size_t sim, int32_t* ok, uint32_t* volume, uint32_t* interface);
-int cpm_engine_stats(const cpm_engine* e, size_t sim, uint64_t* out16);
+int cpm_engine_stats(const cpm_engine* e, size_t sim, uint64_t* out32);
 /* Parity harness: overwrite the dynamic state, decide moves without
  * committing them, or apply moves in order with the sweep's commit. */
 int cpm_engine_write_state(cpm_engine* e, size_t sim, const uint32_t* padded, const uint32_t* volume,
