@@ -36,6 +36,7 @@ enum CpmStat {
     CPM_STAT_CYC_FIX = 18,       // tiled sweep: cycles in the fixpoint iterations
     CPM_STAT_CYC_APPLY = 19,     // tiled sweep: cycles applying and re-evaluating
     CPM_STAT_WIDE_PASSES = 20,   // tiled sweep: tile passes with more than 32 candidates (block-wide resolve)
+    CPM_STAT_CYC_LOWER = 21,     // tiled sweep: cycles finding the lower-priority sharers (warp resolve)
     CPM_STAT_COUNT = 32
 };
 
@@ -81,6 +82,12 @@ struct SimDesc {
     const double* vterm;
     const double* iterm;
     const double* dj;
+    // The same tables and J rounded to float (round to nearest), for the
+    // bounded FP32 pre-decision; null disables it.
+    const float* vterm32;
+    const float* iterm32;
+    const float* dj32;
+    const float* J32;
     int32_t tab_n;
     int32_t pad1;
     // ---- state ----
@@ -128,5 +135,5 @@ struct MoveOut {
     int32_t delta_i_losing, delta_i_gaining;
     double delta_h;
     int32_t accepted;
-    int32_t pad;
+    int32_t accepted_sweep;  // the sweeps' bounded decision (decide_move) on the same u
 };

@@ -87,10 +87,10 @@ struct DeltaOut {
 
 // lambda * (x - target)^2 for an integer-valued x: the exact host-built
 // table when x is in range (same IEEE operations), else computed here.
-__device__ __forceinline__ double term_of(const double* tab, int tab_n, int ty, double lambda, uint32_t target,
-                                          int64_t x) {
-    if (tab != nullptr && x >= 0 && x < tab_n) return __ldg(tab + (int64_t)ty * tab_n + x);
-    return quad_term(lambda, target, (double)x);
+__device__ __forceinline__ double term_of(const double* tab, int tab_n, int ty, const double* lambda,
+                                          const uint32_t* target, int64_t x) {
+    if (tab != nullptr && x >= 0 && x < tab_n) return tab[(int64_t)ty * tab_n + x];
+    return quad_term(lambda[ty], target[ty], (double)x);
 }
 
 // Terms::total_delta = volume + interface + adhesion, each accumulated in the
@@ -110,15 +110,15 @@ __device__ __forceinline__ DeltaOut delta_h(const SimDesc& s, const SigT* sig, c
     int cl = 0, cg = 0;
     if (s.dj != nullptr) {
         const double* D = s.dj + (int64_t)(li * nt1 + gi) * nt1;
-        const double jgl = __ldg(s.J + gi * nt1 + li);   // neighbour == losing: after - 0.0
-        const double jlg = -__ldg(s.J + li * nt1 + gi);  // neighbour == gaining: 0.0 - before
+        const double jgl = s.J[gi * nt1 + li];   // neighbour == losing: after - 0.0
+        const double jlg = -s.J[li * nt1 + gi];  // neighbour == gaining: 0.0 - before
 #pragma unroll
         for (int k = 0; k < NE; ++k) {
             const uint32_t nc = (uint32_t)sig[t + s.energy_off[k]];
             const bool isl = nc == L, isg = nc == G;
             cl += isl;
             cg += isg;
-            const double d = isl ? jgl : (isg ? jlg : __ldg(D + adh_of[nc]));
+            const double d = isl ? jgl : (isg ? jlg : D[adh_of[nc]]);
             adh = __dadd_rn(adh, d);
         }
     } else {
@@ -142,26 +142,26 @@ __device__ __forceinline__ DeltaOut delta_h(const SimDesc& s, const SigT* sig, c
     if (L) {
         const int ty = li - 1;
         const int64_t v = volume[L];
-        vol = __dadd_rn(vol, __dsub_rn(term_of(s.vterm, s.tab_n, ty, s.lambda_v[ty], s.target_v[ty], v - 1),
-                                       term_of(s.vterm, s.tab_n, ty, s.lambda_v[ty], s.target_v[ty], v)));
+        vol = __dadd_rn(vol, __dsub_rn(term_of(s.vterm, s.tab_n, ty, s.lambda_v, s.target_v, v - 1),
+                                       term_of(s.vterm, s.tab_n, ty, s.lambda_v, s.target_v, v)));
     }
     if (G) {
         const int ty = gi - 1;
         const int64_t v = volume[G];
-        vol = __dadd_rn(vol, __dsub_rn(term_of(s.vterm, s.tab_n, ty, s.lambda_v[ty], s.target_v[ty], v + 1),
-                                       term_of(s.vterm, s.tab_n, ty, s.lambda_v[ty], s.target_v[ty], v)));
+        vol = __dadd_rn(vol, __dsub_rn(term_of(s.vterm, s.tab_n, ty, s.lambda_v, s.target_v, v + 1),
+                                       term_of(s.vterm, s.tab_n, ty, s.lambda_v, s.target_v, v)));
     }
     if (L) {
         const int ty = li - 1;
         const int64_t i = interface[L];
-        itf = __dadd_rn(itf, __dsub_rn(term_of(s.iterm, s.tab_n, ty, s.lambda_i[ty], s.target_i[ty], i + o.dl),
-                                       term_of(s.iterm, s.tab_n, ty, s.lambda_i[ty], s.target_i[ty], i)));
+        itf = __dadd_rn(itf, __dsub_rn(term_of(s.iterm, s.tab_n, ty, s.lambda_i, s.target_i, i + o.dl),
+                                       term_of(s.iterm, s.tab_n, ty, s.lambda_i, s.target_i, i)));
     }
     if (G) {
         const int ty = gi - 1;
         const int64_t i = interface[G];
-        itf = __dadd_rn(itf, __dsub_rn(term_of(s.iterm, s.tab_n, ty, s.lambda_i[ty], s.target_i[ty], i + o.dg),
-                                       term_of(s.iterm, s.tab_n, ty, s.lambda_i[ty], s.target_i[ty], i)));
+        itf = __dadd_rn(itf, __dsub_rn(term_of(s.iterm, s.tab_n, ty, s.lambda_i, s.target_i, i + o.dg),
+                                       term_of(s.iterm, s.tab_n, ty, s.lambda_i, s.target_i, i)));
     }
     o.dh = __dadd_rn(__dadd_rn(vol, itf), adh);
     return o;
@@ -186,6 +186,130 @@ __device__ __forceinline__ bool metropolis(double dh, double u) {
     if (uf < ef * 0.99998f) return true;
     if (uf > ef * 1.00002f) return false;
     return u < exp(-dh);
+}
+
+// ------------------------------------------------- bounded decision ----
+// decide_move returns the reference's Metropolis decision for one attempt
+// (monte_carlo.rs:77-82, 158) without FP64 arithmetic in the common case.
+//
+// Delta-H is first summed in float from float copies y_i = fl32(x_i) of
+// the FP64 inputs x_i the reference adds (term-table entries, adhesion
+// differences, J). Both sums are trees of at most h <= 34 additions over the
+// same inputs, so (Higham, "Accuracy and Stability of Numerical
+// Algorithms", 2nd ed., sec. 4.2):
+//   |dh32 - dh64| <= (gamma32_h + u32 + gamma64_h) * sum|y_i| <= 2.2e-6 * sum|y_i|
+// with u32 = 2^-24 and gamma_h = h u / (1 - h u). The code uses
+// eps = 8e-6 * S32 (S32 the float sum of |y_i|), which also absorbs the
+// rounding of S32, of dh32 +- eps and of the float conversions. Then:
+//   dh32 + eps <= 0            -> dh64 <= 0: accept;
+//   dh32 - eps > 0             -> exp(-dh64) lies in [exp(-hi), exp(-lo)];
+//     with expf's 2-ulp error and a 3e-5 relative margin, and u bracketed
+//     by its top 32 bits z (u in [z 2^-32, (z+1) 2^-32)), a bracket wholly
+//     below / above decides accept / reject exactly;
+//   anything else (|dh32| <= eps, a bracket straddling the threshold, a
+//   term outside the tables, non-finite or huge values) recomputes Delta-H
+//   in FP64 in the reference's operation order and compares u < exp(-dh).
+// `draw` supplies the attempt's uniform u (u()) and its top 32 bits
+// z = floor(u 2^32) (z()), computed only when needed.
+struct PhiloxDraw {  // the sweeps: Philox keyed by (seed, mcs, site)
+    uint64_t seed, mcs;
+    uint32_t site;
+    __device__ double u() const { return u53(site_draw(seed, mcs, site)); }
+    __device__ uint32_t z() const { return site_draw(seed, mcs, site).z; }
+};
+struct GivenDraw {  // the parity harness: u given
+    double u_;
+    __device__ double u() const { return u_; }
+    __device__ uint32_t z() const { return (uint32_t)__dmul_rn(u_, 4294967296.0); }
+};
+
+template <int NE, class SigT, class Draw>
+__device__ __forceinline__ bool decide_move(const SimDesc& s, const SigT* sig, const uint16_t* adh_of,
+                                            const uint32_t* volume, const uint32_t* interface, int64_t t, uint32_t L,
+                                            uint32_t G, const Draw& draw, int& dl, int& dg) {
+    const int nt1 = s.n_types + 1;
+    const int li = adh_of[L], gi = adh_of[G];
+    const int tn = s.tab_n;
+    bool fast = s.dj32 != nullptr;
+    float adh = 0.f, sabs = 0.f;
+    int cl = 0, cg = 0;
+    if (fast) {
+        const float* Dt = s.dj32 + (li * nt1 + gi) * nt1;
+        const float jgl = s.J32[gi * nt1 + li];
+        const float jlg = -s.J32[li * nt1 + gi];
+#pragma unroll
+        for (int k = 0; k < NE; ++k) {
+            const uint32_t nc = (uint32_t)sig[t + s.energy_off[k]];
+            const bool isl = nc == L, isg = nc == G;
+            cl += isl;
+            cg += isg;
+            const float d = isl ? jgl : (isg ? jlg : Dt[adh_of[nc]]);
+            adh += d;
+            sabs += fabsf(d);
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < NE; ++k) {
+            const uint32_t nc = (uint32_t)sig[t + s.energy_off[k]];
+            cl += nc == L;
+            cg += nc == G;
+        }
+    }
+    dl = 2 * cl - NE;
+    dg = NE - 2 * cg;
+    if (fast) {
+        float vol = 0.f, itf = 0.f;
+        if (L) {
+            const int ty = li - 1;
+            const int64_t v = volume[L], i = interface[L];
+            if (v >= 1 && v < tn && i + dl >= 0 && i + dl < tn && i < tn) {
+                const float* V = s.vterm32 + ty * tn;
+                const float* I = s.iterm32 + ty * tn;
+                const float a = V[v - 1], b = V[v], c = I[i + dl], d = I[i];
+                vol += a - b;
+                itf += c - d;
+                sabs += (fabsf(a) + fabsf(b)) + (fabsf(c) + fabsf(d));
+            } else {
+                fast = false;
+            }
+        }
+        if (G) {
+            const int ty = gi - 1;
+            const int64_t v = volume[G], i = interface[G];
+            if (v + 1 < tn && i + dg >= 0 && i + dg < tn && i < tn) {
+                const float* V = s.vterm32 + ty * tn;
+                const float* I = s.iterm32 + ty * tn;
+                const float a = V[v + 1], b = V[v], c = I[i + dg], d = I[i];
+                vol += a - b;
+                itf += c - d;
+                sabs += (fabsf(a) + fabsf(b)) + (fabsf(c) + fabsf(d));
+            } else {
+                fast = false;
+            }
+        }
+        if (fast && sabs <= 1e30f) {
+            const float dh = (vol + itf) + adh;
+            const float eps = 8e-6f * sabs + 1e-30f;
+            const float hi = dh + eps, lo = dh - eps;
+            if (hi <= 0.f) return true;
+            if (lo > 0.f) {
+                const uint32_t z = draw.z();
+                if (lo > 64.f) {
+                    if (z != 0u) return false;  // u >= 2^-32 > exp(-64)
+                } else {
+                    const float ulo = __uint2float_rd(z) * 2.3283064365386963e-10f;
+                    const float uhi = __fadd_ru(__uint2float_ru(z), 1.0f) * 2.3283064365386963e-10f;
+                    const float elo = expf(-hi) * (1.0f - 3e-5f);
+                    const float ehi = expf(-lo) * (1.0f + 3e-5f);
+                    if (uhi < elo) return true;
+                    if (ulo > ehi) return false;
+                }
+            }
+        }
+    }
+    // exact: the reference's FP64 operation order
+    const DeltaOut o = delta_h<NE, SigT>(s, sig, adh_of, volume, interface, t, L, G);
+    return metropolis(o.dh, o.dh > 0.0 ? draw.u() : 0.0);
 }
 
 // ------------------------------------------------------------- commit ----

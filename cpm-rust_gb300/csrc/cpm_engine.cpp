@@ -109,7 +109,7 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
     table2d(t2);
     bool need_t3 = false;
     // ---- sizes
-    struct Offs { size_t sigma, adh, vol, itf, sp, so, slots, stats, J, lv, li, tv, ti, vt, it, dj, energy, svol, sitf, ssp, sso, slat, err; };
+    struct Offs { size_t sigma, adh, vol, itf, sp, so, slots, stats, J, lv, li, tv, ti, vt, it, dj, vt32, it32, dj32, J32, energy, svol, sitf, ssp, sso, slat, err; };
     std::vector<int> tab_n(N);
     std::vector<Offs> offs(N);
     Carve cv;
@@ -145,6 +145,10 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
         o.vt = cv.take(nt * (size_t)tab_n[i] * 8);
         o.it = cv.take(nt * (size_t)tab_n[i] * 8);
         o.dj = cv.take((nt + 1) * (nt + 1) * (nt + 1) * 8);
+        o.vt32 = cv.take(nt * (size_t)tab_n[i] * 4);
+        o.it32 = cv.take(nt * (size_t)tab_n[i] * 4);
+        o.dj32 = cv.take((nt + 1) * (nt + 1) * (nt + 1) * 4);
+        o.J32 = cv.take((nt + 1) * (nt + 1) * 4);
         o.energy = cv.take((size_t)std::max(1, L.n_energy) * 8);
         o.svol = cv.take((size_t)L.n_samples * n1 * 4);
         o.sitf = cv.take((size_t)L.n_samples * n1 * 4);
@@ -216,6 +220,16 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
                 for (size_t g = 0; g < n1t; ++g)
                     for (size_t k = 0; k < n1t; ++k) dj[(l * n1t + g) * n1t + k] = J[g * n1t + k] - J[l * n1t + k];
             std::memcpy(stage.data() + o.dj, dj.data(), dj.size() * 8);
+            // float copies (round to nearest) for the bounded pre-decision
+            auto put32 = [&](size_t off, const std::vector<double>& v) {
+                std::vector<float> f(v.size());
+                for (size_t q = 0; q < v.size(); ++q) f[q] = (float)v[q];
+                std::memcpy(stage.data() + off, f.data(), f.size() * 4);
+            };
+            put32(o.vt32, vt);
+            put32(o.it32, it);
+            put32(o.dj32, dj);
+            put32(o.J32, J);
         }
         // descriptor
         SimDesc& s = descs_[i];
@@ -284,6 +298,10 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
         s.vterm = (const double*)(base + o.vt);
         s.iterm = (const double*)(base + o.it);
         s.dj = (const double*)(base + o.dj);
+        s.vterm32 = (const float*)(base + o.vt32);
+        s.iterm32 = (const float*)(base + o.it32);
+        s.dj32 = (const float*)(base + o.dj32);
+        s.J32 = (const float*)(base + o.J32);
         s.tab_n = tab_n[i];
         s.mcs = 0;
         s.energy_out = (double*)(base + o.energy);
@@ -320,7 +338,11 @@ std::string DeviceSims::run_tiled(const RunPlan& p, const uint64_t* t3) {
     const SimLayout& L = layouts_[p.sim];
     int dims[3] = {(int)L.g.dims[0], (int)L.g.dims[1], (int)L.g.dims[2]}, nt[3], max_box = 0;
     cpmgpu::tiled_plan(L.g.D, dims, L.g.periodic, nt, &max_box);
-    const size_t smem = cpmgpu::tiled_smem_bytes(max_box, L.n_cells);
+    size_t smem = cpmgpu::tiled_smem_bytes(max_box, L.n_cells);
+    // the energy tables go to shared memory when they fit beside the tile state
+    const size_t tab = cpmgpu::tiled_table_bytes(descs_[p.sim].n_types, descs_[p.sim].tab_n);
+    const int tables_in_smem = smem + tab <= cpmgpu::resident_smem_limit();
+    if (tables_in_smem) smem += tab;
     int per_sm = 0, dev = 0, sms = 1;
     CUDA_TRY(cpmgpu::tiled_occupancy(L.g.D, L.NE, smem, &per_sm));
     CUDA_TRY(cudaGetDevice(&dev));
@@ -334,7 +356,7 @@ std::string DeviceSims::run_tiled(const RunPlan& p, const uint64_t* t3) {
     auto chunk = [&](uint64_t n) -> std::string {
         if (n == 0) return "";
         CUDA_TRY(cudaMemsetAsync(d_bar_, 0, 64, stream_));
-        CUDA_TRY(cpmgpu::launch_tiled(L.g.D, L.NE, d_sim, n, nt, d_bar_, claims, t3, max_box, smem, grid, stream_));
+        CUDA_TRY(cpmgpu::launch_tiled(L.g.D, L.NE, d_sim, n, nt, d_bar_, claims, t3, max_box, tables_in_smem, smem, grid, stream_));
         return "";
     };
     std::string e;

@@ -208,10 +208,10 @@ __device__ void color_pass(const SimDesc& s, const PassInfo& p, uint64_t mcs, ui
                 pend &= ~(1ull << i);
                 if (L != 0 && volume[L] <= s.min_cell_volume) { ct.guard_reject++; continue; }
                 ct.evaluated++;
-                const DeltaOut o = delta_h<NE, uint32_t>(s, sig, adh_of, volume, interface, t, L, G);
-                const bool acc = metropolis(o.dh, o.dh > 0.0 ? u53(site_draw(s.seed, mcs, (uint32_t)t)) : 0.0);
+                int dl = 0, dg = 0;
+                const bool acc = decide_move<NE, uint32_t>(s, sig, adh_of, volume, interface, t, L, G, PhiloxDraw{s.seed, mcs, (uint32_t)t}, dl, dg);
                 if (acc) {
-                    commit_move<D, uint32_t>(s, sig, volume, interface, s.sum_pos, s.sum_outer, x, L, G, o.dl, o.dg);
+                    commit_move<D, uint32_t>(s, sig, volume, interface, s.sum_pos, s.sum_outer, x, L, G, dl, dg);
                     ct.accepted++;
                 }
             }
@@ -358,7 +358,7 @@ __global__ void evaluate_moves_kernel(const SimDesc* simp, int64_t n, const int6
         o.gaining = s.sigma[o.source_flat];
         o.null_move = o.losing == o.gaining;
         o.topology_ok = 0; o.volume_guard_ok = 0; o.evaluated = 0;
-        o.delta_i_losing = 0; o.delta_i_gaining = 0; o.delta_h = 0.0; o.accepted = 0; o.pad = 0;
+        o.delta_i_losing = 0; o.delta_i_gaining = 0; o.delta_h = 0.0; o.accepted = 0; o.accepted_sweep = 0;
         if (!o.null_move) {
             o.topology_ok = preserves_topology<D, uint32_t>(s, s.sigma, t, o.losing, s.table2d, t3);
             if (o.topology_ok) {
@@ -370,6 +370,9 @@ __global__ void evaluate_moves_kernel(const SimDesc* simp, int64_t n, const int6
                     o.delta_i_gaining = d.dg;
                     o.delta_h = d.dh;
                     o.accepted = metropolis(d.dh, u[i]);
+                    int dl = 0, dg = 0;
+                    o.accepted_sweep = decide_move<NE, uint32_t>(s, s.sigma, s.adh_of, s.volume, s.interface, t, o.losing,
+                                                                 o.gaining, GivenDraw{u[i]}, dl, dg);
                 }
             }
         }

@@ -197,9 +197,9 @@ struct Resident {
         if (L != 0 && vol[L] <= s.min_cell_volume) {
             fl |= F_GUARD;
         } else {
-            const DeltaOut o = delta_h<NE, uint16_t>(s, sig, adh, vol, itf, t, L, G);
-            if (metropolis(o.dh, o.dh > 0.0 ? u53(site_draw(s.seed, mcs, (uint32_t)t)) : 0.0)) fl |= F_ACC;
-            c_dl[c] = (int16_t)((o.dl & 0xFF) | ((o.dg & 0xFF) << 8));
+            int dl = 0, dg = 0;
+            if (decide_move<NE, uint16_t>(s, sig, adh, vol, itf, t, L, G, PhiloxDraw{s.seed, mcs, (uint32_t)t}, dl, dg)) fl |= F_ACC;
+            c_dl[c] = (int16_t)((dl & 0xFF) | ((dg & 0xFF) << 8));
         }
         c_flags[c] = fl;
     }

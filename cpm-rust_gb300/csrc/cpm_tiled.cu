@@ -91,7 +91,7 @@ __device__ bool grid_sync(BarrierState* b, unsigned int n) {
 
 struct TileCounters {
     unsigned long long nonnull, topo, guard, evaluated, accepted, rounds, deferred, wide;
-    unsigned long long c_build, c_eval, c_fix, c_apply;
+    unsigned long long c_build, c_eval, c_fix, c_apply, c_lower;
 };
 
 template <int D, int NE>
@@ -134,10 +134,9 @@ struct TileProc {
         if (L != 0 && vol[L] <= l.min_cell_volume) {
             fl |= T_GUARD;
         } else {
-            const DeltaOut o = delta_h<NE, uint16_t>(l, sig, adh, vol, itf, t, L, G);
-            const double u = o.dh > 0.0 ? u53(site_draw(g.seed, mcs, c_gf[c])) : 0.0;
-            if (metropolis(o.dh, u)) fl |= T_ACC;
-            c_dl[c] = (int16_t)((o.dl & 0xFF) | ((o.dg & 0xFF) << 8));
+            int dl = 0, dg = 0;
+            if (decide_move<NE, uint16_t>(l, sig, adh, vol, itf, t, L, G, PhiloxDraw{g.seed, mcs, c_gf[c]}, dl, dg)) fl |= T_ACC;
+            c_dl[c] = (int16_t)((dl & 0xFF) | ((dg & 0xFF) << 8));
         }
         c_flags[c] = fl;
     }
@@ -206,22 +205,32 @@ struct TileProc {
         const bool have = lane < n;
         long long t0 = clock64();
         if (have) evaluate(lane, mcs);
+        __syncwarp();
+        long long tm = clock64();
+        ct.c_eval += tm - t0;
         const uint32_t cells = have ? c_cells[lane] : 0u;
         const uint32_t key = have ? c_key[lane] : 0xFFFFFFFFu;
         const uint32_t L = cells & 0xFFFFu, G = cells >> 16;
+        // lanes sharing a cell: per-cell lane masks (b0 is free while the
+        // warp resolves), then keep the sharers with a lower key
+        if (L) b0[L] = 0u;
+        if (G) b0[G] = 0u;
+        __syncwarp();
+        if (L) atomicOr(&b0[L], 1u << lane);
+        if (G) atomicOr(&b0[G], 1u << lane);
+        __syncwarp();
+        uint32_t share = ((L ? b0[L] : 0u) | (G ? b0[G] : 0u)) & ~(1u << lane);
         uint32_t lower = 0;
-        for (int j = 0; j < n; ++j) {
-            const uint32_t cj = __shfl_sync(FULL, cells, j);
-            const uint32_t kj = __shfl_sync(FULL, key, j);
-            const uint32_t Lj = cj & 0xFFFFu, Gj = cj >> 16;
-            const bool share = (L && (L == Lj || L == Gj)) || (G && (G == Lj || G == Gj));
-            if (share && kj < key) lower |= 1u << j;
+        while (share) {
+            const int j = __ffs(share) - 1;
+            share &= share - 1;
+            if (c_key[j] < key) lower |= 1u << j;
         }
         __syncwarp();
         uint32_t fl = have ? c_flags[lane] : 0u;
         uint32_t pending = __ballot_sync(FULL, have);
         long long t1 = clock64();
-        ct.c_eval += t1 - t0;
+        ct.c_lower += t1 - tm;
         while (pending) {
             t0 = clock64();
             const bool mine = (pending >> lane) & 1u;
@@ -387,9 +396,17 @@ __host__ __device__ inline TileShared tile_shared(int box_sites, int n_cells) {
     return s;
 }
 
+// Shared-memory copy of the float energy tables (J, adhesion differences,
+// term tables): (n+1)^2 + (n+1)^3 + 2 n tab_n floats.
+size_t tiled_table_bytes(int n_types, int tab_n) {
+    const size_t n1 = (size_t)n_types + 1;
+    return (n1 * n1 + n1 * n1 * n1 + 2 * (size_t)n_types * (size_t)tab_n) * 4;
+}
+
 template <int D, int NE>
 __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_mcs, TileGrid tg_in, BarrierState* bar,
-                                                   unsigned long long* claims, const uint64_t* t3, int max_box) {
+                                                   unsigned long long* claims, const uint64_t* t3, int max_box,
+                                                   int tables_in_smem) {
     extern __shared__ __align__(16) unsigned char sm[];
     __shared__ SimDesc gsd, lsd;
     __shared__ int s_n, s_tile, s_box_dims[3], s_gx0[3], s_tcnt[3];
@@ -399,6 +416,26 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
     if (tid == 0) gsd = *simp;
     if (tid < 8) sstat[tid] = 0;
     __syncthreads();
+    if (tables_in_smem && gsd.dj32 != nullptr) {
+        // the float energy tables move next to the tile state (no global
+        // loads in the common-case decision)
+        float* tb = (float*)(sm + tile_shared(max_box, gsd.n_cells).total);
+        const int n1 = gsd.n_types + 1, nj = n1 * n1, nd = n1 * n1 * n1, nv = gsd.n_types * gsd.tab_n;
+        for (int q = tid; q < nj; q += TB) tb[q] = gsd.J32[q];
+        for (int q = tid; q < nd; q += TB) tb[nj + q] = gsd.dj32[q];
+        for (int q = tid; q < nv; q += TB) {
+            tb[nj + nd + q] = gsd.vterm32[q];
+            tb[nj + nd + nv + q] = gsd.iterm32[q];
+        }
+        __syncthreads();
+        if (tid == 0) {
+            gsd.J32 = tb;
+            gsd.dj32 = tb + nj;
+            gsd.vterm32 = tb + nj + nd;
+            gsd.iterm32 = tb + nj + nd + nv;
+        }
+        __syncthreads();
+    }
     const SimDesc& g = gsd;
     const int nblk = gridDim.x;
     {
@@ -406,7 +443,7 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
         for (int id = tid; id <= g.n_cells; id += TB) seen0[id] = 0u;
         __syncthreads();
     }
-    TileCounters ct = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    TileCounters ct = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     unsigned long long attempts = 0;
     unsigned long long cyc_pass = 0, cyc_stage = 0, cyc_sync = 0;
     const uint64_t mcs0 = g.mcs;
@@ -683,6 +720,7 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
         atomicAdd(&g.stats[CPM_STAT_CYC_FIX], ct.c_fix);
         atomicAdd(&g.stats[CPM_STAT_CYC_APPLY], ct.c_apply);
         atomicAdd(&g.stats[CPM_STAT_WIDE_PASSES], ct.wide);
+        atomicAdd(&g.stats[CPM_STAT_CYC_LOWER], ct.c_lower);
         if (blockIdx.x == 0) {
             atomicAdd(&g.stats[CPM_STAT_PASSES], (unsigned long long)n_mcs * (D == 2 ? 16 : 64));
             if (alive) simp->mcs = mcs0 + n_mcs;
@@ -746,8 +784,8 @@ cudaError_t tiled_occupancy(int D, int NE, size_t smem, int* per_sm) {
 }
 
 cudaError_t launch_tiled(int D, int NE, SimDesc* d_sim, uint64_t n_mcs, const int* nt, void* d_barrier,
-                         unsigned long long* d_claims, const uint64_t* d_t3, int max_box, size_t smem, int grid,
-                         cudaStream_t st) {
+                         unsigned long long* d_claims, const uint64_t* d_t3, int max_box, int tables_in_smem,
+                         size_t smem, int grid, cudaStream_t st) {
     TileGrid tg;
     for (int d = 0; d < 3; ++d) { tg.nt[d] = d < D ? nt[d] : 1; tg.off[d] = 0; }
     tg.colors = 1 << D;
@@ -758,7 +796,7 @@ cudaError_t launch_tiled(int D, int NE, SimDesc* d_sim, uint64_t n_mcs, const in
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);      \
         if (e != cudaSuccess) return e;                                                                     \
         void* args[] = {(void*)&d_sim, (void*)&n_mcs, (void*)&tg, (void*)&bar, (void*)&d_claims, (void*)&d_t3, \
-                        (void*)&max_box};                                                                   \
+                        (void*)&max_box, (void*)&tables_in_smem};                                           \
         return cudaLaunchCooperativeKernel((const void*)k, dim3(grid), dim3(TB), args, smem, st);            \
     }
     switch (tiled_index(D, NE)) {

@@ -58,6 +58,7 @@ STAT_NAMES = (
     "cycles_fixpoint",
     "cycles_apply",
     "wide_passes",
+    "cycles_lower",
 )
 
 
@@ -139,7 +140,7 @@ MOVE_DTYPE = np.dtype([
     ("target_flat", np.int64), ("source_flat", np.int64), ("losing", np.uint32), ("gaining", np.uint32),
     ("null_move", np.int32), ("topology_ok", np.int32), ("volume_guard_ok", np.int32), ("evaluated", np.int32),
     ("delta_i_losing", np.int32), ("delta_i_gaining", np.int32), ("delta_h", np.float64), ("accepted", np.int32),
-    ("pad", np.int32),
+    ("accepted_sweep", np.int32),
 ])
 
 # Every symbol include/cpm_gpu.h declares (checked by the CPU test suite).

@@ -184,7 +184,9 @@ typedef struct {
 
 /* Per-move parity record (monte_carlo.rs:52-145 decided with explicit
  * draws): k indexes the von Neumann copy stencil, u is the uniform draw used
- * when delta_h > 0. */
+ * when delta_h > 0. `accepted` applies the reference's rule to the FP64
+ * delta_h; `accepted_sweep` is the decision the sweeps take for the same u
+ * (float pre-decision with an error bound, FP64 fallback) and must equal it. */
 typedef struct {
     int64_t target_flat, source_flat;
     uint32_t losing, gaining;
@@ -192,7 +194,7 @@ typedef struct {
     int32_t delta_i_losing, delta_i_gaining;
     double delta_h;
     int32_t accepted;
-    int32_t pad;
+    int32_t accepted_sweep;
 } cpm_move;
 
 /* stream: a cudaStream_t to launch on, or NULL for the default stream. */

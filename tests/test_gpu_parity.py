@@ -33,6 +33,9 @@ def _compare(got, want):
     wb = want["delta_h"].view(np.uint64)
     bad = np.flatnonzero(gb != wb)
     assert bad.size == 0, f"delta_h bits differ at {bad[:5]}: {got['delta_h'][bad[:5]]} vs {want['delta_h'][bad[:5]]}"
+    # the sweeps' float pre-decision (with its FP64 fallback) on the same u
+    bad = np.flatnonzero(got["accepted_sweep"] != got["accepted"])
+    assert bad.size == 0, f"sweep decision differs at {bad[:5]}: dh {got['delta_h'][bad[:5]]}"
 
 
 MODELS = {
@@ -68,6 +71,56 @@ def test_per_move_parity_along_oracle_trajectory(name, cuda_required):
         _compare(got, want)
         n_eval += int(want["evaluated"].sum())
     assert n_eval > 500, n_eval
+
+
+# relative offsets of u from exp(-dh): inside, at and beyond the float
+# pre-decision's uncertainty band (3e-5), down to 1e-12 (far above the 1-ulp
+# difference between two correctly implemented FP64 exponentials)
+NEAR = np.array([-1e-3, -1e-4, -3.5e-5, -3e-5, -2e-5, -1e-5, -1e-6, -1e-9, -1e-12,
+                 1e-12, 1e-9, 1e-6, 1e-5, 2e-5, 3e-5, 3.5e-5, 1e-4, 1e-3])
+
+
+# weak couplings, so that many uphill moves have dh of order 1
+SOFT = {
+    "soft_2d": lambda: Model((48, 48), "periodic", [("a", 40, 30, 0.02, 0.01), ("b", 40, 30, 0.03, 0.015)],
+                             [[0, 0.8, 0.7], [0.8, 0.3, 0.55], [0.7, 0.55, 0.35]], [10, 10], seed=8),
+    "soft_3d_26": lambda: Model((16, 16, 16), "periodic", [("a", 60, 90, 0.004, 0.0015)],
+                                [[0, 0.11], [0.11, 0.043]], [8], energy="twenty_six", seed=9),
+}
+
+
+@pytest.mark.parametrize("name", sorted(SOFT))
+def test_sweep_decision_at_the_metropolis_threshold(name, cuda_required):
+    """u placed just below / above exp(-dh): the bounded float decision and
+    its FP64 fallback give the reference's `u < exp(-dh)` every time."""
+    model = SOFT[name]()
+    sim = model.oracle()
+    eng = _engine(model)
+    rng = np.random.default_rng(7)
+    checked = 0
+    for _ in range(3):
+        sim.run_mcs(20 if model.D == 2 else 3)
+        v, i, sp, so = padded_cells(sim)
+        eng.write_state(sim.padded(), v, i, sp, so)
+        t = random_interior_targets(sim, 20000, rng)
+        k = rng.integers(0, 2 * model.D, t.size)
+        first = sim.evaluate_moves(t, k, np.full(t.size, 0.5))
+        # dh < 8 keeps exp(-dh) > 3.3e-4, where the 2^-53 grid of u is finer
+        # than the smallest offset
+        up = np.flatnonzero((first["evaluated"] == 1) & (first["delta_h"] > 0) & (first["delta_h"] < 8))
+        assert up.size > 20, up.size
+        up = up[:400]
+        tt = np.repeat(t[up], NEAR.size)
+        kk = np.repeat(k[up], NEAR.size)
+        e = np.exp(-np.repeat(first["delta_h"][up], NEAR.size))
+        u = e * (1.0 + np.tile(NEAR, up.size))
+        u = np.floor(np.minimum(u, 1 - 2.0**-53) * 2.0**53) * 2.0**-53  # on the 53-bit grid of gen::<f64>
+        got = eng.evaluate_moves(tt, kk, u)
+        want = sim.evaluate_moves(tt, kk, u)
+        _compare(got, want)
+        assert np.array_equal(got["accepted"], (u < e).astype(np.int32))
+        checked += tt.size
+    assert checked > 1000
 
 
 @pytest.mark.parametrize("D", [2, 3])
