@@ -35,8 +35,12 @@ enum CpmStat {
     CPM_STAT_CYC_EVAL = 17,      // tiled sweep: cycles in speculative evaluation
     CPM_STAT_CYC_FIX = 18,       // tiled sweep: cycles in the fixpoint iterations
     CPM_STAT_CYC_APPLY = 19,     // tiled sweep: cycles applying and re-evaluating
-    CPM_STAT_WIDE_PASSES = 20,   // tiled sweep: tile passes with more than 32 candidates (block-wide resolve)
+    CPM_STAT_WIDE_PASSES = 20,   // tiled sweep: tile passes with more than 64 candidates (block-wide resolve)
     CPM_STAT_CYC_LOWER = 21,     // tiled sweep: cycles finding the lower-priority sharers (warp resolve)
+    CPM_STAT_CYC_CLAIM = 22,     // tiled sweep: cycles registering cell claims
+    CPM_STAT_CYC_BAR_CLAIM = 23, // tiled sweep: cycles waiting in the grid barrier after the claims
+    CPM_STAT_CYC_BAR_WRITE = 24, // tiled sweep: cycles waiting in the grid barrier after the write-back
+    CPM_STAT_EXACT_DECISIONS = 25, // decisions the float bracket left to the FP64 computation
     CPM_STAT_COUNT = 32
 };
 
@@ -83,9 +87,13 @@ struct SimDesc {
     const double* iterm;
     const double* dj;
     // The same tables and J rounded to float (round to nearest), for the
-    // bounded FP32 pre-decision; null disables it.
+    // bounded FP32 pre-decision; null disables it. vterm32lo / iterm32lo
+    // hold the remainders fl32(x - fl32(x)), so that hi + lo carries x to
+    // about 2^-48 relative.
     const float* vterm32;
     const float* iterm32;
+    const float* vterm32lo;
+    const float* iterm32lo;
     const float* dj32;
     const float* J32;
     int32_t tab_n;

@@ -192,23 +192,20 @@ __device__ __forceinline__ bool metropolis(double dh, double u) {
 // decide_move returns the reference's Metropolis decision for one attempt
 // (monte_carlo.rs:77-82, 158) without FP64 arithmetic in the common case.
 //
-// Delta-H is first summed in float from float copies y_i = fl32(x_i) of
-// the FP64 inputs x_i the reference adds (term-table entries, adhesion
-// differences, J). Both sums are trees of at most h <= 34 additions over the
-// same inputs, so (Higham, "Accuracy and Stability of Numerical
-// Algorithms", 2nd ed., sec. 4.2):
-//   |dh32 - dh64| <= (gamma32_h + u32 + gamma64_h) * sum|y_i| <= 2.2e-6 * sum|y_i|
-// with u32 = 2^-24 and gamma_h = h u / (1 - h u). The code uses
-// eps = 8e-6 * S32 (S32 the float sum of |y_i|), which also absorbs the
-// rounding of S32, of dh32 +- eps and of the float conversions. Then:
-//   dh32 + eps <= 0            -> dh64 <= 0: accept;
-//   dh32 - eps > 0             -> exp(-dh64) lies in [exp(-hi), exp(-lo)];
-//     with expf's 2-ulp error and a 3e-5 relative margin, and u bracketed
-//     by its top 32 bits z (u in [z 2^-32, (z+1) 2^-32)), a bracket wholly
-//     below / above decides accept / reject exactly;
-//   anything else (|dh32| <= eps, a bracket straddling the threshold, a
-//   term outside the tables, non-finite or huge values) recomputes Delta-H
-//   in FP64 in the reference's operation order and compares u < exp(-dh).
+// Delta-H is first summed in float. Its leaves are the FP64 values the
+// reference adds: the adhesion differences and J entries (x = after -
+// before), converted y = fl32(x), and the four term differences
+// term(x') - term(x), each formed as (c_hi - d_hi) + (c_lo - d_lo) from the
+// float pairs of the two FP64 table entries, which is within
+// 2 u32 |leaf| + 2^-46 (|c| + |d|) of the FP64 difference. Both the float
+// and the reference's FP64 sums are trees of height h <= NE + 3 <= 29 over
+// these leaves, so (Higham, "Accuracy and Stability of Numerical
+// Algorithms", 2nd ed., sec. 4.2)
+//   |dh32 - dh64| <= (gamma32_h + 3 u32) sum|leaf| + 2^-45 sum(|c| + |d|)
+//                 <= 1.9e-6 sum|leaf| + 3e-14 sum(|c| + |d|),
+// u32 = 2^-24, gamma_h = h u / (1 - h u). The code uses
+// eps = 4e-6 sum|leaf| + 1e-12 sum(|c| + |d|), which also covers the float
+// rounding of the sums themselves and of dh32 +- eps. Then:
 // `draw` supplies the attempt's uniform u (u()) and its top 32 bits
 // z = floor(u 2^32) (z()), computed only when needed.
 struct PhiloxDraw {  // the sweeps: Philox keyed by (seed, mcs, site)
@@ -259,16 +256,21 @@ __device__ __forceinline__ bool decide_move(const SimDesc& s, const SigT* sig, c
     dg = NE - 2 * cg;
     if (fast) {
         float vol = 0.f, itf = 0.f;
+        float sterm = 0.f;
+        // one term difference table[x1] - table[x0] as a leaf
+        auto leaf = [&](const float* hi, const float* lo, int64_t x1, int64_t x0) -> float {
+            const float a = hi[x1], b = hi[x0];
+            const float r = (a - b) + (lo[x1] - lo[x0]);
+            sabs += fabsf(r);
+            sterm += fabsf(a) + fabsf(b);
+            return r;
+        };
         if (L) {
             const int ty = li - 1;
             const int64_t v = volume[L], i = interface[L];
             if (v >= 1 && v < tn && i + dl >= 0 && i + dl < tn && i < tn) {
-                const float* V = s.vterm32 + ty * tn;
-                const float* I = s.iterm32 + ty * tn;
-                const float a = V[v - 1], b = V[v], c = I[i + dl], d = I[i];
-                vol += a - b;
-                itf += c - d;
-                sabs += (fabsf(a) + fabsf(b)) + (fabsf(c) + fabsf(d));
+                vol += leaf(s.vterm32 + ty * tn, s.vterm32lo + ty * tn, v - 1, v);
+                itf += leaf(s.iterm32 + ty * tn, s.iterm32lo + ty * tn, i + dl, i);
             } else {
                 fast = false;
             }
@@ -277,43 +279,41 @@ __device__ __forceinline__ bool decide_move(const SimDesc& s, const SigT* sig, c
             const int ty = gi - 1;
             const int64_t v = volume[G], i = interface[G];
             if (v + 1 < tn && i + dg >= 0 && i + dg < tn && i < tn) {
-                const float* V = s.vterm32 + ty * tn;
-                const float* I = s.iterm32 + ty * tn;
-                const float a = V[v + 1], b = V[v], c = I[i + dg], d = I[i];
-                vol += a - b;
-                itf += c - d;
-                sabs += (fabsf(a) + fabsf(b)) + (fabsf(c) + fabsf(d));
+                vol += leaf(s.vterm32 + ty * tn, s.vterm32lo + ty * tn, v + 1, v);
+                itf += leaf(s.iterm32 + ty * tn, s.iterm32lo + ty * tn, i + dg, i);
             } else {
                 fast = false;
             }
         }
-        if (fast && sabs <= 1e30f) {
+        if (fast && sabs <= 1e30f && sterm <= 1e30f) {
             const float dh = (vol + itf) + adh;
-            const float eps = 8e-6f * sabs + 1e-30f;
+            const float eps = 4e-6f * sabs + 1e-12f * sterm + 1e-30f;
             const float hi = dh + eps, lo = dh - eps;
             if (hi <= 0.f) return true;
-            if (lo > 0.f) {
-                const uint32_t z = draw.z();
-                if (lo > 64.f) {
-                    if (z != 0u) return false;  // u >= 2^-32 > exp(-64)
-                } else {
-                    const float ulo = __uint2float_rd(z) * 2.3283064365386963e-10f;
-                    const float uhi = __fadd_ru(__uint2float_ru(z), 1.0f) * 2.3283064365386963e-10f;
-                    const float elo = expf(-hi) * (1.0f - 3e-5f);
+            const uint32_t z = draw.z();
+            if (lo > 64.f) {
+                if (z != 0u) return false;  // u >= 2^-32 > exp(-64)
+            } else if (hi <= 64.f) {
+                const float ulo = __uint2float_rd(z) * 2.3283064365386963e-10f;
+                const float uhi = __fadd_ru(__uint2float_ru(z), 1.0f) * 2.3283064365386963e-10f;
+                // u < exp(-hi) <= exp(-dh64) accepts whatever the sign of dh64
+                const float elo = expf(-hi) * (1.0f - 3e-5f);
+                if (uhi < elo) return true;
+                if (lo > 0.f) {
                     const float ehi = expf(-lo) * (1.0f + 3e-5f);
-                    if (uhi < elo) return true;
                     if (ulo > ehi) return false;
                 }
             }
         }
     }
     // exact: the reference's FP64 operation order
+    if (s.stats) atomicAdd(&s.stats[CPM_STAT_EXACT_DECISIONS], 1ull);
     const DeltaOut o = delta_h<NE, SigT>(s, sig, adh_of, volume, interface, t, L, G);
     return metropolis(o.dh, o.dh > 0.0 ? draw.u() : 0.0);
 }
 
 // ------------------------------------------------------------- commit ----
-// Nearest periodic image of `coord` to `centroid` (dynamics.rs:193-202).
+// Nearest periodic image of `coord` to `centroid` (dynamics.rs:187-202).
 __device__ __forceinline__ int64_t nearest_image(int64_t coord, double centroid, int64_t extent, bool periodic) {
     if (!periodic) return coord;
     int64_t best = coord;
@@ -322,6 +322,31 @@ __device__ __forceinline__ int64_t nearest_image(int64_t coord, double centroid,
     if (d1 < bd) { best = coord - extent; bd = d1; }
     const double d2 = fabs(__dsub_rn((double)(coord + extent), centroid));
     if (d2 < bd) { best = coord + extent; }
+    return best;
+}
+
+// The same choice for centroid = fl(sum / vb), decided in integers:
+// |p - r| < |q - r| for r = sum / vb  <=>  (p - q) (vb (p + q) - 2 sum) < 0.
+// Where the exact distances differ they differ by at least 1/vb (opposite
+// sides of r) or by L (same side), far above the FP64 rounding of the
+// division and subtractions for |sum| < 2^40 and vb < 2^20; where they tie,
+// r = (p + q) / 2 is a half-integer, so the FP64 centroid and distances are
+// exact and compare equal too. Outside those ranges the FP64 form runs.
+__device__ __forceinline__ int64_t nearest_image_exact(int64_t coord, int64_t sum, int64_t vb, int64_t extent,
+                                                       bool periodic) {
+    if (!periodic) return coord;
+    const int64_t lim = (int64_t)1 << 40;
+    if (sum >= lim || sum <= -lim || vb >= ((int64_t)1 << 20) || coord >= lim || coord <= -lim)
+        return nearest_image(coord, (double)sum / (double)vb, extent, true);
+    int64_t best = coord;
+    // p = coord - L against q = coord: (p - q) = -L < 0
+    if (vb * (2 * coord - extent) - 2 * sum > 0) best = coord - extent;
+    // p = coord + L against the current best
+    if (best == coord) {
+        if (vb * (2 * coord + extent) - 2 * sum < 0) best = coord + extent;  // p - q = L > 0
+    } else {
+        if (vb * coord - sum < 0) best = coord + extent;                      // p - q = 2L > 0
+    }
     return best;
 }
 
@@ -379,10 +404,7 @@ __device__ __forceinline__ void commit_move(const SimDesc& s, SigT* sig, uint32_
         int64_t* so = sum_outer + (int64_t)G * D * D;
         int64_t img[3];
 #pragma unroll
-        for (int d = 0; d < D; ++d) {
-            const double cen = (double)sp[d] / (double)vb;
-            img[d] = nearest_image(x[d], cen, s.dims[d], s.periodic != 0);
-        }
+        for (int d = 0; d < D; ++d) img[d] = nearest_image_exact(x[d], sp[d], vb, s.dims[d], s.periodic != 0);
 #pragma unroll
         for (int d = 0; d < D; ++d) sp[d] += img[d];
 #pragma unroll

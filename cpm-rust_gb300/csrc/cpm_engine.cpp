@@ -109,7 +109,7 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
     table2d(t2);
     bool need_t3 = false;
     // ---- sizes
-    struct Offs { size_t sigma, adh, vol, itf, sp, so, slots, stats, J, lv, li, tv, ti, vt, it, dj, vt32, it32, dj32, J32, energy, svol, sitf, ssp, sso, slat, err; };
+    struct Offs { size_t sigma, adh, vol, itf, sp, so, slots, stats, J, lv, li, tv, ti, vt, it, dj, vt32, it32, vt32lo, it32lo, dj32, J32, energy, svol, sitf, ssp, sso, slat, err; };
     std::vector<int> tab_n(N);
     std::vector<Offs> offs(N);
     Carve cv;
@@ -147,6 +147,8 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
         o.dj = cv.take((nt + 1) * (nt + 1) * (nt + 1) * 8);
         o.vt32 = cv.take(nt * (size_t)tab_n[i] * 4);
         o.it32 = cv.take(nt * (size_t)tab_n[i] * 4);
+        o.vt32lo = cv.take(nt * (size_t)tab_n[i] * 4);
+        o.it32lo = cv.take(nt * (size_t)tab_n[i] * 4);
         o.dj32 = cv.take((nt + 1) * (nt + 1) * (nt + 1) * 4);
         o.J32 = cv.take((nt + 1) * (nt + 1) * 4);
         o.energy = cv.take((size_t)std::max(1, L.n_energy) * 8);
@@ -228,6 +230,13 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
             };
             put32(o.vt32, vt);
             put32(o.it32, it);
+            auto put32lo = [&](size_t off, const std::vector<double>& v) {
+                std::vector<float> f(v.size());
+                for (size_t q = 0; q < v.size(); ++q) f[q] = (float)(v[q] - (double)(float)v[q]);
+                std::memcpy(stage.data() + off, f.data(), f.size() * 4);
+            };
+            put32lo(o.vt32lo, vt);
+            put32lo(o.it32lo, it);
             put32(o.dj32, dj);
             put32(o.J32, J);
         }
@@ -300,6 +309,8 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
         s.dj = (const double*)(base + o.dj);
         s.vterm32 = (const float*)(base + o.vt32);
         s.iterm32 = (const float*)(base + o.it32);
+        s.vterm32lo = (const float*)(base + o.vt32lo);
+        s.iterm32lo = (const float*)(base + o.it32lo);
         s.dj32 = (const float*)(base + o.dj32);
         s.J32 = (const float*)(base + o.J32);
         s.tab_n = tab_n[i];
@@ -349,14 +360,24 @@ std::string DeviceSims::run_tiled(const RunPlan& p, const uint64_t* t3) {
     CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     int tiles = 1;
     for (int d = 0; d < L.g.D; ++d) tiles *= nt[d];
-    const int grid = std::max(1, std::min(tiles >> L.g.D, std::max(1, per_sm) * sms));
+    int grid = std::max(1, std::min(tiles >> L.g.D, std::max(1, per_sm) * sms));
+    // CPM_GPU_TILED_GRID caps the grid (several tiles per CTA); the tiling,
+    // and so the trajectory, does not depend on it
+    if (const char* cap = std::getenv("CPM_GPU_TILED_GRID")) grid = std::max(1, std::min(grid, std::atoi(cap)));
+    if ((tiles >> L.g.D) > 511 * grid) return "tiled sweep: too many tiles per CTA for this lattice";
     if (!d_bar_) CUDA_TRY(cudaMalloc(&d_bar_, 64));
     SimDesc* d_sim = d_descs_ + p.sim;
     unsigned long long* claims = descs_[p.sim].slots;
     auto chunk = [&](uint64_t n) -> std::string {
-        if (n == 0) return "";
-        CUDA_TRY(cudaMemsetAsync(d_bar_, 0, 64, stream_));
-        CUDA_TRY(cpmgpu::launch_tiled(L.g.D, L.NE, d_sim, n, nt, d_bar_, claims, t3, max_box, tables_in_smem, smem, grid, stream_));
+        // at most 2^18 MCS per launch: the barrier counter (32 bits) grows by
+        // grid x 2 x colours per MCS within a launch
+        while (n > 0) {
+            const uint64_t m = std::min<uint64_t>(n, 1ull << 18);
+            CUDA_TRY(cudaMemsetAsync(d_bar_, 0, 64, stream_));
+            CUDA_TRY(cpmgpu::launch_tiled(L.g.D, L.NE, d_sim, m, nt, d_bar_, claims, t3, max_box, tables_in_smem, smem,
+                                          grid, stream_));
+            n -= m;
+        }
         return "";
     };
     std::string e;

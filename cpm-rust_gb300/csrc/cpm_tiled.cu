@@ -29,6 +29,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "cpm_common.h"
 #include "cpm_device.cuh"
 #include "cpm_kernels.h"
@@ -60,28 +62,44 @@ struct BarrierState {
     int pad;
 };
 
-// Grid barrier with a bounded spin (~2 s): returns false after a timeout.
-__device__ bool grid_sync(BarrierState* b, unsigned int n) {
+__device__ __forceinline__ void red_release_add(unsigned int* p, unsigned int v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned int ld_acquire(const unsigned int* p) {
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Grid barrier: one release-add per CTA on a counter that only grows
+// within a launch (the host zeroes it), and acquire loads until it reaches
+// `epoch` * n. The wait gives up after 2 s of wall time, records the
+// timeout and returns false instead of hanging.
+__device__ bool grid_sync(BarrierState* b, unsigned int n, unsigned int& epoch) {
     __shared__ int s_ok;
+    ++epoch;
     __syncthreads();
     if (threadIdx.x == 0) {
-        volatile unsigned int* vgen = &b->gen;
-        const unsigned int g = *vgen;
-        __threadfence();
-        const unsigned int arrived = atomicAdd(&b->count, 1u);
+        const unsigned int target = epoch * n;
+        red_release_add(&b->count, 1u);
         int ok = 1;
-        if (arrived == n - 1) {
-            b->count = 0;
-            __threadfence();
-            atomicAdd(&b->gen, 1u);
-        } else {
-            long long spins = 0;
-            while (*vgen == g) {
-                __nanosleep(64);
-                if (++spins > 20000000LL || *((volatile int*)&b->error)) { ok = 0; break; }
+        if (ld_acquire(&b->count) < target) {
+            const unsigned long long t0 = global_ns();
+            unsigned int spins = 0;
+            while (ld_acquire(&b->count) < target) {
+                __nanosleep(20);
+                if ((++spins & 255u) == 0u &&
+                    (global_ns() - t0 > 2000000000ull || *((volatile int*)&b->error))) {
+                    ok = 0;
+                    break;
+                }
             }
         }
-        __threadfence();
         if (!ok) atomicExch(&b->error, 1);
         s_ok = ok && !*((volatile int*)&b->error);
     }
@@ -176,10 +194,7 @@ struct TileProc {
             long long* so = (long long*)g.sum_outer + (long long)G * D * D;
             long long img[3];
 #pragma unroll
-            for (int d = 0; d < D; ++d) {
-                const double cen = (double)__ldcg(sp + d) / (double)vb;
-                img[d] = nearest_image(xg[d], cen, g.dims[d], g.periodic != 0);
-            }
+            for (int d = 0; d < D; ++d) img[d] = nearest_image_exact(xg[d], __ldcg(sp + d), vb, g.dims[d], g.periodic != 0);
 #pragma unroll
             for (int d = 0; d < D; ++d) __stcg(sp + d, __ldcg(sp + d) + img[d]);
 #pragma unroll
@@ -199,68 +214,124 @@ struct TileProc {
     // pending candidate with a committed lower neighbour re-evaluates (a
     // committed candidate sharing a cell with a pending one always has the
     // lower key, or the pending one would have been a final reject).
+    template <int K>
+    using Mask = typename std::conditional<K == 1, uint32_t, uint64_t>::type;
+    template <int K>
+    __device__ __forceinline__ Mask<K> ballot_k(const bool (&p)[K]) const {
+        Mask<K> m = __ballot_sync(0xffffffffu, p[0]);
+        if (K > 1) m |= (Mask<K>)__ballot_sync(0xffffffffu, p[K > 1 ? 1 : 0]) << (K > 1 ? 32 : 0);
+        return m;
+    }
+    template <int K>
+    __device__ __forceinline__ static Mask<K> bit_k(int c) { return (Mask<K>)1 << c; }
+
+    // K = 1 handles n <= 32 candidates, K = 2 n <= 64 (candidate c = lane +
+    // 32 q, bit c of the 64-bit masks).
+    template <int K>
     __device__ void resolve_warp(int n, uint64_t mcs, TileCounters& ct) {
-        const unsigned FULL = 0xffffffffu;
         const int lane = threadIdx.x & 31;
-        const bool have = lane < n;
         long long t0 = clock64();
-        if (have) evaluate(lane, mcs);
+#pragma unroll
+        for (int q = 0; q < K; ++q)
+            if (lane + 32 * q < n) evaluate(lane + 32 * q, mcs);
         __syncwarp();
         long long tm = clock64();
         ct.c_eval += tm - t0;
-        const uint32_t cells = have ? c_cells[lane] : 0u;
-        const uint32_t key = have ? c_key[lane] : 0xFFFFFFFFu;
-        const uint32_t L = cells & 0xFFFFu, G = cells >> 16;
-        // lanes sharing a cell: per-cell lane masks (b0 is free while the
-        // warp resolves), then keep the sharers with a lower key
-        if (L) b0[L] = 0u;
-        if (G) b0[G] = 0u;
-        __syncwarp();
-        if (L) atomicOr(&b0[L], 1u << lane);
-        if (G) atomicOr(&b0[G], 1u << lane);
-        __syncwarp();
-        uint32_t share = ((L ? b0[L] : 0u) | (G ? b0[G] : 0u)) & ~(1u << lane);
-        uint32_t lower = 0;
-        while (share) {
-            const int j = __ffs(share) - 1;
-            share &= share - 1;
-            if (c_key[j] < key) lower |= 1u << j;
+        uint32_t Lc[K], Gc[K], key[K], fl[K];
+        Mask<K> lower[K];
+        bool have[K];
+#pragma unroll
+        for (int q = 0; q < K; ++q) {
+            const int c = lane + 32 * q;
+            have[q] = c < n;
+            const uint32_t cells = have[q] ? c_cells[c] : 0u;
+            key[q] = have[q] ? c_key[c] : 0xFFFFFFFFu;
+            Lc[q] = cells & 0xFFFFu;
+            Gc[q] = cells >> 16;
+        }
+        // candidates sharing a cell: per-cell masks (b0: candidates 0..31,
+        // b1: 32..63; both are free while the warp resolves), then keep the
+        // sharers with a lower key
+#pragma unroll
+        for (int q = 0; q < K; ++q) {
+            if (Lc[q]) { b0[Lc[q]] = 0u; if (K > 1) b1[Lc[q]] = 0u; }
+            if (Gc[q]) { b0[Gc[q]] = 0u; if (K > 1) b1[Gc[q]] = 0u; }
         }
         __syncwarp();
-        uint32_t fl = have ? c_flags[lane] : 0u;
-        uint32_t pending = __ballot_sync(FULL, have);
+#pragma unroll
+        for (int q = 0; q < K; ++q) {
+            uint32_t* bm = q == 0 ? b0 : b1;
+            if (Lc[q]) atomicOr(&bm[Lc[q]], 1u << lane);
+            if (Gc[q]) atomicOr(&bm[Gc[q]], 1u << lane);
+        }
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < K; ++q) {
+            Mask<K> sh = 0;
+            if (Lc[q]) sh |= (Mask<K>)b0[Lc[q]] | (K > 1 ? (Mask<K>)b1[Lc[q]] << (K > 1 ? 32 : 0) : (Mask<K>)0);
+            if (Gc[q]) sh |= (Mask<K>)b0[Gc[q]] | (K > 1 ? (Mask<K>)b1[Gc[q]] << (K > 1 ? 32 : 0) : (Mask<K>)0);
+            sh &= ~bit_k<K>(lane + 32 * q);
+            Mask<K> lw = 0;
+            while (sh) {
+                const int j = K == 1 ? __ffs((uint32_t)sh) - 1 : __ffsll((long long)sh) - 1;
+                sh &= sh - 1;
+                if (c_key[j] < key[q]) lw |= bit_k<K>(j);
+            }
+            lower[q] = lw;
+        }
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < K; ++q) fl[q] = have[q] ? c_flags[lane + 32 * q] : 0u;
+        Mask<K> pending = ballot_k<K>(have);
         long long t1 = clock64();
         ct.c_lower += t1 - tm;
         while (pending) {
             t0 = clock64();
-            const bool mine = (pending >> lane) & 1u;
-            const bool rej = (fl & T_GUARD) || !(fl & T_ACC);
-            uint32_t fin = 0;
+            bool mine[K], rej[K];
+#pragma unroll
+            for (int q = 0; q < K; ++q) {
+                mine[q] = (pending >> (lane + 32 * q)) & 1u;
+                rej[q] = (fl[q] & T_GUARD) || !(fl[q] & T_ACC);
+            }
+            Mask<K> fin = 0;
             for (;;) {
-                const uint32_t frej = __ballot_sync(FULL, ((fin >> lane) & 1u) && rej);
-                const uint32_t nf = __ballot_sync(FULL, mine && (lower & pending & ~frej) == 0);
-                if (nf == fin) break;
-                fin = nf;
+                bool fr[K], nf[K];
+#pragma unroll
+                for (int q = 0; q < K; ++q) fr[q] = ((fin >> (lane + 32 * q)) & 1u) && rej[q];
+                const Mask<K> frej = ballot_k<K>(fr);
+#pragma unroll
+                for (int q = 0; q < K; ++q) nf[q] = mine[q] && (lower[q] & pending & ~frej) == 0;
+                const Mask<K> f2 = ballot_k<K>(nf);
+                if (f2 == fin) break;
+                fin = f2;
             }
             t1 = clock64();
             ct.c_fix += t1 - t0;
-            const bool is_fin = (fin >> lane) & 1u;
-            const bool commit_me = is_fin && !rej;
-            if (is_fin) {
-                if (fl & T_GUARD) ct.guard++;
-                else ct.evaluated++;
+            bool cm[K];
+#pragma unroll
+            for (int q = 0; q < K; ++q) {
+                const bool is_fin = (fin >> (lane + 32 * q)) & 1u;
+                cm[q] = is_fin && !rej[q];
+                if (is_fin) {
+                    if (fl[q] & T_GUARD) ct.guard++;
+                    else ct.evaluated++;
+                }
+                if (cm[q]) {
+                    commit(lane + 32 * q, false);
+                    ct.accepted++;
+                }
             }
-            if (commit_me) {
-                commit(lane, false);
-                ct.accepted++;
-            }
-            const uint32_t committed = __ballot_sync(FULL, commit_me);
+            const Mask<K> committed = ballot_k<K>(cm);
             pending &= ~fin;
             ct.rounds++;
             __syncwarp();
-            if (((pending >> lane) & 1u) && (lower & committed)) {
-                evaluate(lane, mcs);
-                fl = c_flags[lane];
+#pragma unroll
+            for (int q = 0; q < K; ++q) {
+                const int c = lane + 32 * q;
+                if (((pending >> c) & 1u) && (lower[q] & committed)) {
+                    evaluate(c, mcs);
+                    fl[q] = c_flags[c];
+                }
             }
             __syncwarp();
             ct.c_apply += clock64() - t1;
@@ -364,7 +435,7 @@ struct TileProc {
 };
 
 struct TileShared {
-    uint32_t sig, vol, itf, b0, b1, adh, dirty, own, mod, seen, c_site, c_key, c_cells, c_flags, c_gf, c_dl, total;
+    uint32_t sig, vol, itf, b0, b1, adh, dirty, own, mod, seen, clist, c_site, c_key, c_cells, c_flags, c_gf, c_dl, total;
 };
 
 __host__ __device__ inline uint32_t tl_take(uint32_t& off, uint64_t b) {
@@ -386,6 +457,7 @@ __host__ __device__ inline TileShared tile_shared(int box_sites, int n_cells) {
     s.own = tl_take(off, n1);
     s.mod = tl_take(off, n1);
     s.seen = tl_take(off, n1 * 4);
+    s.clist = tl_take(off, (uint64_t)(box_sites < n_cells ? box_sites : n_cells) * 4);
     s.c_site = tl_take(off, TCMAX * 4);
     s.c_key = tl_take(off, TCMAX * 4);
     s.c_cells = tl_take(off, TCMAX * 4);
@@ -397,10 +469,10 @@ __host__ __device__ inline TileShared tile_shared(int box_sites, int n_cells) {
 }
 
 // Shared-memory copy of the float energy tables (J, adhesion differences,
-// term tables): (n+1)^2 + (n+1)^3 + 2 n tab_n floats.
+// term tables and their remainders): (n+1)^2 + (n+1)^3 + 4 n tab_n floats.
 size_t tiled_table_bytes(int n_types, int tab_n) {
     const size_t n1 = (size_t)n_types + 1;
-    return (n1 * n1 + n1 * n1 * n1 + 2 * (size_t)n_types * (size_t)tab_n) * 4;
+    return (n1 * n1 + n1 * n1 * n1 + 4 * (size_t)n_types * (size_t)tab_n) * 4;
 }
 
 template <int D, int NE>
@@ -409,7 +481,7 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                                                    int tables_in_smem) {
     extern __shared__ __align__(16) unsigned char sm[];
     __shared__ SimDesc gsd, lsd;
-    __shared__ int s_n, s_tile, s_box_dims[3], s_gx0[3], s_tcnt[3];
+    __shared__ int s_n, s_tile, s_ncell, s_box_dims[3], s_gx0[3], s_tcnt[3];
     __shared__ int perm[8], sperm[27];
     __shared__ unsigned long long sstat[8];
     const int tid = threadIdx.x;
@@ -426,6 +498,8 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
         for (int q = tid; q < nv; q += TB) {
             tb[nj + nd + q] = gsd.vterm32[q];
             tb[nj + nd + nv + q] = gsd.iterm32[q];
+            tb[nj + nd + 2 * nv + q] = gsd.vterm32lo[q];
+            tb[nj + nd + 3 * nv + q] = gsd.iterm32lo[q];
         }
         __syncthreads();
         if (tid == 0) {
@@ -433,6 +507,8 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
             gsd.dj32 = tb + nj;
             gsd.vterm32 = tb + nj + nd;
             gsd.iterm32 = tb + nj + nd + nv;
+            gsd.vterm32lo = tb + nj + nd + 2 * nv;
+            gsd.iterm32lo = tb + nj + nd + 3 * nv;
         }
         __syncthreads();
     }
@@ -445,9 +521,10 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
     }
     TileCounters ct = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     unsigned long long attempts = 0;
-    unsigned long long cyc_pass = 0, cyc_stage = 0, cyc_sync = 0;
+    unsigned long long cyc_pass = 0, cyc_stage = 0, cyc_sync = 0, cyc_claim = 0, cyc_bar1 = 0, cyc_bar2 = 0;
     const uint64_t mcs0 = g.mcs;
     bool alive = true;
+    unsigned int bar_epoch = 0;
     for (uint64_t m = 0; m < n_mcs && alive; ++m) {
         const uint64_t mcs = mcs0 + m;
         // ---- tiling of this MCS: random offset (periodic), random tile-colour order
@@ -483,42 +560,16 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                     tc[d] = 2 * q + ((color >> d) & 1);
                 }
             };
-            // ---- claim the cells of every box this CTA will process
-            long long t_c0 = clock64();
-            for (int k = blockIdx.x; k < per_color; k += nblk) {
-                int tc[3];
-                tile_coords(k, tc);
-                int bdim[3], x0[3];
-                int box = 1;
-                for (int d = 0; d < D; ++d) {
-                    const int L = g.dims[d];
-                    const int b0 = tile_begin(tc[d], L, tg.nt[d]), b1 = tile_begin(tc[d] + 1, L, tg.nt[d]);
-                    x0[d] = b0 + tg.off[d];
-                    bdim[d] = b1 - b0 + 2;
-                    box *= bdim[d];
-                }
-                const int tile_id = k;
-                const unsigned long long key = base_key | (unsigned long long)tile_id;
-                uint32_t* seen = (uint32_t*)(sm + tile_shared(max_box, g.n_cells).seen);
-                const uint32_t stamp = (uint32_t)(epoch * 1024u + (uint32_t)(k / nblk)) + 1u;
-                for (int q = tid; q < box; q += TB) {
-                    int r = q, gf = 0;
-                    for (int d = D - 1; d >= 0; --d) {
-                        const int i = r % bdim[d];
-                        r /= bdim[d];
-                        int x = x0[d] + i - 1;
-                        if (g.periodic) { x %= g.dims[d]; if (x < 0) x += g.dims[d]; gf += (x + 1) * (int)g.strides[d]; }
-                        else gf += (x + 1) * (int)g.strides[d];
-                    }
-                    const uint32_t id = __ldcg(g.sigma + gf);
-                    if (id && atomicExch(&seen[id], stamp) != stamp) atomicMin(claims + id, key);
-                }
-                __syncthreads();
-            }
-            if (!grid_sync(bar, nblk)) { alive = false; break; }
-            cyc_sync += clock64() - t_c0;
-            // ---- process the tiles
-            for (int k = blockIdx.x; k < per_color; k += nblk) {
+            const TileShared ts = tile_shared(max_box, g.n_cells);
+            uint32_t* seen = (uint32_t*)(sm + ts.seen);
+            // seen[] stamps, unique within a launch (at most 2^18 MCS x 8
+            // sub-phases x 1024 slots; seen[] starts zeroed)
+            auto stamp_of = [&](int k) -> uint32_t {
+                return (uint32_t)((m * 8 + (uint64_t)ci) * 1024u + (uint32_t)(k / nblk)) + 1u;
+            };
+            uint32_t* clist = (uint32_t*)(sm + ts.clist);
+            // box geometry of tile k: global origin, extents, local strides and offsets
+            auto setup_tile = [&](int k) {
                 int tc[3];
                 tile_coords(k, tc);
                 if (tid == 0) {
@@ -536,6 +587,7 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                     for (int d = D - 1; d >= 0; --d) { lsd.strides[d] = st; st *= lsd.pdims[d]; }
                     lsd.n_padded = st;
                     s_tile = k;
+                    s_ncell = 0;
                 }
                 __syncthreads();
                 // local stencil offsets from the integer offset vectors (one thread each)
@@ -552,32 +604,113 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                     if (kk < g.n_copy) lsd.copy_off[kk] = c;
                 }
                 __syncthreads();
-                long long t_s0 = clock64();
-                const TileShared ts = tile_shared(max_box, g.n_cells);
-                TileProc<D, NE> P{g, lsd, (uint16_t*)(sm + ts.sig), s_gx0, (uint32_t*)(sm + ts.vol),
-                                  (uint32_t*)(sm + ts.itf), (uint32_t*)(sm + ts.b0), (uint32_t*)(sm + ts.b1),
-                                  (uint16_t*)(sm + ts.adh), (uint8_t*)(sm + ts.dirty), (uint8_t*)(sm + ts.own),
-                                  (uint8_t*)(sm + ts.mod), (uint32_t*)(sm + ts.c_site), (uint32_t*)(sm + ts.c_key),
-                                  (uint32_t*)(sm + ts.c_cells), (uint32_t*)(sm + ts.c_flags), (uint32_t*)(sm + ts.c_gf),
-                                  (int16_t*)(sm + ts.c_dl), t3, &s_n};
+            };
+            TileProc<D, NE> P{g, lsd, (uint16_t*)(sm + ts.sig), s_gx0, (uint32_t*)(sm + ts.vol),
+                              (uint32_t*)(sm + ts.itf), (uint32_t*)(sm + ts.b0), (uint32_t*)(sm + ts.b1),
+                              (uint16_t*)(sm + ts.adh), (uint8_t*)(sm + ts.dirty), (uint8_t*)(sm + ts.own),
+                              (uint8_t*)(sm + ts.mod), (uint32_t*)(sm + ts.c_site), (uint32_t*)(sm + ts.c_key),
+                              (uint32_t*)(sm + ts.c_cells), (uint32_t*)(sm + ts.c_flags), (uint32_t*)(sm + ts.c_gf),
+                              (int16_t*)(sm + ts.c_dl), t3, &s_n};
+            // Stage the box of the current tile: sigma into shared memory,
+            // each distinct cell listed once (and claimed when `claim`),
+            // then the listed cells' V, I and type. Nothing writes sigma, V
+            // or I between the two grid barriers of a sub-phase, so staging
+            // may run before the claim barrier.
+            auto stage_box = [&](int k, bool claim, uint32_t salt) {
                 const unsigned long long key = base_key | (unsigned long long)k;
+                const uint32_t stamp = stamp_of(k) + salt;
                 int box = 1;
                 for (int d = 0; d < D; ++d) box *= s_box_dims[d];
-                // stage the box and its cells
                 for (int q = tid; q < box; q += TB) {
                     int xg[3];
                     // a fixed lattice's rim outside the box maps to its medium halo
                     const int gf = P.gflat_of_box(q, xg);
                     const uint32_t id = __ldcg(g.sigma + gf);
                     P.sig[q] = (uint16_t)id;
+                    if (id && atomicExch(&seen[id], stamp) != stamp) {
+                        if (claim) atomicMin(claims + id, key);
+                        clist[atomicAdd(&s_ncell, 1)] = id;
+                    }
+                }
+                __syncthreads();
+                const int nc = s_ncell;
+                for (int i = tid; i <= nc; i += TB) {
+                    const uint32_t id = i < nc ? clist[i] : 0u;  // the medium rides along as entry nc
                     P.vol[id] = __ldcg(g.volume + id);
                     P.itf[id] = __ldcg(g.interface + id);
                     P.adh[id] = g.adh_of[id];
                     P.dirty[id] = 0;
                     P.mod[id] = 0;
+                }
+            };
+            // own[id]: the lowest claiming tile of this sub-phase is this one
+            auto read_claims = [&](int k) {
+                const unsigned long long key = base_key | (unsigned long long)k;
+                const int nc = s_ncell;
+                for (int i = tid; i <= nc; i += TB) {
+                    const uint32_t id = i < nc ? clist[i] : 0u;
                     P.own[id] = id == 0 || __ldcg(claims + id) == key;
                 }
                 __syncthreads();
+            };
+            // With one tile per CTA the box is staged while claiming.
+            const bool single = per_color <= nblk;
+            long long t_c0 = clock64();
+            if (single) {
+                if (blockIdx.x < per_color) {
+                    setup_tile(blockIdx.x);
+                    stage_box(blockIdx.x, true, 0u);
+                }
+            } else {
+                // ---- claim the cells of every box this CTA will process
+                for (int k = blockIdx.x; k < per_color; k += nblk) {
+                    int tc[3];
+                    tile_coords(k, tc);
+                    int bdim[3], x0[3];
+                    int box = 1;
+                    for (int d = 0; d < D; ++d) {
+                        const int L = g.dims[d];
+                        const int b0 = tile_begin(tc[d], L, tg.nt[d]), b1 = tile_begin(tc[d] + 1, L, tg.nt[d]);
+                        x0[d] = b0 + tg.off[d];
+                        bdim[d] = b1 - b0 + 2;
+                        box *= bdim[d];
+                    }
+                    const unsigned long long key = base_key | (unsigned long long)k;
+                    const uint32_t stamp = stamp_of(k);
+                    for (int q = tid; q < box; q += TB) {
+                        int r = q, gf = 0;
+                        for (int d = D - 1; d >= 0; --d) {
+                            const int i = r % bdim[d];
+                            r /= bdim[d];
+                            int x = x0[d] + i - 1;
+                            if (g.periodic) { x %= g.dims[d]; if (x < 0) x += g.dims[d]; }
+                            gf += (x + 1) * (int)g.strides[d];
+                        }
+                        const uint32_t id = __ldcg(g.sigma + gf);
+                        if (id && atomicExch(&seen[id], stamp) != stamp) atomicMin(claims + id, key);
+                    }
+                    __syncthreads();
+                }
+            }
+            const long long t_c1 = clock64();
+            if (!grid_sync(bar, nblk, bar_epoch)) { alive = false; break; }
+            const long long t_c2 = clock64();
+            cyc_sync += t_c2 - t_c0;
+            cyc_claim += t_c1 - t_c0;
+            cyc_bar1 += t_c2 - t_c1;
+            // ---- process the tiles
+            for (int k = blockIdx.x; k < per_color; k += nblk) {
+                long long t_s0 = clock64();
+                if (!single) {
+                    setup_tile(k);
+                    stage_box(k, false, 512u);  // a stamp distinct from the claim pass over this box
+                    __syncthreads();
+                }
+                read_claims(k);
+                const unsigned long long key = base_key | (unsigned long long)k;
+                (void)key;
+                int box = 1;
+                for (int d = 0; d < D; ++d) box *= s_box_dims[d];
                 long long t_p0 = clock64();
                 cyc_stage += t_p0 - t_s0;
                 // site-colour passes of this tile, random order
@@ -654,11 +787,14 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                     const int n = min(s_n, TCMAX);
                     __syncthreads();
                     ct.c_build += clock64() - tb0;
-                    if (n > 32) {
+                    if (n > 64) {
                         P.resolve(n, mcs, ct);
                         ct.wide++;
                     } else if (n > 0) {
-                        if (tid < 32) P.resolve_warp(n, mcs, ct);
+                        if (tid < 32) {
+                            if (n > 32) P.template resolve_warp<2>(n, mcs, ct);
+                            else P.template resolve_warp<1>(n, mcs, ct);
+                        }
                         __syncthreads();
                     }
                     attempts += tid == 0 ? (unsigned long long)n_class : 0ull;
@@ -683,9 +819,9 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                     }
                 }
                 __syncthreads();
-                for (int q = tid; q < box; q += TB) {
-                    const uint32_t id = P.sig[q];
-                    if (id && P.own[id] && P.mod[id]) {
+                for (int i = tid; i < s_ncell; i += TB) {
+                    const uint32_t id = clist[i];
+                    if (P.own[id] && P.mod[id]) {
                         __stcg(g.volume + id, P.vol[id]);
                         __stcg(g.interface + id, P.itf[id]);
                     }
@@ -693,10 +829,10 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                 __syncthreads();
                 cyc_stage += clock64() - t_w0;
             }
-            __threadfence();
             long long t_b0 = clock64();
-            if (!grid_sync(bar, nblk)) { alive = false; break; }
+            if (!grid_sync(bar, nblk, bar_epoch)) { alive = false; break; }
             cyc_sync += clock64() - t_b0;
+            cyc_bar2 += clock64() - t_b0;
         }
     }
     // statistics: every site was attempted once per completed MCS
@@ -721,6 +857,9 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
         atomicAdd(&g.stats[CPM_STAT_CYC_APPLY], ct.c_apply);
         atomicAdd(&g.stats[CPM_STAT_WIDE_PASSES], ct.wide);
         atomicAdd(&g.stats[CPM_STAT_CYC_LOWER], ct.c_lower);
+        atomicAdd(&g.stats[CPM_STAT_CYC_CLAIM], cyc_claim);
+        atomicAdd(&g.stats[CPM_STAT_CYC_BAR_CLAIM], cyc_bar1);
+        atomicAdd(&g.stats[CPM_STAT_CYC_BAR_WRITE], cyc_bar2);
         if (blockIdx.x == 0) {
             atomicAdd(&g.stats[CPM_STAT_PASSES], (unsigned long long)n_mcs * (D == 2 ? 16 : 64));
             if (alive) simp->mcs = mcs0 + n_mcs;

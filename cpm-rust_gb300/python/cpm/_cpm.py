@@ -59,6 +59,10 @@ STAT_NAMES = (
     "cycles_apply",
     "wide_passes",
     "cycles_lower",
+    "cycles_claim",
+    "cycles_barrier_claim",
+    "cycles_barrier_write",
+    "exact_decisions",
 )
 
 

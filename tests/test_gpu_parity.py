@@ -123,6 +123,33 @@ def test_sweep_decision_at_the_metropolis_threshold(name, cuda_required):
     assert checked > 1000
 
 
+def test_sweep_decision_for_zero_delta_h(cuda_required):
+    """dh == 0 (the float bracket straddles zero) accepts for every u, up to
+    the largest u below 1; small non-zero dh keep the reference's rule."""
+    model = MODELS["sorting_moore"]()
+    sim = model.oracle()
+    eng = _engine(model)
+    rng = np.random.default_rng(11)
+    n_zero = 0
+    for _ in range(3):
+        sim.run_mcs(30)
+        v, i, sp, so = padded_cells(sim)
+        eng.write_state(sim.padded(), v, i, sp, so)
+        t = random_interior_targets(sim, 40000, rng)
+        k = rng.integers(0, 4, t.size)
+        first = sim.evaluate_moves(t, k, np.full(t.size, 0.5))
+        sel = np.flatnonzero((first["evaluated"] == 1) & (np.abs(first["delta_h"]) < 0.5))
+        n_zero += int((first["delta_h"][sel] == 0).sum())
+        us = np.array([0.0, 0.5, 0.999, 1 - 1e-6, 1 - 3 * 2.0**-53, 1 - 2 * 2.0**-53, 1 - 2.0**-53])
+        tt = np.repeat(t[sel], us.size)
+        kk = np.repeat(k[sel], us.size)
+        u = np.tile(us, sel.size)
+        got = eng.evaluate_moves(tt, kk, u)
+        want = sim.evaluate_moves(tt, kk, u)
+        _compare(got, want)
+    assert n_zero > 10, n_zero
+
+
 @pytest.mark.parametrize("D", [2, 3])
 def test_topology_verdicts_on_random_patterns(D, cuda_required):
     """Random ids on the lattice give arbitrary 8/26-bit neighbourhood patterns."""
@@ -319,3 +346,28 @@ def test_tiled_sweep_keeps_exact_state(name, cuda_required, monkeypatch):
     again.run_mcs(n - n // 2)
     again.synchronize()
     assert np.array_equal(again.lattice(), lat)
+
+
+@pytest.mark.parametrize("D", [2, 3])
+def test_tiled_sweep_independent_of_grid(D, cuda_required, monkeypatch):
+    """Tiles, claims and priorities are functions of (seed, MCS, tile id): a
+    grid with several tiles per CTA gives the same trajectory as one tile
+    per CTA."""
+    monkeypatch.setenv("CPM_GPU_FORCE_TILED", "1")
+    model = sorting_model(side=128, seed=16) if D == 2 else organoid_model(side=64, counts=(60, 60), seed=17)
+    n = 12 if D == 2 else 3
+    wide = _engine(model)
+    wide.run_mcs(n)
+    wide.synchronize()
+    monkeypatch.setenv("CPM_GPU_TILED_GRID", "3")
+    narrow = _engine(model)
+    narrow.run_mcs(n)
+    narrow.synchronize()
+    assert np.array_equal(wide.lattice(), narrow.lattice())
+    a, b = wide.stats(), narrow.stats()
+    for k in ("attempts", "nonnull", "accepted", "evaluated", "deferred", "rounds"):
+        assert a[k] == b[k], (k, a[k], b[k])
+    ok, _, _ = narrow.recount_check()
+    assert ok
+    assert np.array_equal(wide.cells()[2], narrow.cells()[2])
+
