@@ -351,7 +351,8 @@ def run_gpu(args, rank, world, dist):
             "algorithmic_bytes_per_attempt": bytes_per_attempt,
         },
         "stats": {"f_nonnull": f_nonnull, "f_acc": f_acc,
-                  "rounds_per_pass": (s1["rounds"] - s0["rounds"]) / max(1, s1["passes"] - s0["passes"])},
+                  "rounds_per_pass": (s1["rounds"] - s0["rounds"]) / max(1, s1["passes"] - s0["passes"]),
+                  "exact_decisions": s1["exact_decisions"] - s0["exact_decisions"]},
         "clocks": clk,
     }
     if world == 1 and not args.no_cpu:
@@ -366,8 +367,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--mcs-per-step", type=int, default=50)
-    ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--e2e-mcs", type=int, default=100)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-mcs", type=int, default=1000)
     ap.add_argument("--cpu-mcs", type=int, default=200)
     ap.add_argument("--ref-mcs", type=int, default=40)
     ap.add_argument("--no-cpu", action="store_true")

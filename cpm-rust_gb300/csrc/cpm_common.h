@@ -22,7 +22,7 @@ enum CpmStat {
     CPM_STAT_EVALUATED = 4,  // reached Delta-H
     CPM_STAT_ACCEPTED = 5,
     CPM_STAT_ROUNDS = 6,     // conflict-resolution rounds (summed over passes)
-    CPM_STAT_PASSES = 7,
+    CPM_STAT_PASSES = 7,         // colour passes (tiled sweep: tile passes, one per tile and site colour)
     CPM_STAT_SPIN_TIMEOUTS = 8,  // bounded waits that gave up (must stay 0)
     CPM_STAT_FIXPOINT_ITERS = 9, // fixpoint iterations summed over threads
     CPM_STAT_H2D_BYTES = 10,     // host-to-device bytes of the call (host-side count)

@@ -520,7 +520,7 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
         __syncthreads();
     }
     TileCounters ct = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    unsigned long long attempts = 0;
+    unsigned long long attempts = 0, tile_passes = 0;
     unsigned long long cyc_pass = 0, cyc_stage = 0, cyc_sync = 0, cyc_claim = 0, cyc_bar1 = 0, cyc_bar2 = 0;
     const uint64_t mcs0 = g.mcs;
     bool alive = true;
@@ -798,6 +798,7 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                         __syncthreads();
                     }
                     attempts += tid == 0 ? (unsigned long long)n_class : 0ull;
+                    tile_passes += tid == 0 ? 1ull : 0ull;
                 }
                 long long t_w0 = clock64();
                 cyc_pass += t_w0 - t_p0;
@@ -860,10 +861,8 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
         atomicAdd(&g.stats[CPM_STAT_CYC_CLAIM], cyc_claim);
         atomicAdd(&g.stats[CPM_STAT_CYC_BAR_CLAIM], cyc_bar1);
         atomicAdd(&g.stats[CPM_STAT_CYC_BAR_WRITE], cyc_bar2);
-        if (blockIdx.x == 0) {
-            atomicAdd(&g.stats[CPM_STAT_PASSES], (unsigned long long)n_mcs * (D == 2 ? 16 : 64));
-            if (alive) simp->mcs = mcs0 + n_mcs;
-        }
+        atomicAdd(&g.stats[CPM_STAT_PASSES], tile_passes);
+        if (blockIdx.x == 0 && alive) simp->mcs = mcs0 + n_mcs;
         if (!alive) {
             atomicAdd(&g.stats[CPM_STAT_SPIN_TIMEOUTS], 1ull);
             if (g.error) atomicExch(g.error, 5);
