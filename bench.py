@@ -106,6 +106,88 @@ def oracle_spec():
     return O.ModelSpec(GRID, True, [t[1:] for t in TYPES], adhesion(SEED), cell_counts=[PER_TYPE] * 4)
 
 
+# ------------------------------------------------- batch workload (C4) ----
+BATCH_SIDES = (64, 96, 128, 192, 256)
+
+
+def batch_thetas(n, seed=2):
+    """n theta vectors of the 2-type model, layout [lambda_V[2], lambda_I[2],
+    J upper triangle incl. the medium row (6), lambda_Act[2], MaxAct[2]]
+    (theta.rs:43-50), and one grid side per theta."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    sides = rng.choice(BATCH_SIDES, size=n)
+    lv = rng.uniform(1, 20, (n, 2))
+    li = rng.uniform(0, 5, (n, 2))
+    jm = rng.uniform(5, 20, (n, 2))
+    jt = rng.uniform(0, 20, (n, 3))
+    thetas = [[float(x) for x in (*lv[i], *li[i], 0.0, jm[i, 0], jm[i, 1], jt[i, 0], jt[i, 1], jt[i, 2])] +
+              [0.0, 0.0, 0.0, 0.0] for i in range(n)]
+    return [int(x) for x in sides], thetas
+
+
+def batch_sim(side, theta, seed):
+    """One member of the batch: side x side periodic, 2 types (V*=50,
+    I*=75), phi = 0.7 split evenly, parameters from theta."""
+    import warnings
+
+    import cpm
+
+    sim = cpm.CPM(grid=(side, side), boundary="periodic", seed=seed)
+    for t in range(2):
+        sim.register_cell_type(f"t{t}", 50, 75, theta[t], theta[2 + t])
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        n = cpm.cells_for_density((side, side), 50, 0.35)
+    for t in range(2):
+        sim.add_cells(f"t{t}", n)
+    j = theta[4:10]
+    sim.set_adhesion([[j[0], j[1], j[2]], [j[1], j[3], j[4]], [j[2], j[4], j[5]]])
+    sim.initialize(warn_on_default_init=False)
+    return sim
+
+
+def run_batch_bench(args):
+    """Batched sims/s (all thetas in one persistent launch through
+    cpm.run_many) against a loop of single runs (cpm.CPM.run per theta) on
+    one theta of each grid side; seeds derive_seed_u64(master, i)."""
+    import cpm
+    from cpm import _cpm
+
+    burn, readout, interval = args.batch_mcs
+    sides, thetas = batch_thetas(args.batch_n)
+    master = 7
+    seeds = [_cpm.derive_seed_u64(master, i) for i in range(args.batch_n)]
+    sims = [batch_sim(sides[i], thetas[i], seeds[i]) for i in range(args.batch_n)]
+    t0 = time.perf_counter()
+    res = cpm.run_many(sims, burn, readout, interval)
+    t_batch = time.perf_counter() - t0
+    attempts = sum(r.stats["attempts"] for r in res)
+    # the plain loop: one theta per side (the sides are uniform over the set)
+    loop_t = []
+    for side in BATCH_SIDES:
+        i = sides.index(side)
+        sim = batch_sim(sides[i], thetas[i], seeds[i])
+        t0 = time.perf_counter()
+        sim.run(burn, readout, interval)
+        loop_t.append(time.perf_counter() - t0)
+    loop_sims_s = len(loop_t) / sum(loop_t)
+    batch_sims_s = args.batch_n / t_batch
+    return {
+        "workload": f"{args.batch_n} thetas, 2 types (V*=50, I*=75), side uniform in {list(BATCH_SIDES)}, phi=0.7, "
+                    f"Moore energy, periodic; {burn} burn-in + {readout} readout MCS, sampling every {interval}",
+        "sims_per_s": batch_sims_s,
+        "attempts_per_s": attempts / t_batch,
+        "seconds": t_batch,
+        "plain_loop_sims_per_s": loop_sims_s,
+        "plain_loop_sample": "one theta per side, each run alone through cpm.CPM.run; seconds per side " +
+                             ", ".join(f"{s}:{t:.2f}" for s, t in zip(BATCH_SIDES, loop_t)),
+        "speedup_vs_plain_loop": batch_sims_s / loop_sims_s,
+        "timed": "cpm.run_many(...) end to end: host placement, upload, one persistent launch, readouts",
+    }
+
+
 # --------------------------------------------------------------- clocks ----
 class ClockSampler:
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -357,6 +439,8 @@ def run_gpu(args, rank, world, dist):
     }
     if world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args)
+    if args.batch_n > 0:
+        line["batch"] = run_batch_bench(args)
     print(json.dumps(line), flush=True)
 
 
@@ -372,6 +456,9 @@ def main():
     ap.add_argument("--cpu-mcs", type=int, default=200)
     ap.add_argument("--ref-mcs", type=int, default=40)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--batch-n", type=int, default=4096, help="thetas of the batch workload (0 skips it)")
+    ap.add_argument("--batch-mcs", type=lambda v: tuple(int(x) for x in v.split(",")), default=(2000, 2000, 100),
+                    help="burn-in,readout,interval MCS of each batch member")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

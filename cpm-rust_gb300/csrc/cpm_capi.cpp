@@ -10,7 +10,9 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <atomic>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/cpm_gpu.h"
@@ -452,9 +454,24 @@ static int prepare(const cpm_builder* const* builders, size_t n, std::vector<Con
         std::string msg = validate(cfgs[i]);
         if (!msg.empty()) return fail(CPM_E_CONFIG, msg);
         if ((e = check_supported(cfgs[i]))) return e;
-        msg = initialize(cfgs[i], inits[i]);
-        if (!msg.empty()) return fail(CPM_E_INIT, msg);
     }
+    // placements are independent: host threads over simulations; the first
+    // failure in input order is reported
+    std::vector<std::string> errs(n);
+    std::atomic<size_t> next{0};
+    auto worker = [&]() {
+        for (size_t i; (i = next.fetch_add(1)) < n;) errs[i] = initialize(cfgs[i], inits[i]);
+    };
+    const unsigned nthreads = (unsigned)std::max<size_t>(1, std::min<size_t>(std::thread::hardware_concurrency(), n));
+    if (nthreads == 1) {
+        worker();
+    } else {
+        std::vector<std::thread> th;
+        for (unsigned t = 0; t < nthreads; ++t) th.emplace_back(worker);
+        for (auto& t : th) t.join();
+    }
+    for (size_t i = 0; i < n; ++i)
+        if (!errs[i].empty()) return fail(CPM_E_INIT, errs[i]);
     return ok();
 }
 

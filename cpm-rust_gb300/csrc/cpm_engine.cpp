@@ -102,6 +102,7 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
     // Selects the tiled sweep wherever it applies (tests use it on lattices
     // small enough for the resident sweep).
     force_tiled_ = std::getenv("CPM_GPU_FORCE_TILED") != nullptr;
+    prefer_tiled_ = std::getenv("CPM_GPU_PREFER_TILED") != nullptr;
     const size_t N = configs.size();
     layouts_.resize(N);
     descs_.resize(N);
@@ -334,13 +335,20 @@ DeviceSims::Path DeviceSims::path(size_t i) const {
     const SimLayout& L = layouts_[i];
     if (force_global_) return GLOBAL;
     if (L.n_cells >= 65535) return GLOBAL;
-    if (!force_tiled_ && cpmgpu::resident_smem_bytes(L.g.n_padded, L.n_cells) <= cpmgpu::resident_smem_limit())
+    int dims[3] = {(int)L.g.dims[0], (int)L.g.dims[1], (int)L.g.dims[2]}, nt[3] = {1, 1, 1}, max_box = 0;
+    const bool tiled_ok = cpmgpu::tiled_plan(L.g.D, dims, L.g.periodic, nt, &max_box) &&
+                          cpmgpu::tiled_smem_bytes(max_box, L.n_cells) <= cpmgpu::resident_smem_limit();
+    if (!force_tiled_ && cpmgpu::resident_smem_bytes(L.g.n_padded, L.n_cells) <= cpmgpu::resident_smem_limit()) {
+        // The path is a function of the simulation's own configuration, so a
+        // simulation's trajectory is the same alone and inside any batch.
+        // CPM_GPU_PREFER_TILED opts a simulation with at least 8 tiles per
+        // colour into the tiled sweep (many SMs instead of one; a different,
+        // equally exact chain, hence opt-in).
+        const int per_color = (nt[0] * nt[1] * nt[2]) >> L.g.D;
+        if (prefer_tiled_ && tiled_ok && per_color >= 8) return TILED;
         return RESIDENT;
-    int dims[3] = {(int)L.g.dims[0], (int)L.g.dims[1], (int)L.g.dims[2]}, nt[3], max_box = 0;
-    if (cpmgpu::tiled_plan(L.g.D, dims, L.g.periodic, nt, &max_box) &&
-        cpmgpu::tiled_smem_bytes(max_box, L.n_cells) <= cpmgpu::resident_smem_limit())
-        return TILED;
-    return GLOBAL;
+    }
+    return tiled_ok ? TILED : GLOBAL;
 }
 
 // One simulation on the tiled sweep: the run window is replayed from the

@@ -84,6 +84,7 @@ class DeviceSims {
     cudaStream_t stream_ = 0;
     bool force_global_ = false;
     bool force_tiled_ = false;
+    bool prefer_tiled_ = false;
     void* d_bar_ = nullptr;
     std::vector<size_t> tiled_ran_;
     std::string run_tiled(const RunPlan& p, const uint64_t* t3);

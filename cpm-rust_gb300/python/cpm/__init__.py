@@ -2,12 +2,13 @@
 DebajyotiS/cpm-rust (`cpm.CPM`, `cells_for_density`, the warning classes),
 running the Monte Carlo hot loop as sm_103a kernels through libcpm_gpu.so."""
 
-from .model import CPM
+from .model import CPM, run_many
 from .parameters import cells_for_density
 from .warnings import CPMInitializationWarning, CPMLowResolutionWarning
 
 __all__ = [
     "CPM",
+    "run_many",
     "cells_for_density",
     "CPMInitializationWarning",
     "CPMLowResolutionWarning",

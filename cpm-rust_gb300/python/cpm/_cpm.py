@@ -311,7 +311,7 @@ class Sample:
 class RunResult:
     """PyRunResult (convert.rs:97-115)."""
 
-    __slots__ = ("metadata", "status", "samples", "cell_type_index", "cell_type_names", "stats")
+    __slots__ = ("metadata", "status", "samples", "cell_type_index", "cell_type_names", "stats", "used_default")
 
 
 def _result_from_handle(h) -> RunResult:
@@ -391,6 +391,7 @@ def _result_from_handle(h) -> RunResult:
         r = RunResult()
         r.metadata, r.status, r.samples = meta, status, samples
         r.cell_type_index, r.cell_type_names = cti, names
+        r.used_default = bool(info.used_default)
         r.stats = {name: int(stats[i]) for i, name in enumerate(STAT_NAMES)}
         return r
     finally:

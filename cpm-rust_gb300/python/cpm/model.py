@@ -108,3 +108,17 @@ class CPM:
         if any_used_default and self._warn_on_default_init:
             warnings.warn(_BATCH, CPMInitializationWarning, stacklevel=2)
         return results
+
+
+def run_many(sims: list[CPM], burn_in_mcs: int, readout_mcs: int, sampling_interval_mcs: int,
+             include_lattice: bool = False, topology: bool = True) -> list[Any]:
+    """Runs many independent simulations, each with its own grid, parameters
+    and seed, in one persistent device launch (an extension: the reference's
+    ``run_batch`` shares one grid). ``topology=False`` skips the contact graph
+    and labelling readouts. At most one warning for the whole set."""
+    results = _cpm.run_many([s._raw for s in sims], burn_in_mcs, readout_mcs, sampling_interval_mcs,
+                            include_lattice=include_lattice, topology=topology)
+    if any(r.used_default and s._warn_on_default_init for s, r in zip(sims, results)):
+        warnings.warn(_BATCH, CPMInitializationWarning, stacklevel=2)
+    return results
+

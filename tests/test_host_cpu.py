@@ -209,3 +209,15 @@ def test_cells_for_density_matches_reference_helper():
     # the survey's config sizes
     assert cpm.cells_for_density((512, 512), 50, 0.2) == 1049
     assert cpm.cells_for_density((128, 128, 128), 1048, 0.8 / 3) == 534
+
+
+def test_batch_workload_theta_round_trip():
+    """The batch benchmark's members carry exactly their theta (theta.rs
+    layout): extract_theta() of each built simulation returns it."""
+    import bench
+
+    sides, thetas = bench.batch_thetas(12)
+    for side, th in zip(sides, thetas):
+        sim = bench.batch_sim(side, th, seed=3)
+        assert sim.extract_theta() == th
+        assert len(th) == len(sim.theta_names()) == 14
