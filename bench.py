@@ -188,6 +188,145 @@ def run_batch_bench(args):
     }
 
 
+# ------------------------------------------------ serving workload (C5) ----
+def organoid_placement(side, per_type):
+    """Explicit 3D placement for densities scatter-and-grow cannot seed:
+    one 2x2x2 seed per cell on a cubic grid of spacing >= 2, the seeds
+    nearest the centre first, types in order from the centre outwards
+    (nested spherical layers); the cells grow to their volume in burn-in."""
+    import numpy as np
+
+    k = int(sum(per_type))
+    g = max(2, int((side ** 3 / max(k, 1)) ** (1.0 / 3.0)))
+    while True:
+        ax = np.arange(g // 2, side - 1, g)
+        pts = np.stack(np.meshgrid(ax, ax, ax, indexing="ij"), -1).reshape(-1, 3)
+        if len(pts) >= k or g == 2:
+            break
+        g -= 1
+    if len(pts) < k:
+        raise ValueError(f"{k} cells do not fit a {side}^3 lattice")
+    c = (side - 1) / 2.0
+    order = np.lexsort((np.arange(len(pts)), ((pts - c) ** 2).sum(1)))
+    pts = pts[order[:k]]
+    lat = np.zeros((side, side, side), dtype=np.uint32)
+    for i, (x, y, z) in enumerate(pts):
+        lat[x:x + 2, y:y + 2, z:z + 2] = i + 1
+    types = np.repeat(np.arange(len(per_type)), per_type)
+    return lat.ravel(), types
+
+
+def serve_requests(n, rate=200.0, seed=5):
+    """The request stream: Poisson arrivals, 70 % 2D (side U{64..512}) and
+    30 % 3D (side U{32..96}), theta drawn as for the batch workload, MCS
+    U{1000..5000} split evenly into burn-in and readout, sampling every 100."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    arrival = np.cumsum(rng.exponential(1.0 / rate, n))
+    two_d = rng.random(n) < 0.7
+    side2 = rng.integers(64, 513, n)
+    side3 = rng.integers(32, 97, n)
+    mcs = rng.integers(1000, 5001, n)
+    lv = rng.uniform(1, 20, (n, 2))
+    li = rng.uniform(0, 5, (n, 2))
+    jm = rng.uniform(5, 20, (n, 2))
+    jt = rng.uniform(0, 20, (n, 3))
+    out = []
+    for i in range(n):
+        burn = int(mcs[i] // 2 // 100 * 100)
+        readout = max(100, int((mcs[i] - burn) // 100 * 100))
+        theta = [float(x) for x in (*lv[i], *li[i], 0.0, jm[i, 0], jm[i, 1], jt[i, 0], jt[i, 1], jt[i, 2])]
+        out.append({"arrival": float(arrival[i]), "D": 2 if two_d[i] else 3,
+                    "side": int(side2[i] if two_d[i] else side3[i]), "burn": burn, "readout": readout,
+                    "interval": 100, "theta": theta, "seed": 1000 + i})
+    return out
+
+
+def serve_sim(q):
+    """One request: 2D as the batch members (V*=50, I*=75, scatter-and-grow,
+    phi=0.7); 3D organoid-like (V*=1048, I*=600, 26-neighbour energy,
+    explicit nested-layer placement, phi=0.7)."""
+    import warnings
+
+    import cpm
+
+    th = q["theta"]
+    j = th[4:10]
+    adh = [[j[0], j[1], j[2]], [j[1], j[3], j[4]], [j[2], j[4], j[5]]]
+    side = q["side"]
+    if q["D"] == 2:
+        return batch_sim(side, th + [0.0] * 4, q["seed"])
+    sim = cpm.CPM(grid=(side, side, side), boundary="periodic", seed=q["seed"], energy_neighborhood="twenty_six")
+    for t in range(2):
+        sim.register_cell_type(f"t{t}", 1048, 600, th[t], th[2 + t])
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        n = max(1, cpm.cells_for_density((side, side, side), 1048, 0.35))
+    for t in range(2):
+        sim.add_cells(f"t{t}", n)
+    sim.set_adhesion(adh)
+    lat, types = organoid_placement(side, [n, n])
+    sim.initialize(lattice=lat.tolist(), cell_type_of=types.tolist(), warn_on_default_init=False)
+    return sim
+
+
+def run_serve_bench(args):
+    """Latency and throughput of the serving loop on the request stream,
+    against each request run alone on an idle server."""
+    import numpy as np
+
+    import cpm
+
+    reqs = serve_requests(args.serve_n, rate=args.serve_rate)
+    sims = [serve_sim(q) for q in reqs]
+    attempts = [q["side"] ** q["D"] * (q["burn"] + q["readout"]) for q in reqs]
+    # alone: one request at a time on an idle server
+    alone = []
+    with cpm.Server() as srv:
+        for q, sim in zip(reqs, sims):
+            t = srv.submit(sim, q["burn"], q["readout"], q["interval"])
+            st, res, tm = srv.wait(t)
+            assert st == "done", st
+            alone.append(tm["finished_s"] - tm["submitted_s"])
+    # the stream: submitted at their arrival times
+    lat = [0.0] * len(reqs)
+    with cpm.Server() as srv:
+        t0 = time.perf_counter()
+        tickets = []
+        for q, sim in zip(reqs, sims):
+            dt = q["arrival"] - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(dt)
+            tickets.append(srv.submit(sim, q["burn"], q["readout"], q["interval"]))
+        for i, t in enumerate(tickets):
+            st, res, tm = srv.wait(t)
+            assert st == "done", st
+            lat[i] = tm["finished_s"] - tm["submitted_s"]
+        wall = time.perf_counter() - t0
+        stats = srv.stats()
+    lat = np.array(lat)
+    alone = np.array(alone)
+    ratio = lat / alone
+    return {
+        "workload": f"{len(reqs)} requests, Poisson arrivals at {args.serve_rate:g}/s; 70% 2D side U{{64..512}} "
+                    "(V*=50, I*=75), 30% 3D side U{32..96} (V*=1048, I*=600, 26-neighbour), phi=0.7, theta as the "
+                    "batch workload, MCS U{1000..5000} half burn-in, sampling every 100",
+        "p50_latency_s": float(np.percentile(lat, 50)),
+        "p99_latency_s": float(np.percentile(lat, 99)),
+        "isolated_p50_s": float(np.percentile(alone, 50)),
+        "isolated_p99_s": float(np.percentile(alone, 99)),
+        "latency_over_isolated_p50": float(np.percentile(ratio, 50)),
+        "latency_over_isolated_p99": float(np.percentile(ratio, 99)),
+        "sims_per_s": len(reqs) / wall,
+        "attempts_per_s": float(sum(attempts)) / wall,
+        "offered_attempts_per_s": float(sum(attempts)) / reqs[-1]["arrival"],
+        "wall_s": wall,
+        "peak_active": stats["peak_active"],
+        "peak_device_bytes": stats["peak_bytes"],
+    }
+
+
 # --------------------------------------------------------------- clocks ----
 class ClockSampler:
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -441,6 +580,8 @@ def run_gpu(args, rank, world, dist):
         line["cpu_baseline"] = cpu_baseline(args)
     if args.batch_n > 0:
         line["batch"] = run_batch_bench(args)
+    if args.serve_n > 0:
+        line["serve"] = run_serve_bench(args)
     print(json.dumps(line), flush=True)
 
 
@@ -459,6 +600,8 @@ def main():
     ap.add_argument("--batch-n", type=int, default=4096, help="thetas of the batch workload (0 skips it)")
     ap.add_argument("--batch-mcs", type=lambda v: tuple(int(x) for x in v.split(",")), default=(2000, 2000, 100),
                     help="burn-in,readout,interval MCS of each batch member")
+    ap.add_argument("--serve-n", type=int, default=0, help="requests of the serving workload (0 skips it)")
+    ap.add_argument("--serve-rate", type=float, default=200.0, help="Poisson arrival rate of the requests (1/s)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -19,6 +19,7 @@
 #include "cpm_engine.h"
 #include "cpm_host.h"
 #include "cpm_kernels.h"
+#include "cpm_serve.h"
 
 using namespace cpmhost;
 
@@ -779,3 +780,114 @@ extern "C" int cpm_builder_hashes(const cpm_builder* b, uint64_t burn, uint64_t 
 }
 
 extern "C" uint64_t cpm_derive_seed_u64(uint64_t master, uint64_t index) { return derive_seed_u64(master, index); }
+
+// ------------------------------------------------------------ serving ----
+struct cpm_server {
+    Server s;
+};
+
+static void copy_times(const ReqTimes& t, cpm_request_times* o) {
+    if (!o) return;
+    o->submitted_s = t.submitted;
+    o->admitted_s = t.admitted;
+    o->device_done_s = t.device_done;
+    o->finished_s = t.finished;
+    o->device_bytes = t.device_bytes;
+}
+
+extern "C" int cpm_serve_start(const cpm_serve_options* o, cpm_server** out) {
+    if (!out) return fail(CPM_E_ARG, "null argument");
+    auto sv = std::make_unique<cpm_server>();
+    ServeOptions opt;
+    if (o) {
+        if (o->hbm_budget_bytes) opt.hbm_budget = o->hbm_budget_bytes;
+        if (o->max_active > 0) opt.max_active = o->max_active;
+        opt.placement_threads = o->placement_threads;
+        if (o->tiled_grid_cap > 0) opt.tiled_grid_cap = o->tiled_grid_cap;
+    }
+    const std::string e = sv->s.start(opt);
+    if (!e.empty()) return fail(CPM_E_CUDA, e);
+    *out = sv.release();
+    return ok();
+}
+
+extern "C" int cpm_serve_submit(cpm_server* s, const cpm_builder* b, uint64_t burn, uint64_t readout, uint64_t interval,
+                                int32_t include_lattice, int32_t topology, uint64_t* ticket) {
+    if (!s || !b || !ticket) return fail(CPM_E_ARG, "null argument");
+    Config c;
+    int rc = resolve(b, burn, readout, interval, c);
+    if (rc) return rc;
+    const std::string msg = validate(c);
+    if (!msg.empty()) return fail(CPM_E_CONFIG, msg);
+    if ((rc = check_supported(c))) return rc;
+    ReadoutOptions ro;
+    ro.include_lattice = include_lattice != 0;
+    ro.topology = topology != 0;
+    const std::string e = s->s.submit(c, ro, *ticket);
+    if (!e.empty()) return fail(CPM_E_ARG, e);
+    return ok();
+}
+
+static int serve_outcome(ReqState st, Result& r, const std::string& err, int32_t* state, cpm_result** out) {
+    if (state) *state = (int32_t)st;
+    if (st == REQ_DONE && out) {
+        auto h = std::make_unique<cpm_result>();
+        h->r = std::move(r);
+        *out = h.release();
+    }
+    if (st == REQ_FAILED) return fail(code_for(err), err);
+    return ok();
+}
+
+extern "C" int cpm_serve_poll(cpm_server* s, uint64_t ticket, int32_t* state, cpm_result** out,
+                              cpm_request_times* times) {
+    if (!s) return fail(CPM_E_ARG, "null argument");
+    Result r;
+    ReqTimes t;
+    std::string err;
+    const ReqState st = s->s.poll(ticket, out != nullptr, &r, &t, &err);
+    copy_times(t, times);
+    return serve_outcome(st, r, err, state, out);
+}
+
+extern "C" int cpm_serve_wait(cpm_server* s, uint64_t ticket, double timeout_s, int32_t* state, cpm_result** out,
+                              cpm_request_times* times) {
+    if (!s) return fail(CPM_E_ARG, "null argument");
+    Result r;
+    ReqTimes t;
+    std::string err;
+    const ReqState st = s->s.wait(ticket, timeout_s, &r, &t, &err);
+    copy_times(t, times);
+    return serve_outcome(st, r, err, state, out);
+}
+
+extern "C" int cpm_serve_cancel(cpm_server* s, uint64_t ticket) {
+    if (!s) return fail(CPM_E_ARG, "null argument");
+    if (!s->s.cancel(ticket)) return fail(CPM_E_ARG, "ticket " + std::to_string(ticket) + " is not pending");
+    return ok();
+}
+
+extern "C" int cpm_serve_stats_get(cpm_server* s, cpm_serve_stats* o) {
+    if (!s || !o) return fail(CPM_E_ARG, "null argument");
+    const ServeStats t = s->s.stats();
+    o->submitted = t.submitted;
+    o->completed = t.completed;
+    o->failed = t.failed;
+    o->cancelled = t.cancelled;
+    o->launched = t.launched;
+    o->active = t.active;
+    o->queued = t.queued;
+    o->peak_active = t.peak_active;
+    o->bytes_in_use = t.bytes_in_use;
+    o->peak_bytes = t.peak_bytes;
+    o->busy_seconds = t.busy_seconds;
+    return ok();
+}
+
+extern "C" int cpm_serve_stop(cpm_server* s) {
+    if (!s) return fail(CPM_E_ARG, "null argument");
+    s->s.stop();
+    delete s;
+    return ok();
+}
+

@@ -73,12 +73,20 @@ const uint64_t* device_table3d(std::string& err) {
 }
 
 // --------------------------------------------------------- DeviceSims ----
+// Stream-ordered allocations (cudaMallocAsync) do not serialise the work of
+// other streams the way cudaMalloc/cudaFree may; the serving loop, which
+// allocates while other simulations run, asks for them.
+cudaError_t DeviceSims::dev_alloc(void** p, size_t bytes) {
+    return stream_ordered_ ? cudaMallocAsync(p, bytes, stream_) : cudaMalloc(p, bytes);
+}
+void DeviceSims::dev_free(void* p) {
+    if (stream_ordered_) cudaFreeAsync(p, stream_);
+    else cudaFree(p);
+}
+
 DeviceSims::~DeviceSims() {
-    if (d_bar_) cudaFree(d_bar_);
-    if (arena_) cudaFree(arena_);
-    if (d_descs_) cudaFree(d_descs_);
-    if (d_plans_) cudaFree(d_plans_);
-    if (d_next_) cudaFree(d_next_);
+    for (void* p : {(void*)d_bar_, (void*)arena_, (void*)d_descs_, (void*)d_plans_, (void*)d_next_})
+        if (p) dev_free(p);
 }
 
 namespace {
@@ -166,9 +174,10 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
         t3 = device_table3d(err);
         if (!t3) return err;
     }
-    CUDA_TRY(cudaMalloc(&arena_, std::max<size_t>(cv.off, 256)));
-    CUDA_TRY(cudaMalloc(&d_descs_, std::max<size_t>(N, 1) * sizeof(SimDesc)));
-    CUDA_TRY(cudaMalloc(&d_next_, sizeof(int) * 16));
+    CUDA_TRY(dev_alloc((void**)&arena_, std::max<size_t>(cv.off, 256)));
+    CUDA_TRY(dev_alloc((void**)&d_descs_, std::max<size_t>(N, 1) * sizeof(SimDesc)));
+    CUDA_TRY(dev_alloc((void**)&d_next_, sizeof(int) * 16));
+    device_bytes_ = std::max<size_t>(cv.off, 256) + std::max<size_t>(N, 1) * sizeof(SimDesc) + sizeof(int) * 16;
     (void)t3;
     // ---- host staging, then one upload per buffer
     std::vector<char> stage(cv.off, 0);
@@ -372,8 +381,9 @@ std::string DeviceSims::run_tiled(const RunPlan& p, const uint64_t* t3) {
     // CPM_GPU_TILED_GRID caps the grid (several tiles per CTA); the tiling,
     // and so the trajectory, does not depend on it
     if (const char* cap = std::getenv("CPM_GPU_TILED_GRID")) grid = std::max(1, std::min(grid, std::atoi(cap)));
+    if (tiled_grid_cap_ > 0) grid = std::max(1, std::min(grid, tiled_grid_cap_));
     if ((tiles >> L.g.D) > 511 * grid) return "tiled sweep: too many tiles per CTA for this lattice";
-    if (!d_bar_) CUDA_TRY(cudaMalloc(&d_bar_, 64));
+    if (!d_bar_) CUDA_TRY(dev_alloc(&d_bar_, 64));
     SimDesc* d_sim = d_descs_ + p.sim;
     unsigned long long* claims = descs_[p.sim].slots;
     auto chunk = [&](uint64_t n) -> std::string {
@@ -436,9 +446,9 @@ std::string DeviceSims::run(const std::vector<RunPlan>& plans, int grid_override
     size_t total = 0;
     for (auto& kv : groups) total += kv.second.size();
     if (total > plans_cap_) {
-        if (d_plans_) cudaFree(d_plans_);
+        if (d_plans_) dev_free(d_plans_);
         d_plans_ = nullptr;
-        CUDA_TRY(cudaMalloc(&d_plans_, total * sizeof(RunPlan)));
+        CUDA_TRY(dev_alloc((void**)&d_plans_, total * sizeof(RunPlan)));
         plans_cap_ = total;
     }
     std::vector<RunPlan> flat;
@@ -514,6 +524,12 @@ std::string DeviceSims::read_cells(size_t i, std::vector<uint32_t>& vol, std::ve
     CUDA_TRY(cudaMemcpy(sp.data(), descs_[i].sum_pos, sp.size() * 8, cudaMemcpyDeviceToHost));
     d2h_bytes_ += so.size() * 8;
     CUDA_TRY(cudaMemcpy(so.data(), descs_[i].sum_outer, so.size() * 8, cudaMemcpyDeviceToHost));
+    return "";
+}
+
+std::string DeviceSims::set_desc(size_t i, const SimDesc& d) {
+    descs_[i] = d;
+    CUDA_TRY(cudaMemcpyAsync(d_descs_ + i, &descs_[i], sizeof(SimDesc), cudaMemcpyHostToDevice, stream_));
     return "";
 }
 
@@ -789,7 +805,7 @@ static Status status_of(const Config& c, const std::vector<double>& trace, const
 }
 
 // Number of energy-trace points the burn-in loop records (output.rs:441-454).
-static int trace_points(uint64_t burn_in, uint64_t interval, uint64_t start) {
+int trace_points(uint64_t burn_in, uint64_t interval, uint64_t start) {
     uint64_t burned = 0;
     int n = 0;
     while (burned < burn_in) {
@@ -799,7 +815,7 @@ static int trace_points(uint64_t burn_in, uint64_t interval, uint64_t start) {
     return n;
 }
 
-static RunPlan plan_for(const Config& c, int sim, bool write_lattice) {
+RunPlan plan_for(const Config& c, int sim, bool write_lattice) {
     RunPlan p;
     std::memset(&p, 0, sizeof p);
     p.sim = sim;
@@ -811,6 +827,72 @@ static RunPlan plan_for(const Config& c, int sim, bool write_lattice) {
     p.write_samples = 1;
     p.write_lattice = write_lattice ? 1 : 0;
     return p;
+}
+
+// Reads simulation i of `dev` back after its whole run window and builds
+// the run result (output.rs:434-529): samples with per-cell summaries and
+// topology readouts, the status, the metadata hashes and the counters.
+std::string assemble_result(const Config& c, const Initial& init, const DeviceSims& dev, size_t i, int ns, int nt,
+                            const ReadoutOptions& ro, Result& R) {
+    const bool snapshots = ro.include_lattice || ro.topology;
+    const SimLayout& L = dev.layout(i);
+    R = Result();
+    R.D = c.D;
+    for (int d = 0; d < c.D; ++d) R.grid.push_back(c.grid[d]);
+    R.used_default = init.used_default;
+    for (auto& t : c.types) R.cell_type_names.push_back(t.name);
+    R.cell_type_index = init.type_of;
+    std::vector<uint32_t> sv, si, slat;
+    std::vector<int64_t> ssp, sso;
+    std::vector<double> energy;
+    std::string e = dev.read_samples(i, ns, sv, si, ssp, sso, snapshots ? &slat : nullptr);
+    if (e.empty()) e = dev.read_energy(i, energy);
+    if (e.empty()) e = dev.read_stats(i, R.stats);
+    std::vector<uint32_t> fin;
+    if (e.empty()) e = dev.read_padded(i, fin);
+    if (!e.empty()) return e;
+    const int n = L.n_cells, D = c.D;
+    const size_t n1 = (size_t)n + 1;
+    std::vector<double> trace(energy.begin(), energy.begin() + nt);
+    R.samples.resize(ns);
+    for (int s = 0; s < ns; ++s) {
+        Sample& S = R.samples[s];
+        S.mcs = c.burn_in + (uint64_t)(s + 1) * c.interval;
+        S.energy = energy[nt + s];
+        S.cells.resize(n);
+        for (int id = 1; id <= n; ++id)
+            cell_summary(D, (uint32_t)id, sv[s * n1 + id], si[s * n1 + id], &ssp[(s * n1 + id) * D],
+                         &sso[(s * n1 + id) * D * D], S.cells[id - 1]);
+        if (snapshots) {
+            std::vector<uint32_t> interior(slat.begin() + (size_t)s * L.g.n_sites,
+                                           slat.begin() + (size_t)(s + 1) * L.g.n_sites);
+            if (ro.topology) topology_readouts(c, L.g, pad_lattice(L.g, interior), n, S);
+            if (ro.include_lattice) { S.lattice = std::move(interior); S.has_lattice = true; }
+        }
+    }
+    R.status = status_of(c, trace, R.samples, n, ro.topology);
+    // metadata (output.rs:66-78): hashes of the final state
+    std::vector<uint32_t> fin_int((size_t)L.g.n_sites);
+    int64_t x[3] = {0, 0, 0};
+    uint64_t occupied = 0;
+    for (int64_t q = 0; q < L.g.n_sites; ++q) {
+        fin_int[q] = fin[L.g.flat(x)];
+        for (int d = D - 1; d >= 0; --d) { if (++x[d] < L.g.dims[d]) break; x[d] = 0; }
+    }
+    std::vector<uint32_t> vol, itf;
+    std::vector<int64_t> sp, so;
+    e = dev.read_cells(i, vol, itf, sp, so);
+    if (!e.empty()) return e;
+    for (size_t id = 1; id < n1; ++id) occupied += vol[id];
+    R.metadata.cpm_version = "0.2.0+gb300";
+    R.metadata.convention_version = 1;
+    R.metadata.convention_hash = convention_hash(c);
+    R.metadata.model_hash = model_hash(c, fin_int, init.type_of);
+    R.metadata.seed = c.seed;
+    R.metadata.seed_policy = "independent";
+    R.metadata.derived_phi = (double)(uint32_t)occupied / (double)L.g.n_sites;
+    R.metadata.theta_layout_version = 1;
+    return "";
 }
 
 std::string run_many(const std::vector<Config>& configs, const std::vector<Initial>& initials, const ReadoutOptions& ro,
@@ -846,64 +928,7 @@ std::string run_many(const std::vector<Config>& configs, const std::vector<Initi
         for (;;) {
             const size_t i = next.fetch_add(1);
             if (i >= N) return;
-            const Config& c = configs[i];
-            const SimLayout& L = dev.layout(i);
-            Result& R = out[i];
-            R.D = c.D;
-            for (int d = 0; d < c.D; ++d) R.grid.push_back(c.grid[d]);
-            R.used_default = initials[i].used_default;
-            for (auto& t : c.types) R.cell_type_names.push_back(t.name);
-            R.cell_type_index = initials[i].type_of;
-            std::vector<uint32_t> sv, si, slat;
-            std::vector<int64_t> ssp, sso;
-            std::vector<double> energy;
-            std::string e = dev.read_samples(i, ns[i], sv, si, ssp, sso, snapshots ? &slat : nullptr);
-            if (e.empty()) e = dev.read_energy(i, energy);
-            if (e.empty()) e = dev.read_stats(i, R.stats);
-            std::vector<uint32_t> fin;
-            if (e.empty()) e = dev.read_padded(i, fin);
-            if (!e.empty()) { errs[i] = e; continue; }
-            const int n = L.n_cells, D = c.D;
-            const size_t n1 = (size_t)n + 1;
-            std::vector<double> trace(energy.begin(), energy.begin() + nt[i]);
-            R.samples.resize(ns[i]);
-            for (int s = 0; s < ns[i]; ++s) {
-                Sample& S = R.samples[s];
-                S.mcs = c.burn_in + (uint64_t)(s + 1) * c.interval;
-                S.energy = energy[nt[i] + s];
-                S.cells.resize(n);
-                for (int id = 1; id <= n; ++id)
-                    cell_summary(D, (uint32_t)id, sv[s * n1 + id], si[s * n1 + id], &ssp[(s * n1 + id) * D],
-                                 &sso[(s * n1 + id) * D * D], S.cells[id - 1]);
-                if (snapshots) {
-                    std::vector<uint32_t> interior(slat.begin() + (size_t)s * L.g.n_sites,
-                                                   slat.begin() + (size_t)(s + 1) * L.g.n_sites);
-                    if (ro.topology) topology_readouts(c, L.g, pad_lattice(L.g, interior), n, S);
-                    if (ro.include_lattice) { S.lattice = std::move(interior); S.has_lattice = true; }
-                }
-            }
-            R.status = status_of(c, trace, R.samples, n, ro.topology);
-            // metadata (output.rs:66-78): hashes of the final state
-            std::vector<uint32_t> fin_int((size_t)L.g.n_sites);
-            int64_t x[3] = {0, 0, 0};
-            uint64_t occupied = 0;
-            for (int64_t q = 0; q < L.g.n_sites; ++q) {
-                fin_int[q] = fin[L.g.flat(x)];
-                for (int d = D - 1; d >= 0; --d) { if (++x[d] < L.g.dims[d]) break; x[d] = 0; }
-            }
-            std::vector<uint32_t> vol, itf;
-            std::vector<int64_t> sp, so;
-            e = dev.read_cells(i, vol, itf, sp, so);
-            if (!e.empty()) { errs[i] = e; continue; }
-            for (size_t id = 1; id < n1; ++id) occupied += vol[id];
-            R.metadata.cpm_version = "0.2.0+gb300";
-            R.metadata.convention_version = 1;
-            R.metadata.convention_hash = convention_hash(c);
-            R.metadata.model_hash = model_hash(c, fin_int, initials[i].type_of);
-            R.metadata.seed = c.seed;
-            R.metadata.seed_policy = "independent";
-            R.metadata.derived_phi = (double)(uint32_t)occupied / (double)L.g.n_sites;
-            R.metadata.theta_layout_version = 1;
+            errs[i] = assemble_result(configs[i], initials[i], dev, i, ns[i], nt[i], ro, out[i]);
         }
     };
     (void)0;

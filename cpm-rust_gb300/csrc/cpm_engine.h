@@ -72,6 +72,17 @@ class DeviceSims {
     std::string write_state(size_t i, const std::vector<uint32_t>& padded, const std::vector<uint32_t>& vol,
                             const std::vector<uint32_t>& itf, const std::vector<int64_t>* sp = nullptr,
                             const std::vector<int64_t>* so = nullptr);
+    // Replaces the descriptor of simulation i (host copy and, asynchronously
+    // on the object's stream, the device copy): the serving loop points the
+    // output buffers at the slice of the run window a launch produces.
+    std::string set_desc(size_t i, const SimDesc& d);
+    // Device bytes this object allocated (arena, descriptors, plan table).
+    size_t device_bytes() const { return device_bytes_; }
+    // Before create(): allocate and free in stream order on the object's
+    // stream (which must then outlive the object).
+    void set_stream_ordered(bool on) { stream_ordered_ = on; }
+    // Caps the grid of tiled launches (the trajectory does not depend on it).
+    void set_tiled_grid_cap(int cap) { tiled_grid_cap_ = cap; }
 
    private:
     std::vector<SimLayout> layouts_;
@@ -90,7 +101,20 @@ class DeviceSims {
     std::string run_tiled(const RunPlan& p, const uint64_t* t3);
     uint64_t h2d_bytes_ = 0;
     mutable std::atomic<uint64_t> d2h_bytes_{0};
+    size_t device_bytes_ = 0;
+    bool stream_ordered_ = false;
+    int tiled_grid_cap_ = 0;
+    cudaError_t dev_alloc(void** p, size_t bytes);
+    void dev_free(void* p);
 };
+
+// The whole-window plan of a configuration (output.rs:441-468) and the
+// number of burn-in energy-trace points it records.
+RunPlan plan_for(const Config& c, int sim, bool write_lattice);
+int trace_points(uint64_t burn_in, uint64_t interval, uint64_t start);
+// Reads simulation i back after its run window and builds its result.
+std::string assemble_result(const Config& c, const Initial& init, const DeviceSims& dev, size_t i, int ns, int nt,
+                            const ReadoutOptions& ro, Result& R);
 
 // The 8 MiB 3D simple-point table of the current device (generated once).
 const uint64_t* device_table3d(std::string& err);

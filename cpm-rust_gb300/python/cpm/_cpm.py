@@ -163,6 +163,8 @@ EXPORTED_SYMBOLS = (
     "cpm_run_many",
     "cpm_builder_initial_state", "cpm_builder_hashes", "cpm_derive_seed_u64",
     "cpm_run_mcs_noalloc",
+    "cpm_serve_start", "cpm_serve_submit", "cpm_serve_poll", "cpm_serve_wait", "cpm_serve_cancel",
+    "cpm_serve_stats_get", "cpm_serve_stop",
 )
 
 
@@ -222,6 +224,13 @@ def _load():
     L.cpm_builder_hashes.argtypes = [_P, U64, U64, U64, _P, SZ, _P, SZ, ctypes.c_char_p, ctypes.c_char_p]
     L.cpm_derive_seed_u64.argtypes = [U64, U64]
     L.cpm_derive_seed_u64.restype = U64
+    L.cpm_serve_start.argtypes = [_P, ctypes.POINTER(_P)]
+    L.cpm_serve_submit.argtypes = [_P, _P, U64, U64, U64, I32, I32, ctypes.POINTER(U64)]
+    L.cpm_serve_poll.argtypes = [_P, U64, ctypes.POINTER(I32), ctypes.POINTER(_P), _P]
+    L.cpm_serve_wait.argtypes = [_P, U64, D, ctypes.POINTER(I32), ctypes.POINTER(_P), _P]
+    L.cpm_serve_cancel.argtypes = [_P, U64]
+    L.cpm_serve_stats_get.argtypes = [_P, _P]
+    L.cpm_serve_stop.argtypes = [_P]
     return L
 
 
@@ -635,3 +644,95 @@ class Engine:
         t = np.ascontiguousarray(target, dtype=np.int64)
         g = np.ascontiguousarray(gaining, dtype=np.uint32)
         _check(_lib.cpm_engine_commit_moves(self._h, i, t.size, _ptr(t), _ptr(g)))
+
+
+# ------------------------------------------------------------- serving ----
+class ServeOptionsC(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_active", ctypes.c_int32),
+                ("placement_threads", ctypes.c_int32), ("tiled_grid_cap", ctypes.c_int32), ("pad", ctypes.c_int32)]
+
+
+class RequestTimes(ctypes.Structure):
+    _fields_ = [("submitted_s", ctypes.c_double), ("admitted_s", ctypes.c_double), ("device_done_s", ctypes.c_double),
+                ("finished_s", ctypes.c_double), ("device_bytes", ctypes.c_uint64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ServeStatsC(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in ("submitted", "completed", "failed", "cancelled", "launched", "active",
+                                               "queued", "peak_active", "bytes_in_use", "peak_bytes")] + \
+               [("busy_seconds", ctypes.c_double)]
+
+
+REQ_STATES = ("placing", "queued", "running", "done", "failed", "cancelled")
+
+
+class Server:
+    """The serving loop (``cpm_serve_*``): submit simulations at any time;
+    they share the device by continuous batching and each result equals the
+    one ``CPM.run`` gives for the same builder and window."""
+
+    def __init__(self, hbm_budget_bytes=0, max_active=0, placement_threads=0, tiled_grid_cap=0):
+        o = ServeOptionsC(int(hbm_budget_bytes), int(max_active), int(placement_threads), int(tiled_grid_cap), 0)
+        h = _P()
+        self._h = None
+        _check(_lib.cpm_serve_start(ctypes.byref(o), ctypes.byref(h)))
+        self._h = h
+
+    def submit(self, builder, burn_in_mcs, readout_mcs, sampling_interval_mcs, include_lattice=False,
+               topology=True) -> int:
+        t = ctypes.c_uint64(0)
+        _check(_lib.cpm_serve_submit(self._h, builder.handle, _u64(burn_in_mcs, "burn_in_mcs"),
+                                     _u64(readout_mcs, "readout_mcs"),
+                                     _u64(sampling_interval_mcs, "sampling_interval_mcs"), int(bool(include_lattice)),
+                                     int(bool(topology)), ctypes.byref(t)))
+        return int(t.value)
+
+    def poll(self, ticket):
+        """(state, result or None, times): non-blocking; a done result is
+        handed over once."""
+        st = ctypes.c_int32(0)
+        out = _P()
+        tm = RequestTimes()
+        _check(_lib.cpm_serve_poll(self._h, int(ticket), ctypes.byref(st), ctypes.byref(out), ctypes.byref(tm)))
+        res = _result_from_handle(out) if out.value else None
+        return REQ_STATES[st.value], res, tm.as_dict()
+
+    def wait(self, ticket, timeout=None):
+        """(state, result or None, times) once the request has finished (or
+        the timeout, in seconds, passed)."""
+        st = ctypes.c_int32(0)
+        out = _P()
+        tm = RequestTimes()
+        _check(_lib.cpm_serve_wait(self._h, int(ticket), -1.0 if timeout is None else float(timeout),
+                                   ctypes.byref(st), ctypes.byref(out), ctypes.byref(tm)))
+        res = _result_from_handle(out) if out.value else None
+        return REQ_STATES[st.value], res, tm.as_dict()
+
+    def cancel(self, ticket):
+        _check(_lib.cpm_serve_cancel(self._h, int(ticket)))
+
+    def stats(self):
+        s = ServeStatsC()
+        _check(_lib.cpm_serve_stats_get(self._h, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in s._fields_}
+
+    def close(self):
+        if self._h:
+            h, self._h = self._h, None
+            _lib.cpm_serve_stop(h)
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+

@@ -122,3 +122,42 @@ def run_many(sims: list[CPM], burn_in_mcs: int, readout_mcs: int, sampling_inter
         warnings.warn(_BATCH, CPMInitializationWarning, stacklevel=2)
     return results
 
+
+class Server:
+    """A serving loop on the GPU: :meth:`submit` a configured :class:`CPM`
+    with its run window at any time and collect the result with
+    :meth:`wait` or :meth:`poll`. Simulations share the device by continuous
+    batching (admitted as slots and ``hbm_budget_bytes`` allow, run side by
+    side with their lattices resident until read back, freed when done);
+    each result equals :meth:`CPM.run` for the same simulation (an
+    extension: the reference has no serving API)."""
+
+    def __init__(self, hbm_budget_bytes: int = 0, max_active: int = 0, placement_threads: int = 0,
+                 tiled_grid_cap: int = 0) -> None:
+        self._s = _cpm.Server(hbm_budget_bytes, max_active, placement_threads, tiled_grid_cap)
+
+    def submit(self, sim: CPM, burn_in_mcs: int, readout_mcs: int, sampling_interval_mcs: int,
+               include_lattice: bool = False, topology: bool = True) -> int:
+        return self._s.submit(sim._raw, burn_in_mcs, readout_mcs, sampling_interval_mcs, include_lattice, topology)
+
+    def poll(self, ticket: int):
+        return self._s.poll(ticket)
+
+    def wait(self, ticket: int, timeout: float | None = None):
+        return self._s.wait(ticket, timeout)
+
+    def cancel(self, ticket: int) -> None:
+        self._s.cancel(ticket)
+
+    def stats(self) -> dict:
+        return self._s.stats()
+
+    def close(self) -> None:
+        self._s.close()
+
+    def __enter__(self) -> "Server":
+        return self
+
+    def __exit__(self, *exc) -> None:
+        self.close()
+

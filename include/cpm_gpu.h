@@ -288,10 +288,67 @@ typedef struct {
     const double* lambda_interface;
     const uint32_t* target_volume;
     const uint32_t* target_interface;
-    uint64_t* stats;              /* optional: 16 device counters accumulated by the sweep */
+    uint64_t* stats;              /* optional: 32 device counters (the cpm_engine_stats layout) accumulated by the sweep */
 } cpm_device_sim;
 
 int cpm_run_mcs_noalloc(cpm_device_sim* sim, uint64_t n_mcs, void* stream);
+
+/* ------------------------------------------------------------ serving ---
+ * A device-resident request loop (no counterpart in the reference, whose
+ * unit of work is one blocking `run` or `run_batch` call): simulations are
+ * submitted at any time, admitted in submission order while the active ones
+ * fit `max_active` slots and the HBM budget, run side by side on the device
+ * (each on its own stream with its whole run window enqueued; lattices stay
+ * on the device from upload to read-back), and read out and freed when
+ * their windows end, which admits the next. Each result equals what
+ * `cpm_builder_run` returns for the same builder and window, alone or in
+ * any mix. All functions are thread-safe. */
+typedef struct cpm_server cpm_server;
+
+typedef struct {
+    uint64_t hbm_budget_bytes;  /* device bytes admitted simulations may hold; 0 = 150 GiB */
+    int32_t max_active;         /* simulations on the device at once; 0 = 128 */
+    int32_t placement_threads;  /* host threads for placements and read-backs; 0 = automatic */
+    int32_t tiled_grid_cap;     /* CTAs of one simulation on the tiled sweep; 0 = 64 */
+    int32_t pad;
+} cpm_serve_options;
+
+#define CPM_REQ_PLACING 0
+#define CPM_REQ_QUEUED 1
+#define CPM_REQ_RUNNING 2
+#define CPM_REQ_DONE 3
+#define CPM_REQ_FAILED 4
+#define CPM_REQ_CANCELLED 5
+
+typedef struct {
+    double submitted_s, admitted_s, device_done_s, finished_s; /* seconds since the server started */
+    uint64_t device_bytes;                                     /* device bytes it held */
+} cpm_request_times;
+
+typedef struct {
+    uint64_t submitted, completed, failed, cancelled, launched;
+    uint64_t active, queued, peak_active;
+    uint64_t bytes_in_use, peak_bytes;
+    double busy_seconds;                        /* wall time with simulations on the device */
+} cpm_serve_stats;
+
+int cpm_serve_start(const cpm_serve_options* options, cpm_server** out);
+/* Validates the builder's configuration with the window (as cpm_builder_run
+ * does) and enqueues it; the ticket names the request from then on. */
+int cpm_serve_submit(cpm_server* s, const cpm_builder* b, uint64_t burn_in_mcs, uint64_t readout_mcs,
+                     uint64_t sampling_interval_mcs, int32_t include_lattice, int32_t topology, uint64_t* ticket);
+/* Non-blocking. state receives CPM_REQ_*; when it is CPM_REQ_DONE and out is
+ * not NULL, *out receives the result (free with cpm_result_free) and the
+ * ticket is retired. A failed request returns its error code and message. */
+int cpm_serve_poll(cpm_server* s, uint64_t ticket, int32_t* state, cpm_result** out, cpm_request_times* times);
+/* Blocks until the request finishes or timeout_s passes (negative: no
+ * limit); then as cpm_serve_poll with out. */
+int cpm_serve_wait(cpm_server* s, uint64_t ticket, double timeout_s, int32_t* state, cpm_result** out,
+                   cpm_request_times* times);
+int cpm_serve_cancel(cpm_server* s, uint64_t ticket);
+int cpm_serve_stats_get(cpm_server* s, cpm_serve_stats* out);
+/* Cancels unfinished requests, stops the loop and frees the server. */
+int cpm_serve_stop(cpm_server* s);
 
 #ifdef __cplusplus
 }

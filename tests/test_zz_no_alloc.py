@@ -85,7 +85,7 @@ def test_noalloc_sweep_matches_engine_on_two_calls(cuda_required):
     lam_i = dev(np.array([t[4] for t in model.types], np.float64))
     tv = dev(np.array([t[1] for t in model.types], np.int32))
     ti = dev(np.array([t[2] for t in model.types], np.int32))
-    stats = torch.zeros(16, dtype=torch.int64, device="cuda")
+    stats = torch.zeros(32, dtype=torch.int64, device="cuda")  # CPM_STAT_COUNT counters
     torch.cuda.synchronize()
 
     ds = DeviceSim()
