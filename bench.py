@@ -324,6 +324,9 @@ def run_serve_bench(args):
         "wall_s": wall,
         "peak_active": stats["peak_active"],
         "peak_device_bytes": stats["peak_bytes"],
+        "requests": [[q["D"], q["side"], q["burn"] + q["readout"], round(a, 3), round(m, 3)]
+                     for q, a, m in zip(reqs, alone, lat)],
+        "requests_columns": ["D", "side", "MCS", "isolated_s", "in_stream_s"],
     }
 
 

@@ -888,6 +888,9 @@ bool tiled_plan(int D, const int* dims, int periodic, int* nt, int* max_box) {
         if (periodic && (L & 1)) return false;  // odd periodic axes need a third site colour
         int n = L / target;
         if (n & 1) n -= 1;
+        // small 3D lattices: 4 tiles per axis (8 per colour) while tiles
+        // stay at least 10 sites wide, rather than one tile per colour
+        if (D == 3 && n < 4 && L >= 40) n = 4;
         if (n < 2) return false;
         nt[d] = n;
         const int tmax = (L + n - 1) / n;
