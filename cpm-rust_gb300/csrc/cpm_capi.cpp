@@ -207,6 +207,7 @@ static int check_supported(const Config& c) {
 
 static int code_for(const std::string& e) {
     if (e.rfind("CUDA error", 0) == 0) return CPM_E_CUDA;
+    if (e.find("timed out") != std::string::npos) return CPM_E_TIMEOUT;
     return CPM_E_INIT;
 }
 
@@ -534,7 +535,7 @@ extern "C" int cpm_engine_run_mcs(cpm_engine* e, uint64_t n) {
 extern "C" int cpm_engine_synchronize(cpm_engine* e) {
     if (!e) return fail(CPM_E_ARG, "null argument");
     const std::string msg = e->sims.sync();
-    if (!msg.empty()) return fail(CPM_E_CUDA, msg);
+    if (!msg.empty()) return fail(code_for(msg) == CPM_E_TIMEOUT ? CPM_E_TIMEOUT : CPM_E_CUDA, msg);
     return ok();
 }
 

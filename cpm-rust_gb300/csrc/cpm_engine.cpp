@@ -383,6 +383,10 @@ std::string DeviceSims::run_tiled(const RunPlan& p, const uint64_t* t3) {
     if (const char* cap = std::getenv("CPM_GPU_TILED_GRID")) grid = std::max(1, std::min(grid, std::atoi(cap)));
     if (tiled_grid_cap_ > 0) grid = std::max(1, std::min(grid, tiled_grid_cap_));
     if ((tiles >> L.g.D) > 511 * grid) return "tiled sweep: too many tiles per CTA for this lattice";
+    // CPM_GPU_TEST_BARRIER_TIMEOUT (tests only): the grid barrier waits for
+    // one CTA more than the grid has, so every bounded wait runs out, the
+    // kernel records the timeout and returns; nothing else changes
+    const int barrier_extra = std::getenv("CPM_GPU_TEST_BARRIER_TIMEOUT") ? 1 : 0;
     if (!d_bar_) CUDA_TRY(dev_alloc(&d_bar_, 64));
     SimDesc* d_sim = d_descs_ + p.sim;
     unsigned long long* claims = descs_[p.sim].slots;
@@ -392,8 +396,8 @@ std::string DeviceSims::run_tiled(const RunPlan& p, const uint64_t* t3) {
         while (n > 0) {
             const uint64_t m = std::min<uint64_t>(n, 1ull << 18);
             CUDA_TRY(cudaMemsetAsync(d_bar_, 0, 64, stream_));
-            CUDA_TRY(cpmgpu::launch_tiled(L.g.D, L.NE, d_sim, m, nt, d_bar_, claims, t3, max_box, tables_in_smem, smem,
-                                          grid, stream_));
+            CUDA_TRY(cpmgpu::launch_tiled(L.g.D, L.NE, d_sim, m, nt, d_bar_, claims, t3, max_box, tables_in_smem,
+                                          barrier_extra, smem, grid, stream_));
             n -= m;
         }
         return "";
@@ -499,7 +503,7 @@ std::string DeviceSims::sync() {
     for (size_t i : tiled_ran_) {
         int32_t err = 0;
         CUDA_TRY(cudaMemcpy(&err, descs_[i].error, 4, cudaMemcpyDeviceToHost));
-        if (err) return "CUDA error: device wait timed out in the tiled sweep (error " + std::to_string(err) + ")";
+        if (err) return "device wait timed out in the tiled sweep (error " + std::to_string(err) + ")";
     }
     tiled_ran_.clear();
     return "";

@@ -180,28 +180,37 @@ struct Placer {
         }
         return std::sqrt(s);
     }
-    bool connected(uint32_t id) const {
-        std::vector<int64_t> sites;
+    // Size of the connected component (connectivity is von Neumann) holding
+    // each cell's first site in scan order, for all cells in one pass over
+    // the lattice; a cell is connected when that size equals its volume.
+    std::vector<uint64_t> first_component_sizes(size_t n) const {
+        std::vector<int64_t> first(n + 1, -1);
         int64_t x[3] = {0, 0, 0};
         for (int64_t i = 0; i < g.n_sites; ++i) {
             const int64_t f = g.flat(x);
-            if (lat[f] == id) sites.push_back(f);
+            const uint32_t id = lat[f];
+            if (id && id <= n && first[id] < 0) first[id] = f;
             for (int d = g.D - 1; d >= 0; --d) { if (++x[d] < g.dims[d]) break; x[d] = 0; }
         }
-        if (sites.empty()) return false;
+        std::vector<uint64_t> size(n + 1, 0);
         std::vector<char> vis(lat.size(), 0);
-        std::vector<int64_t> st{sites[0]};
-        vis[sites[0]] = 1;
-        size_t n = 1;
-        while (!st.empty()) {
-            const int64_t f = st.back();
-            st.pop_back();
-            for (int64_t off : copy_off) {  // connectivity is von Neumann
-                const int64_t nb = canonical(f, off);
-                if (lat[nb] == id && !vis[nb]) { vis[nb] = 1; ++n; st.push_back(nb); }
+        std::vector<int64_t> st;
+        for (size_t id = 1; id <= n; ++id) {
+            if (first[id] < 0) continue;
+            st.assign(1, first[id]);
+            vis[first[id]] = 1;
+            uint64_t c = 1;
+            while (!st.empty()) {
+                const int64_t f = st.back();
+                st.pop_back();
+                for (int64_t off : copy_off) {
+                    const int64_t nb = canonical(f, off);
+                    if (lat[nb] == id && !vis[nb]) { vis[nb] = 1; ++c; st.push_back(nb); }
+                }
             }
+            size[id] = c;
         }
-        return n == sites.size();
+        return size;
     }
     std::vector<uint32_t> interior_copy() const {
         std::vector<uint32_t> out((size_t)g.n_sites);
@@ -243,8 +252,9 @@ std::string initialize(const Config& c, Initial& out) {
         }
         for (size_t i = 0; i < n; ++i)
             if (vol[i] == 0) return "cell " + std::to_string(i + 1) + " has zero volume in the supplied lattice";
+        const std::vector<uint64_t> comp = P.first_component_sizes(n);
         for (size_t id = 1; id <= n; ++id)
-            if (!P.connected((uint32_t)id))
+            if (comp[id] != vol[id - 1])
                 return "cell " + std::to_string(id) +
                        " is not connected under connectivity_neighborhood — every explicitly-placed cell must already be connected";
         out.lattice = c.init_lattice;

@@ -35,7 +35,7 @@ int tiled_block();
 cudaError_t tiled_occupancy(int D, int NE, size_t smem, int* per_sm);
 cudaError_t launch_tiled(int D, int NE, SimDesc* d_sim, uint64_t n_mcs, const int* nt, void* d_barrier,
                          unsigned long long* d_claims, const uint64_t* d_t3, int max_box, int tables_in_smem,
-                         size_t smem, int grid, cudaStream_t st);
+                         int barrier_extra, size_t smem, int grid, cudaStream_t st);
 // Copies one sample (V, I, position sums, optional lattice) of simulation d_sim.
 cudaError_t launch_sample(int D, const SimDesc* d_sim, int sample, int write_lattice, int64_t n_sites, cudaStream_t st);
 }  // namespace cpmgpu

@@ -478,7 +478,7 @@ size_t tiled_table_bytes(int n_types, int tab_n) {
 template <int D, int NE>
 __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_mcs, TileGrid tg_in, BarrierState* bar,
                                                    unsigned long long* claims, const uint64_t* t3, int max_box,
-                                                   int tables_in_smem) {
+                                                   int tables_in_smem, int barrier_extra) {
     extern __shared__ __align__(16) unsigned char sm[];
     __shared__ SimDesc gsd, lsd;
     __shared__ int s_n, s_tile, s_ncell, s_box_dims[3], s_gx0[3], s_tcnt[3];
@@ -514,6 +514,7 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
     }
     const SimDesc& g = gsd;
     const int nblk = gridDim.x;
+    const unsigned int arrivals = (unsigned int)(nblk + barrier_extra);  // barrier_extra: timeout test hook
     {
         uint32_t* seen0 = (uint32_t*)(sm + tile_shared(max_box, g.n_cells).seen);
         for (int id = tid; id <= g.n_cells; id += TB) seen0[id] = 0u;
@@ -693,7 +694,7 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                 }
             }
             const long long t_c1 = clock64();
-            if (!grid_sync(bar, nblk, bar_epoch)) { alive = false; break; }
+            if (!grid_sync(bar, arrivals, bar_epoch)) { alive = false; break; }
             const long long t_c2 = clock64();
             cyc_sync += t_c2 - t_c0;
             cyc_claim += t_c1 - t_c0;
@@ -831,7 +832,7 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                 cyc_stage += clock64() - t_w0;
             }
             long long t_b0 = clock64();
-            if (!grid_sync(bar, nblk, bar_epoch)) { alive = false; break; }
+            if (!grid_sync(bar, arrivals, bar_epoch)) { alive = false; break; }
             cyc_sync += clock64() - t_b0;
             cyc_bar2 += clock64() - t_b0;
         }
@@ -882,7 +883,9 @@ static int tiled_index(int D, int NE) {
 
 bool tiled_plan(int D, const int* dims, int periodic, int* nt, int* max_box) {
     int box = 1, klass = 1;
-    const int target = D == 2 ? 21 : 16;
+    // target tile widths: 21 in 2D (cells of ~50 sites are ~8 wide), 12 in
+    // 3D (more tiles per colour: 8 colours there)
+    const int target = D == 2 ? 21 : 12;
     for (int d = 0; d < D; ++d) {
         const int L = dims[d];
         if (periodic && (L & 1)) return false;  // odd periodic axes need a third site colour
@@ -926,7 +929,7 @@ cudaError_t tiled_occupancy(int D, int NE, size_t smem, int* per_sm) {
 
 cudaError_t launch_tiled(int D, int NE, SimDesc* d_sim, uint64_t n_mcs, const int* nt, void* d_barrier,
                          unsigned long long* d_claims, const uint64_t* d_t3, int max_box, int tables_in_smem,
-                         size_t smem, int grid, cudaStream_t st) {
+                         int barrier_extra, size_t smem, int grid, cudaStream_t st) {
     TileGrid tg;
     for (int d = 0; d < 3; ++d) { tg.nt[d] = d < D ? nt[d] : 1; tg.off[d] = 0; }
     tg.colors = 1 << D;
@@ -937,7 +940,7 @@ cudaError_t launch_tiled(int D, int NE, SimDesc* d_sim, uint64_t n_mcs, const in
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);      \
         if (e != cudaSuccess) return e;                                                                     \
         void* args[] = {(void*)&d_sim, (void*)&n_mcs, (void*)&tg, (void*)&bar, (void*)&d_claims, (void*)&d_t3, \
-                        (void*)&max_box, (void*)&tables_in_smem};                                           \
+                        (void*)&max_box, (void*)&tables_in_smem, (void*)&barrier_extra};                    \
         return cudaLaunchCooperativeKernel((const void*)k, dim3(grid), dim3(TB), args, smem, st);            \
     }
     switch (tiled_index(D, NE)) {

@@ -371,3 +371,26 @@ def test_tiled_sweep_independent_of_grid(D, cuda_required, monkeypatch):
     assert ok
     assert np.array_equal(wide.cells()[2], narrow.cells()[2])
 
+
+
+def test_tiled_barrier_timeout_is_reported_and_the_context_survives(cuda_required, monkeypatch):
+    """The grid barrier's bounded wait: with a barrier that waits for one CTA
+    more than the grid has (test hook), every CTA gives up after its time
+    limit, the kernel records the timeout and returns, the host reports
+    CPM_E_TIMEOUT, and the next launch on the same context runs normally."""
+    from cpm import _cpm
+
+    monkeypatch.setenv("CPM_GPU_FORCE_TILED", "1")
+    model = sorting_model(side=64, seed=12)
+    monkeypatch.setenv("CPM_GPU_TEST_BARRIER_TIMEOUT", "1")
+    bad = _engine(model)
+    bad.run_mcs(1)
+    with pytest.raises(_cpm.CPMRuntimeError, match="timed out"):
+        bad.synchronize()
+    assert bad.stats()["spin_timeouts"] >= 1
+    monkeypatch.delenv("CPM_GPU_TEST_BARRIER_TIMEOUT")
+    good = _engine(model)
+    good.run_mcs(5)
+    good.synchronize()
+    assert good.stats()["spin_timeouts"] == 0
+    assert good.recount_check()[0]
