@@ -346,7 +346,7 @@ DeviceSims::Path DeviceSims::path(size_t i) const {
     if (L.n_cells >= 65535) return GLOBAL;
     int dims[3] = {(int)L.g.dims[0], (int)L.g.dims[1], (int)L.g.dims[2]}, nt[3] = {1, 1, 1}, max_box = 0;
     const bool tiled_ok = cpmgpu::tiled_plan(L.g.D, dims, L.g.periodic, nt, &max_box) &&
-                          cpmgpu::tiled_smem_bytes(max_box, L.n_cells) <= cpmgpu::resident_smem_limit();
+                          cpmgpu::tiled_smem_bytes(max_box, L.n_cells, 0, L.g.D) <= cpmgpu::resident_smem_limit();
     if (!force_tiled_ && cpmgpu::resident_smem_bytes(L.g.n_padded, L.n_cells) <= cpmgpu::resident_smem_limit()) {
         // The path is a function of the simulation's own configuration, so a
         // simulation's trajectory is the same alone and inside any batch.
@@ -366,8 +366,12 @@ std::string DeviceSims::run_tiled(const RunPlan& p, const uint64_t* t3) {
     const SimLayout& L = layouts_[p.sim];
     int dims[3] = {(int)L.g.dims[0], (int)L.g.dims[1], (int)L.g.dims[2]}, nt[3], max_box = 0;
     cpmgpu::tiled_plan(L.g.D, dims, L.g.periodic, nt, &max_box);
-    size_t smem = cpmgpu::tiled_smem_bytes(max_box, L.n_cells);
-    // the energy tables go to shared memory when they fit beside the tile state
+    // position sums of up to 1024 listed cells per box in shared memory (as
+    // many as fit), then the energy tables if they fit beside the tile state
+    int cl_cap = (int)std::min<int64_t>(std::min<int64_t>(max_box, L.n_cells), 1024);
+    while (cl_cap > 0 && cpmgpu::tiled_smem_bytes(max_box, L.n_cells, cl_cap, L.g.D) > cpmgpu::resident_smem_limit())
+        cl_cap /= 2;
+    size_t smem = cpmgpu::tiled_smem_bytes(max_box, L.n_cells, cl_cap, L.g.D);
     const size_t tab = cpmgpu::tiled_table_bytes(descs_[p.sim].n_types, descs_[p.sim].tab_n);
     const int tables_in_smem = smem + tab <= cpmgpu::resident_smem_limit();
     if (tables_in_smem) smem += tab;
@@ -397,7 +401,7 @@ std::string DeviceSims::run_tiled(const RunPlan& p, const uint64_t* t3) {
             const uint64_t m = std::min<uint64_t>(n, 1ull << 18);
             CUDA_TRY(cudaMemsetAsync(d_bar_, 0, 64, stream_));
             CUDA_TRY(cpmgpu::launch_tiled(L.g.D, L.NE, d_sim, m, nt, d_bar_, claims, t3, max_box, tables_in_smem,
-                                          barrier_extra, smem, grid, stream_));
+                                          barrier_extra, cl_cap, smem, grid, stream_));
             n -= m;
         }
         return "";

@@ -29,13 +29,13 @@ cudaError_t launch_resident(int D, int NE, SimDesc* d_sims, const RunPlan* d_pla
 cudaError_t resident_occupancy(int D, int NE, size_t smem, int* blocks_per_sm);
 // Tiled cooperative sweep for large lattices (cpm_tiled.cu).
 bool tiled_plan(int D, const int* dims, int periodic, int* nt, int* max_box);
-size_t tiled_smem_bytes(int max_box, int n_cells);
+size_t tiled_smem_bytes(int max_box, int n_cells, int cl_cap, int D);
 size_t tiled_table_bytes(int n_types, int tab_n);
 int tiled_block();
 cudaError_t tiled_occupancy(int D, int NE, size_t smem, int* per_sm);
 cudaError_t launch_tiled(int D, int NE, SimDesc* d_sim, uint64_t n_mcs, const int* nt, void* d_barrier,
                          unsigned long long* d_claims, const uint64_t* d_t3, int max_box, int tables_in_smem,
-                         int barrier_extra, size_t smem, int grid, cudaStream_t st);
+                         int barrier_extra, int cl_cap, size_t smem, int grid, cudaStream_t st);
 // Copies one sample (V, I, position sums, optional lattice) of simulation d_sim.
 cudaError_t launch_sample(int D, const SimDesc* d_sim, int sample, int write_lattice, int64_t n_sites, cudaStream_t st);
 }  // namespace cpmgpu

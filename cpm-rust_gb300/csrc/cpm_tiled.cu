@@ -112,6 +112,15 @@ struct TileCounters {
     unsigned long long c_build, c_eval, c_fix, c_apply, c_lower;
 };
 
+// The attempt's draw with its top word taken from the per-site table staged
+// with the box; the full 53-bit u (FP64 fallback only) is recomputed.
+struct TileDraw {
+    uint64_t seed, mcs;
+    uint32_t site, zv;
+    __device__ double u() const { return u53(site_draw(seed, mcs, site)); }
+    __device__ uint32_t z() const { return zv; }
+};
+
 template <int D, int NE>
 struct TileProc {
     const SimDesc& g;     // global descriptor
@@ -121,10 +130,32 @@ struct TileProc {
     uint32_t *vol, *itf, *b0, *b1;
     uint16_t* adh;
     uint8_t *dirty, *own, *mod;
-    uint32_t *c_site, *c_key, *c_cells, *c_flags, *c_gf;
+    uint32_t *c_site, *c_key, *c_cells, *c_flags, *c_gf, *c_z;
     int16_t* c_dl;
     const uint64_t* t3;
     int* s_n;
+    // position sums of the first cl_cap listed cells, staged in shared
+    // memory (slot[id] < cl_cap); other cells use HBM through L2
+    uint16_t* slot;
+    long long *ssp, *sso;
+    int cl_cap;
+
+    __device__ __forceinline__ bool sums_of(uint32_t id, long long*& sp, long long*& so) const {
+        const uint32_t k = slot[id];
+        if ((int)k < cl_cap) {
+            sp = ssp + (long long)k * D;
+            so = sso + (long long)k * D * D;
+            return true;
+        }
+        sp = (long long*)g.sum_pos + (long long)id * D;
+        so = (long long*)g.sum_outer + (long long)id * D * D;
+        return false;
+    }
+    static __device__ __forceinline__ long long ld_sum(const long long* p, bool shared) { return shared ? *p : __ldcg(p); }
+    static __device__ __forceinline__ void st_sum(long long* p, long long v, bool shared) {
+        if (shared) *p = v;
+        else __stcg(p, v);
+    }
 
     __device__ int gcoord(int d, int local) const {  // box position -> global interior coordinate
         int x = gx0[d] + local - 1;
@@ -153,7 +184,7 @@ struct TileProc {
             fl |= T_GUARD;
         } else {
             int dl = 0, dg = 0;
-            if (decide_move<NE, uint16_t>(l, sig, adh, vol, itf, t, L, G, PhiloxDraw{g.seed, mcs, c_gf[c]}, dl, dg)) fl |= T_ACC;
+            if (decide_move<NE, uint16_t>(l, sig, adh, vol, itf, t, L, G, TileDraw{g.seed, mcs, c_gf[c], c_z[c]}, dl, dg)) fl |= T_ACC;
             c_dl[c] = (int16_t)((dl & 0xFF) | ((dg & 0xFF) << 8));
         }
         c_flags[c] = fl;
@@ -173,14 +204,15 @@ struct TileProc {
         if (L) {
             vol[L] -= 1;
             itf[L] += (uint32_t)dl;
-            long long* sp = (long long*)g.sum_pos + (long long)L * D;
-            long long* so = (long long*)g.sum_outer + (long long)L * D * D;
+            long long *sp, *so;
+            const bool sh = sums_of(L, sp, so);
 #pragma unroll
-            for (int d = 0; d < D; ++d) __stcg(sp + d, __ldcg(sp + d) - xg[d]);
+            for (int d = 0; d < D; ++d) st_sum(sp + d, ld_sum(sp + d, sh) - xg[d], sh);
 #pragma unroll
             for (int d = 0; d < D; ++d)
 #pragma unroll
-                for (int e = 0; e < D; ++e) __stcg(so + d * D + e, __ldcg(so + d * D + e) - (long long)xg[d] * xg[e]);
+                for (int e = 0; e < D; ++e)
+                    st_sum(so + d * D + e, ld_sum(so + d * D + e, sh) - (long long)xg[d] * xg[e], sh);
             if (mark) dirty[L] = 1;
             mod[L] = 1;
         }
@@ -190,17 +222,19 @@ struct TileProc {
             itf[G] += (uint32_t)dg;
             uint32_t vb = vnew >= 1 ? vnew - 1 : 0;
             if (vb < 1) vb = 1;
-            long long* sp = (long long*)g.sum_pos + (long long)G * D;
-            long long* so = (long long*)g.sum_outer + (long long)G * D * D;
-            long long img[3];
+            long long *sp, *so;
+            const bool sh = sums_of(G, sp, so);
+            long long img[3], cur[3];
 #pragma unroll
-            for (int d = 0; d < D; ++d) img[d] = nearest_image_exact(xg[d], __ldcg(sp + d), vb, g.dims[d], g.periodic != 0);
+            for (int d = 0; d < D; ++d) cur[d] = ld_sum(sp + d, sh);
 #pragma unroll
-            for (int d = 0; d < D; ++d) __stcg(sp + d, __ldcg(sp + d) + img[d]);
+            for (int d = 0; d < D; ++d) img[d] = nearest_image_exact(xg[d], cur[d], vb, g.dims[d], g.periodic != 0);
+#pragma unroll
+            for (int d = 0; d < D; ++d) st_sum(sp + d, cur[d] + img[d], sh);
 #pragma unroll
             for (int d = 0; d < D; ++d)
 #pragma unroll
-                for (int e = 0; e < D; ++e) __stcg(so + d * D + e, __ldcg(so + d * D + e) + img[d] * img[e]);
+                for (int e = 0; e < D; ++e) st_sum(so + d * D + e, ld_sum(so + d * D + e, sh) + img[d] * img[e], sh);
             if (mark) dirty[G] = 1;
             mod[G] = 1;
         }
@@ -435,7 +469,8 @@ struct TileProc {
 };
 
 struct TileShared {
-    uint32_t sig, vol, itf, b0, b1, adh, dirty, own, mod, seen, clist, c_site, c_key, c_cells, c_flags, c_gf, c_dl, total;
+    uint32_t sig, skd, sgf, sz, vol, itf, b0, b1, adh, dirty, own, mod, seen, clist, slot, ssp, sso, c_site, c_key, c_cells,
+        c_flags, c_gf, c_z, c_dl, total;
 };
 
 __host__ __device__ inline uint32_t tl_take(uint32_t& off, uint64_t b) {
@@ -443,11 +478,14 @@ __host__ __device__ inline uint32_t tl_take(uint32_t& off, uint64_t b) {
     off = (uint32_t)((off + b + 15) & ~(uint64_t)15);
     return o;
 }
-__host__ __device__ inline TileShared tile_shared(int box_sites, int n_cells) {
+__host__ __device__ inline TileShared tile_shared(int box_sites, int n_cells, int cl_cap, int D) {
     TileShared s;
     uint32_t off = 0;
     const uint64_t n1 = (uint64_t)n_cells + 1;
     s.sig = tl_take(off, (uint64_t)box_sites * 2);
+    s.skd = tl_take(off, (uint64_t)box_sites);      // copy direction of each tile site's attempt
+    s.sgf = tl_take(off, (uint64_t)box_sites * 4);  // its global flat index (the draw's counter)
+    s.sz = tl_take(off, (uint64_t)box_sites * 4);   // the top word of its uniform
     s.vol = tl_take(off, n1 * 4);
     s.itf = tl_take(off, n1 * 4);
     s.b0 = tl_take(off, n1 * 4);
@@ -458,11 +496,15 @@ __host__ __device__ inline TileShared tile_shared(int box_sites, int n_cells) {
     s.mod = tl_take(off, n1);
     s.seen = tl_take(off, n1 * 4);
     s.clist = tl_take(off, (uint64_t)(box_sites < n_cells ? box_sites : n_cells) * 4);
+    s.slot = tl_take(off, n1 * 2);
+    s.ssp = tl_take(off, (uint64_t)cl_cap * D * 8);
+    s.sso = tl_take(off, (uint64_t)cl_cap * D * D * 8);
     s.c_site = tl_take(off, TCMAX * 4);
     s.c_key = tl_take(off, TCMAX * 4);
     s.c_cells = tl_take(off, TCMAX * 4);
     s.c_flags = tl_take(off, TCMAX * 4);
     s.c_gf = tl_take(off, TCMAX * 4);
+    s.c_z = tl_take(off, TCMAX * 4);
     s.c_dl = tl_take(off, TCMAX * 2);
     s.total = off;
     return s;
@@ -478,11 +520,12 @@ size_t tiled_table_bytes(int n_types, int tab_n) {
 template <int D, int NE>
 __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_mcs, TileGrid tg_in, BarrierState* bar,
                                                    unsigned long long* claims, const uint64_t* t3, int max_box,
-                                                   int tables_in_smem, int barrier_extra) {
+                                                   int tables_in_smem, int barrier_extra, int cl_cap) {
     extern __shared__ __align__(16) unsigned char sm[];
     __shared__ SimDesc gsd, lsd;
     __shared__ int s_n, s_tile, s_ncell, s_box_dims[3], s_gx0[3], s_tcnt[3];
     __shared__ int perm[8], sperm[27];
+    __shared__ uint32_t s_pkey[8];
     __shared__ unsigned long long sstat[8];
     const int tid = threadIdx.x;
     if (tid == 0) gsd = *simp;
@@ -491,7 +534,7 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
     if (tables_in_smem && gsd.dj32 != nullptr) {
         // the float energy tables move next to the tile state (no global
         // loads in the common-case decision)
-        float* tb = (float*)(sm + tile_shared(max_box, gsd.n_cells).total);
+        float* tb = (float*)(sm + tile_shared(max_box, gsd.n_cells, cl_cap, D).total);
         const int n1 = gsd.n_types + 1, nj = n1 * n1, nd = n1 * n1 * n1, nv = gsd.n_types * gsd.tab_n;
         for (int q = tid; q < nj; q += TB) tb[q] = gsd.J32[q];
         for (int q = tid; q < nd; q += TB) tb[nj + q] = gsd.dj32[q];
@@ -512,11 +555,14 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
         }
         __syncthreads();
     }
+    // the box descriptor: gsd's parameters, box geometry set per tile
+    for (int q = tid; q < (int)(sizeof(SimDesc) / 8); q += TB) ((uint64_t*)&lsd)[q] = ((const uint64_t*)&gsd)[q];
+    __syncthreads();
     const SimDesc& g = gsd;
     const int nblk = gridDim.x;
     const unsigned int arrivals = (unsigned int)(nblk + barrier_extra);  // barrier_extra: timeout test hook
     {
-        uint32_t* seen0 = (uint32_t*)(sm + tile_shared(max_box, g.n_cells).seen);
+        uint32_t* seen0 = (uint32_t*)(sm + tile_shared(max_box, g.n_cells, cl_cap, D).seen);
         for (int id = tid; id <= g.n_cells; id += TB) seen0[id] = 0u;
         __syncthreads();
     }
@@ -561,7 +607,7 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                     tc[d] = 2 * q + ((color >> d) & 1);
                 }
             };
-            const TileShared ts = tile_shared(max_box, g.n_cells);
+            const TileShared ts = tile_shared(max_box, g.n_cells, cl_cap, D);
             uint32_t* seen = (uint32_t*)(sm + ts.seen);
             // seen[] stamps, unique within a launch (at most 2^18 MCS x 8
             // sub-phases x 1024 slots; seen[] starts zeroed)
@@ -574,7 +620,8 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                 int tc[3];
                 tile_coords(k, tc);
                 if (tid == 0) {
-                    lsd = gsd;
+                    // lsd holds gsd's parameters since the kernel started;
+                    // only the box geometry changes per tile
                     for (int d = 0; d < D; ++d) {
                         const int L = g.dims[d];
                         const int b0 = tile_begin(tc[d], L, tg.nt[d]), b1 = tile_begin(tc[d] + 1, L, tg.nt[d]);
@@ -611,7 +658,11 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                               (uint16_t*)(sm + ts.adh), (uint8_t*)(sm + ts.dirty), (uint8_t*)(sm + ts.own),
                               (uint8_t*)(sm + ts.mod), (uint32_t*)(sm + ts.c_site), (uint32_t*)(sm + ts.c_key),
                               (uint32_t*)(sm + ts.c_cells), (uint32_t*)(sm + ts.c_flags), (uint32_t*)(sm + ts.c_gf),
-                              (int16_t*)(sm + ts.c_dl), t3, &s_n};
+                              (uint32_t*)(sm + ts.c_z), (int16_t*)(sm + ts.c_dl), t3, &s_n,
+                              (uint16_t*)(sm + ts.slot), (long long*)(sm + ts.ssp), (long long*)(sm + ts.sso), cl_cap};
+            uint8_t* skd = (uint8_t*)(sm + ts.skd);
+            uint32_t* sgf = (uint32_t*)(sm + ts.sgf);
+            uint32_t* sz = (uint32_t*)(sm + ts.sz);
             // Stage the box of the current tile: sigma into shared memory,
             // each distinct cell listed once (and claimed when `claim`),
             // then the listed cells' V, I and type. Nothing writes sigma, V
@@ -622,17 +673,57 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                 const uint32_t stamp = stamp_of(k) + salt;
                 int box = 1;
                 for (int d = 0; d < D; ++d) box *= s_box_dims[d];
-                for (int q = tid; q < box; q += TB) {
-                    int xg[3];
-                    // a fixed lattice's rim outside the box maps to its medium halo
-                    const int gf = P.gflat_of_box(q, xg);
-                    const uint32_t id = __ldcg(g.sigma + gf);
-                    P.sig[q] = (uint16_t)id;
-                    if (id && atomicExch(&seen[id], stamp) != stamp) {
-                        if (claim) atomicMin(claims + id, key);
-                        clist[atomicAdd(&s_ncell, 1)] = id;
+                // four sites per thread in flight: their sigma loads first, then the rest
+                for (int q0 = tid; q0 < box; q0 += 4 * TB) {
+                    int gfs[4];
+                    uint32_t ids[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int q = q0 + u * TB;
+                        int xg[3];
+                        // a fixed lattice's rim outside the box maps to its medium halo
+                        gfs[u] = q < box ? P.gflat_of_box(q, xg) : 0;
+                        ids[u] = q < box ? __ldcg(g.sigma + gfs[u]) : 0u;
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int q = q0 + u * TB;
+                        if (q >= box) break;
+                        const uint32_t id = ids[u];
+                        const int gf = gfs[u];
+                        P.sig[q] = (uint16_t)id;
+                        if (id && atomicExch(&seen[id], stamp) != stamp) {
+                            if (claim) atomicMin(claims + id, key);
+                            clist[atomicAdd(&s_ncell, 1)] = id;
+                        }
+                        // this MCS's draw of each tile site (site_draw keyed by the global flat index)
+                        bool interior = true;
+                        int r = q;
+                        for (int d = D - 1; d >= 0; --d) {
+                            const int li = r % s_box_dims[d];
+                            r /= s_box_dims[d];
+                            if (li == 0 || li == s_box_dims[d] - 1) interior = false;
+                        }
+                        if (interior) {
+                            const uint4 rd = site_draw(g.seed, mcs, (uint32_t)gf);
+                            skd[q] = (uint8_t)(((unsigned long long)rd.x * (unsigned)g.n_copy) >> 32);
+                            sgf[q] = (uint32_t)gf;
+                            sz[q] = rd.z;
+                        }
                     }
                 }
+                // the tile's site-colour order and pass keys
+                if (tid == 0) {
+                    const int ncol = 1 << D;
+                    for (int c = 0; c < ncol; ++c) sperm[c] = c;
+                    for (int c = ncol - 1; c > 0; --c) {
+                        const uint4 rr = aux_draw(g.seed, mcs, TAG_TILE, 2u + (uint32_t)k, (uint32_t)c);
+                        const int j = (int)(((unsigned long long)rr.x * (unsigned)(c + 1)) >> 32);
+                        const int t = sperm[c]; sperm[c] = sperm[j]; sperm[j] = t;
+                    }
+                }
+                if (tid < (1 << D))
+                    s_pkey[tid] = aux_draw(g.seed, mcs, TAG_PASS, (uint32_t)(tid * 64 + ci), (uint32_t)k).x;
                 __syncthreads();
                 const int nc = s_ncell;
                 for (int i = tid; i <= nc; i += TB) {
@@ -642,6 +733,11 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                     P.adh[id] = g.adh_of[id];
                     P.dirty[id] = 0;
                     P.mod[id] = 0;
+                    P.slot[id] = (i < nc && i < cl_cap) ? (uint16_t)i : (uint16_t)0xFFFFu;
+                    if (i < nc && i < cl_cap) {
+                        for (int d = 0; d < D; ++d) P.ssp[i * D + d] = __ldcg(g.sum_pos + (int64_t)id * D + d);
+                        for (int d = 0; d < D * D; ++d) P.sso[i * D * D + d] = __ldcg(g.sum_outer + (int64_t)id * D * D + d);
+                    }
                 }
             };
             // own[id]: the lowest claiming tile of this sub-phase is this one
@@ -714,18 +810,8 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                 for (int d = 0; d < D; ++d) box *= s_box_dims[d];
                 long long t_p0 = clock64();
                 cyc_stage += t_p0 - t_s0;
-                // site-colour passes of this tile, random order
-                int ncol = 1;
-                for (int d = 0; d < D; ++d) ncol *= 2;
-                if (tid == 0) {
-                    for (int c = 0; c < ncol; ++c) sperm[c] = c;
-                    for (int c = ncol - 1; c > 0; --c) {
-                        const uint4 r = aux_draw(g.seed, mcs, TAG_TILE, 2u + (uint32_t)k, (uint32_t)c);
-                        const int j = (int)(((unsigned long long)r.x * (unsigned)(c + 1)) >> 32);
-                        const int t = sperm[c]; sperm[c] = sperm[j]; sperm[j] = t;
-                    }
-                }
-                __syncthreads();
+                // site-colour passes of this tile, in the order staged with the box
+                const int ncol = 1 << D;
                 for (int pi = 0; pi < ncol; ++pi) {
                     const int sc = sperm[pi];
                     // local sites with global coordinate parity == colour bit
@@ -739,7 +825,7 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                         cnt[d] = s_tcnt[d] > first ? (s_tcnt[d] - first + 1) / 2 : 0;
                         n_class *= cnt[d];
                     }
-                    const uint32_t pass_key = aux_draw(g.seed, mcs, TAG_PASS, (uint32_t)(pi * 64 + ci), (uint32_t)k).x;
+                    const uint32_t pass_key = s_pkey[pi];
                     const long long tb0 = clock64();
                     if (tid == 0) s_n = 0;
                     __syncthreads();
@@ -756,10 +842,8 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                                 r /= cnt[d];
                                 t += (base[d] + 2 * i + 1) * (int)lsd.strides[d];
                             }
-                            int xg[3];
-                            gf = P.gflat_of_box(t, xg);
-                            const uint4 rd = site_draw(g.seed, mcs, (uint32_t)gf);
-                            kd = (int)(((unsigned long long)rd.x * (unsigned)g.n_copy) >> 32);
+                            gf = (int)sgf[t];
+                            kd = skd[t];
                             L = P.sig[t];
                             G = P.sig[t + (int)lsd.copy_off[kd]];
                             if (L != G) {
@@ -781,6 +865,7 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                                 P.c_key[pos] = (mix32((uint32_t)j * 0x9E3779B9u ^ pass_key) & 0xFFFFC000u) | (uint32_t)j;
                                 P.c_flags[pos] = (uint32_t)kd | T_PEND;
                                 P.c_gf[pos] = (uint32_t)gf;
+                                P.c_z[pos] = sz[t];
                             }
                         }
                     }
@@ -826,6 +911,11 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                     if (P.own[id] && P.mod[id]) {
                         __stcg(g.volume + id, P.vol[id]);
                         __stcg(g.interface + id, P.itf[id]);
+                        if (i < cl_cap) {
+                            for (int d = 0; d < D; ++d) __stcg((long long*)g.sum_pos + (int64_t)id * D + d, P.ssp[i * D + d]);
+                            for (int d = 0; d < D * D; ++d)
+                                __stcg((long long*)g.sum_outer + (int64_t)id * D * D + d, P.sso[i * D * D + d]);
+                        }
                     }
                 }
                 __syncthreads();
@@ -904,7 +994,9 @@ bool tiled_plan(int D, const int* dims, int periodic, int* nt, int* max_box) {
     return box <= TMAX_BOX && klass <= TCMAX;
 }
 
-size_t tiled_smem_bytes(int max_box, int n_cells) { return tile_shared(max_box, n_cells).total; }
+size_t tiled_smem_bytes(int max_box, int n_cells, int cl_cap, int D) {
+    return tile_shared(max_box, n_cells, cl_cap, D).total;
+}
 int tiled_block() { return TB; }
 
 cudaError_t tiled_occupancy(int D, int NE, size_t smem, int* per_sm) {
@@ -929,7 +1021,7 @@ cudaError_t tiled_occupancy(int D, int NE, size_t smem, int* per_sm) {
 
 cudaError_t launch_tiled(int D, int NE, SimDesc* d_sim, uint64_t n_mcs, const int* nt, void* d_barrier,
                          unsigned long long* d_claims, const uint64_t* d_t3, int max_box, int tables_in_smem,
-                         int barrier_extra, size_t smem, int grid, cudaStream_t st) {
+                         int barrier_extra, int cl_cap, size_t smem, int grid, cudaStream_t st) {
     TileGrid tg;
     for (int d = 0; d < 3; ++d) { tg.nt[d] = d < D ? nt[d] : 1; tg.off[d] = 0; }
     tg.colors = 1 << D;
@@ -940,7 +1032,7 @@ cudaError_t launch_tiled(int D, int NE, SimDesc* d_sim, uint64_t n_mcs, const in
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);      \
         if (e != cudaSuccess) return e;                                                                     \
         void* args[] = {(void*)&d_sim, (void*)&n_mcs, (void*)&tg, (void*)&bar, (void*)&d_claims, (void*)&d_t3, \
-                        (void*)&max_box, (void*)&tables_in_smem, (void*)&barrier_extra};                    \
+                        (void*)&max_box, (void*)&tables_in_smem, (void*)&barrier_extra, (void*)&cl_cap};   \
         return cudaLaunchCooperativeKernel((const void*)k, dim3(grid), dim3(TB), args, smem, st);            \
     }
     switch (tiled_index(D, NE)) {
