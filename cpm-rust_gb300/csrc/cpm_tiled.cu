@@ -53,7 +53,7 @@ struct TileGrid {
 
 // Tile j on an axis covers global coordinates [off + b_j, off + b_{j+1}) mod L,
 // b_j = floor(j * L / nt).
-__device__ __forceinline__ int tile_begin(int j, int L, int nt) { return (int)(((long long)j * L) / nt); }
+__device__ __forceinline__ int tile_begin(int j, int L, int nt) { return (int)(((unsigned)j * (unsigned)L) / (unsigned)nt); }
 
 struct BarrierState {
     unsigned int count;
@@ -674,7 +674,10 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                 int box = 1;
                 for (int d = 0; d < D; ++d) box *= s_box_dims[d];
                 // four sites per thread in flight: their sigma loads first, then the rest
-                for (int q0 = tid; q0 < box; q0 += 4 * TB) {
+                // the loop bound is uniform across the block: every lane reaches
+                // the warp-wide match below, lanes past the box with id 0
+                for (int base = 0; base < box; base += 4 * TB) {
+                    const int q0 = base + tid;
                     int gfs[4];
                     uint32_t ids[4];
 #pragma unroll
@@ -688,11 +691,16 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
 #pragma unroll
                     for (int u = 0; u < 4; ++u) {
                         const int q = q0 + u * TB;
-                        if (q >= box) break;
-                        const uint32_t id = ids[u];
+                        const bool valid = q < box;
+                        const uint32_t id = valid ? ids[u] : 0u;
+                        // one lane per distinct id of the warp touches the cell's stamp
+                        // (every lane takes part in the match; lanes past the box carry id 0)
+                        const unsigned peers = __match_any_sync(0xffffffffu, id);
+                        const bool leader = (int)(threadIdx.x & 31) == __ffs(peers) - 1;
+                        if (!valid) continue;
                         const int gf = gfs[u];
                         P.sig[q] = (uint16_t)id;
-                        if (id && atomicExch(&seen[id], stamp) != stamp) {
+                        if (id && leader && atomicExch(&seen[id], stamp) != stamp) {
                             if (claim) atomicMin(claims + id, key);
                             clist[atomicAdd(&s_ncell, 1)] = id;
                         }
