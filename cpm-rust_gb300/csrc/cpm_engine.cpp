@@ -85,6 +85,9 @@ void DeviceSims::dev_free(void* p) {
 }
 
 DeviceSims::~DeviceSims() {
+    for (auto a : aux_) cudaStreamDestroy(a);
+    for (auto e : joins_) cudaEventDestroy(e);
+    if (ev_fork_) cudaEventDestroy(ev_fork_);
     for (void* p : {(void*)d_bar_, (void*)arena_, (void*)d_descs_, (void*)d_plans_, (void*)d_next_})
         if (p) dev_free(p);
 }
@@ -433,7 +436,8 @@ std::string DeviceSims::run_tiled(const RunPlan& p, const uint64_t* t3) {
 std::string DeviceSims::run(const std::vector<RunPlan>& plans, int grid_override) {
     std::string err;
     const uint64_t* t3 = nullptr;
-    // group plans by kernel variant: (resident?, D, NE); tiled plans run one by one
+    // group plans by kernel: (path, D, NE); resident plans also by block
+    // variant (0: 512 threads, 1: 256); tiled plans run one by one
     std::map<std::tuple<int, int, int>, std::vector<RunPlan>> groups;
     std::vector<RunPlan> tiled;
     for (const RunPlan& p : plans) {
@@ -444,7 +448,8 @@ std::string DeviceSims::run(const std::vector<RunPlan>& plans, int grid_override
         }
         const Path pa = path(p.sim);
         if (pa == TILED) { tiled.push_back(p); continue; }
-        groups[std::make_tuple(pa == RESIDENT ? 1 : 0, L.g.D, L.NE)].push_back(p);
+        const int kind = pa == RESIDENT ? 1 + cpmgpu::resident_variant(L.g.n_padded, L.n_cells) : 0;
+        groups[std::make_tuple(kind, L.g.D, L.NE)].push_back(p);
     }
     for (const RunPlan& p : tiled) {
         err = run_tiled(p, t3);
@@ -474,9 +479,24 @@ std::string DeviceSims::run(const std::vector<RunPlan>& plans, int grid_override
     int dev = 0, sms = 1;
     CUDA_TRY(cudaGetDevice(&dev));
     CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    // groups after the first run on auxiliary streams forked from and joined
+    // to the object's stream, so one group's CTAs start as another's drain
+    if (groups.size() > 1 && aux_.empty()) {
+        aux_.resize(std::min<size_t>(groups.size(), 16) - 1);
+        for (auto& a : aux_) CUDA_TRY(cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking));
+        CUDA_TRY(cudaEventCreateWithFlags(&ev_fork_, cudaEventDisableTiming));
+        joins_.resize(aux_.size());
+        for (auto& e : joins_) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    if (groups.size() > 1) CUDA_TRY(cudaEventRecord(ev_fork_, stream_));
     size_t gi = 0;
     for (auto& kv : groups) {
         const auto r = ranges[gi];
+        cudaStream_t gst = stream_;
+        if (gi > 0 && gi - 1 < aux_.size()) {
+            gst = aux_[gi - 1];
+            CUDA_TRY(cudaStreamWaitEvent(gst, ev_fork_, 0));
+        }
         const int res = std::get<0>(kv.first), D = std::get<1>(kv.first), NE = std::get<2>(kv.first);
         int max_cells = 0;
         size_t smem = 0;
@@ -486,15 +506,20 @@ std::string DeviceSims::run(const std::vector<RunPlan>& plans, int grid_override
             smem = std::max(smem, cpmgpu::resident_smem_bytes(L.g.n_padded, L.n_cells));
         }
         if (res) {
+            const int variant = res - 1;
             int per_sm = 1;
-            CUDA_TRY(cpmgpu::resident_occupancy(D, NE, smem, &per_sm));
+            CUDA_TRY(cpmgpu::resident_occupancy(D, NE, variant, smem, &per_sm));
             int grid = grid_override > 0 ? grid_override : std::min<int>((int)r.second, sms * std::max(1, per_sm));
-            CUDA_TRY(cpmgpu::launch_resident(D, NE, d_descs_, d_plans_ + r.first, (int)r.second, d_next_ + gi, t3, smem,
-                                             std::max(1, grid), stream_));
+            CUDA_TRY(cpmgpu::launch_resident(D, NE, variant, d_descs_, d_plans_ + r.first, (int)r.second, d_next_ + gi, t3, smem,
+                                             std::max(1, grid), gst));
         } else {
             int grid = grid_override > 0 ? grid_override : std::min<int>((int)r.second, sms * 4);
             CUDA_TRY(cpmgpu::launch_sweep(D, NE, d_descs_, d_plans_ + r.first, (int)r.second, d_next_ + gi, t3, max_cells,
-                                          std::max(1, grid), stream_));
+                                          std::max(1, grid), gst));
+        }
+        if (gst != stream_) {
+            CUDA_TRY(cudaEventRecord(joins_[gi - 1], gst));
+            CUDA_TRY(cudaStreamWaitEvent(stream_, joins_[gi - 1], 0));
         }
         ++gi;
     }

@@ -104,6 +104,9 @@ class DeviceSims {
     size_t device_bytes_ = 0;
     bool stream_ordered_ = false;
     int tiled_grid_cap_ = 0;
+    std::vector<cudaStream_t> aux_;  // further kernel groups of one run
+    std::vector<cudaEvent_t> joins_;
+    cudaEvent_t ev_fork_ = nullptr;
     cudaError_t dev_alloc(void** p, size_t bytes);
     void dev_free(void* p);
 };

@@ -34,9 +34,16 @@
 
 namespace cpmgpu {
 
-constexpr int RB = 512;       // threads per CTA
-constexpr int CMAX = 2048;    // candidate slots of one chunk
-constexpr int CHUNK = 8192;   // sites per chunk (halved while a chunk overflows CMAX)
+// Two block sizes: 512 threads (one CTA per SM) for simulations whose
+// shared state needs more than half an SM, 256 threads with half the
+// candidate capacity for smaller ones, so that two share an SM and hide
+// each other's barrier latency. Which one a simulation uses depends only on
+// its own size (resident_variant).
+template <int BS>
+struct ResCfg {
+    static constexpr int CMAX = BS == 512 ? 2048 : 1024;   // candidate slots of one chunk
+    static constexpr int CHUNK = BS == 512 ? 8192 : 4096;  // sites per chunk (halved while a chunk overflows CMAX)
+};
 
 // flag bits of a candidate
 enum : uint32_t {
@@ -58,7 +65,7 @@ __host__ __device__ inline uint32_t res_take(uint32_t& off, uint64_t bytes) {
     return o;
 }
 
-__host__ __device__ inline ResLayout res_layout(int64_t n_padded, int n_cells) {
+__host__ __device__ inline ResLayout res_layout(int64_t n_padded, int n_cells, int CMAX) {
     ResLayout L;
     uint32_t off = 0;
     const uint64_t n1 = (uint64_t)n_cells + 1;
@@ -132,7 +139,7 @@ __device__ double block_sum_r(double v, double* scratch) {
 
 // Global energy of the resident state (each unordered pair of different
 // neighbouring cells contributes J once; volume and interface terms).
-template <int D, int NE>
+template <int D, int NE, int RB>
 __device__ double res_energy(const SimDesc& s, const uint16_t* sig, const uint32_t* vol, const uint32_t* itf,
                              const uint16_t* adh, double* scratch) {
     const int nt1 = s.n_types + 1;
@@ -175,8 +182,10 @@ __device__ double res_energy(const SimDesc& s, const uint16_t* sig, const uint32
     return (ev + ei) + ea;
 }
 
-template <int D, int NE>
+template <int D, int NE, int RB>
 struct Resident {
+    static constexpr int CMAX = ResCfg<RB>::CMAX;
+    static constexpr int CHUNK = ResCfg<RB>::CHUNK;
     const SimDesc& s;
     uint16_t* sig;
     uint32_t *vol, *itf, *b0, *b1;
@@ -384,9 +393,9 @@ struct Resident {
     }
 };
 
-template <int D, int NE>
-__global__ void __launch_bounds__(RB) resident_kernel(SimDesc* sims, const RunPlan* plans, int n_plans, int* next_plan,
-                                                      const uint64_t* t3) {
+template <int D, int NE, int RB>
+__global__ void __launch_bounds__(RB, 512 / RB) resident_kernel(SimDesc* sims, const RunPlan* plans, int n_plans,
+                                                                int* next_plan, const uint64_t* t3) {
     extern __shared__ __align__(16) unsigned char sm[];
     __shared__ SimDesc sd;
     __shared__ int s_plan, s_n, s_flag;
@@ -405,8 +414,8 @@ __global__ void __launch_bounds__(RB) resident_kernel(SimDesc* sims, const RunPl
         if (tid == 0) sd = sims[plan.sim];
         if (tid < 10) sstat[tid] = 0;
         __syncthreads();
-        const ResLayout lay = res_layout(sd.n_padded, sd.n_cells);
-        Resident<D, NE> R{sd,
+        const ResLayout lay = res_layout(sd.n_padded, sd.n_cells, ResCfg<RB>::CMAX);
+        Resident<D, NE, RB> R{sd,
                           (uint16_t*)(sm + lay.sig),
                           (uint32_t*)(sm + lay.vol),
                           (uint32_t*)(sm + lay.itf),
@@ -462,14 +471,14 @@ __global__ void __launch_bounds__(RB) resident_kernel(SimDesc* sims, const RunPl
             for (uint64_t m = 0; m < chunk; ++m, ++mcs) one_mcs(mcs);
             burned += chunk;
             if (burned >= plan.energy_sample_start) {
-                const double e = res_energy<D, NE>(sd, R.sig, R.vol, R.itf, R.adh, scratch);
+                const double e = res_energy<D, NE, RB>(sd, R.sig, R.vol, R.itf, R.adh, scratch);
                 if (tid == 0 && sd.energy_out) sd.energy_out[e_idx] = e;
                 ++e_idx;
             }
         }
         for (int smp = 0; smp < plan.n_samples; ++smp) {
             for (uint64_t m = 0; m < plan.interval; ++m, ++mcs) one_mcs(mcs);
-            const double e = res_energy<D, NE>(sd, R.sig, R.vol, R.itf, R.adh, scratch);
+            const double e = res_energy<D, NE, RB>(sd, R.sig, R.vol, R.itf, R.adh, scratch);
             if (tid == 0 && sd.energy_out) sd.energy_out[e_idx + smp] = e;
             if (plan.write_samples) {
                 const int n1 = sd.n_cells + 1;
@@ -529,18 +538,34 @@ static int res_index(int D, int NE) {
     return -1;
 }
 
-size_t resident_smem_bytes(int64_t n_padded, int n_cells) { return res_layout(n_padded, n_cells).total; }
 size_t resident_smem_limit() { return 227 * 1024 - 4096; }
-int resident_block() { return RB; }
 
-cudaError_t launch_resident(int Dd, int NEd, SimDesc* d_sims, const RunPlan* d_plans, int n_plans, int* d_next,
-                            const uint64_t* d_t3, size_t smem, int grid, cudaStream_t st) {
+// 1: the 256-thread variant (two CTAs per SM), when its shared state fits
+// half an SM; 0: the 512-thread variant.
+int resident_variant(int64_t n_padded, int n_cells) {
+    return res_layout(n_padded, n_cells, ResCfg<256>::CMAX).total <= resident_smem_limit() / 2 - 1024 ? 1 : 0;
+}
+size_t resident_smem_bytes(int64_t n_padded, int n_cells) {
+    return resident_variant(n_padded, n_cells) ? res_layout(n_padded, n_cells, ResCfg<256>::CMAX).total
+                                               : res_layout(n_padded, n_cells, ResCfg<512>::CMAX).total;
+}
+int resident_block(int variant) { return variant ? 256 : 512; }
+
+cudaError_t launch_resident(int Dd, int NEd, int variant, SimDesc* d_sims, const RunPlan* d_plans, int n_plans,
+                            int* d_next, const uint64_t* d_t3, size_t smem, int grid, cudaStream_t st) {
 #define RES_CASE(I, D_, NE_)                                                                                   \
     case I: {                                                                                                  \
-        auto k = resident_kernel<D_, NE_>;                                                                      \
-        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);         \
-        if (e != cudaSuccess) return e;                                                                        \
-        k<<<grid, RB, smem, st>>>(d_sims, d_plans, n_plans, d_next, d_t3);                                     \
+        if (variant) {                                                                                         \
+            auto k = resident_kernel<D_, NE_, 256>;                                                             \
+            cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);     \
+            if (e != cudaSuccess) return e;                                                                    \
+            k<<<grid, 256, smem, st>>>(d_sims, d_plans, n_plans, d_next, d_t3);                                \
+        } else {                                                                                               \
+            auto k = resident_kernel<D_, NE_, 512>;                                                             \
+            cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);     \
+            if (e != cudaSuccess) return e;                                                                    \
+            k<<<grid, 512, smem, st>>>(d_sims, d_plans, n_plans, d_next, d_t3);                                \
+        }                                                                                                      \
         break;                                                                                                 \
     }
     switch (res_index(Dd, NEd)) {
@@ -555,14 +580,21 @@ cudaError_t launch_resident(int Dd, int NEd, SimDesc* d_sims, const RunPlan* d_p
     return cudaGetLastError();
 }
 
-cudaError_t resident_occupancy(int Dd, int NEd, size_t smem, int* blocks_per_sm) {
+cudaError_t resident_occupancy(int Dd, int NEd, int variant, size_t smem, int* blocks_per_sm) {
     *blocks_per_sm = 1;
 #define OCC_CASE(I, D_, NE_)                                                                                  \
     case I: {                                                                                                 \
-        auto k = resident_kernel<D_, NE_>;                                                                     \
-        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);        \
+        cudaError_t e;                                                                                        \
+        if (variant) {                                                                                        \
+            auto k = resident_kernel<D_, NE_, 256>;                                                            \
+            e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);               \
+            if (e != cudaSuccess) return e;                                                                   \
+            return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k, 256, smem);                \
+        }                                                                                                     \
+        auto k = resident_kernel<D_, NE_, 512>;                                                                \
+        e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);                   \
         if (e != cudaSuccess) return e;                                                                       \
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k, RB, smem);                     \
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k, 512, smem);                    \
     }
     switch (res_index(Dd, NEd)) {
         OCC_CASE(0, 2, 4)
