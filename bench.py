@@ -448,17 +448,24 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def profiled_traffic_per_attempt():
-    """DRAM bytes per attempt of the sweep kernel from the committed ncu summary (or None)."""
+def profiled_traffic(mcs_per_launch):
+    """DRAM bytes of one sweep launch of `mcs_per_launch` MCS on this
+    workload, from the committed ncu summary (None when it holds no capture
+    of that launch: the traffic is the lattice reload after the L2 flush
+    plus the write-back, not proportional to the MCS)."""
     path = os.path.join(ROOT, "profiles", "sweep_c2_traffic.txt")
+    vals = {}
     try:
         with open(path) as f:
             for line in f:
-                if line.startswith("dram_bytes_per_attempt:"):
-                    return float(line.split(":", 1)[1])
+                if ":" in line and not line.startswith("#"):
+                    k, v = line.split(":", 1)
+                    vals[k.strip()] = float(v)
     except Exception:
-        pass
-    return None
+        return None
+    if int(vals.get("mcs_per_launch", -1)) != mcs_per_launch:
+        return None
+    return vals.get("dram_bytes_per_launch")
 
 
 # ---------------------------------------------------------- reference arm ----
@@ -577,7 +584,7 @@ def run_gpu(args, rank, world, dist):
     launch_s = (total_ms / 1000.0) / args.steps
     achieved = bytes_per_attempt * (attempts / args.steps) / launch_s / 1e9
     peaks, src = measured_peaks()
-    traffic_pa = profiled_traffic_per_attempt()
+    traffic_launch = profiled_traffic(args.mcs_per_step)
 
     # ---- e2e through the public API (host buffers, copies inside the timed region)
     e2e = None
@@ -625,7 +632,7 @@ def run_gpu(args, rank, world, dist):
             "peak": peaks.get("hbm_gbs"),
             "unit": "GB/s",
             "frac": achieved / peaks.get("hbm_gbs"),
-            "traffic": traffic_pa * attempts / args.steps if traffic_pa is not None else None,
+            "traffic": traffic_launch,
             "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)" if src == "measured" else "fallback",
             "algorithmic_bytes_per_attempt": bytes_per_attempt,
         },
