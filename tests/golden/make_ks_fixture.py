@@ -6,7 +6,11 @@ frozen trajectory) for seeds 1..N of the quickstart configuration
 type V*=50 I*=75 lambda_V=10 lambda_I=2, 5 cells, J=[[0,5],[5,2]], default
 placement, 5000 burn-in + 5000 readout MCS) and stores the last sample's
 per-cell volume, interface, squared radius of gyration and kappa^2 plus the
-final energy. Usage: python tests/golden/make_ks_fixture.py
+final energy; and (`fluct_oracle_summary.npz`) the per-seed summaries of a
+second configuration sized for the tiled sweep — 84x84 periodic, one type
+V*=40 I*=30 lambda_V=3 lambda_I=0.6, 80 cells, J=[[0,6.5],[6.5,2.2]],
+2000 burn-in + 1000 readout MCS, seeds 1..160 — whose state is stationary
+well before the sample. Usage: python tests/golden/make_ks_fixture.py
 """
 
 import os
@@ -26,6 +30,32 @@ def c1_spec():
     return O.ModelSpec((30, 30), True, [(50, 75, 10.0, 2.0)], [[0, 5], [5, 2]], cell_counts=[5])
 
 
+FLUCT_SEEDS = 160
+FLUCT_BURN_IN, FLUCT_READOUT = 2000, 1000
+
+
+def fluct_spec():
+    return O.ModelSpec((84, 84), True, [(40, 30, 3.0, 0.6)], [[0, 6.5], [6.5, 2.2]], cell_counts=[80])
+
+
+def fluct_main():
+    seeds = np.arange(1, FLUCT_SEEDS + 1, dtype=np.uint64)
+    failed, cells, energy, n = O.run_many(fluct_spec(), seeds, FLUCT_BURN_IN, FLUCT_READOUT, threads=0,
+                                          local_halo=True)
+    assert failed == 0 and np.all(n == 80)
+    v = cells["volume"].astype(np.float64)
+    i = cells["interface"].astype(np.float64)
+    np.savez_compressed(
+        os.path.join(HERE, "fluct_oracle_summary.npz"),
+        seeds=seeds,
+        energy=energy,
+        mean_volume=v.mean(1),
+        volume_std=v.std(1),
+        mean_interface=i.mean(1),
+    )
+    print("wrote", os.path.join(HERE, "fluct_oracle_summary.npz"))
+
+
 def main():
     seeds = np.arange(1, N_SEEDS + 1, dtype=np.uint64)
     failed, cells, energy, n = O.run_many(c1_spec(), seeds, BURN_IN, READOUT, threads=0, local_halo=True)
@@ -43,4 +73,8 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    if "--fluct" in sys.argv:
+        fluct_main()
+    else:
+        main()
+        fluct_main()

@@ -59,3 +59,40 @@ def test_c1_summary_distributions_match_oracle(cuda_required):
         assert pvals[key] > 0.001, pvals
     # every run kept exact state: volumes sum consistently and stay >= 1
     assert np.all(gpu["volume"] >= 1)
+
+
+def _fluct_builders(seeds):
+    from helpers import Model
+
+    return [Model((84, 84), "periodic", [("a", 40, 30, 3.0, 0.6)], [[0, 6.5], [6.5, 2.2]], [80],
+                  seed=int(s)).builder(warn=False) for s in seeds]
+
+
+@pytest.mark.parametrize("path", ["tiled", "resident"])
+def test_fluctuating_cells_match_oracle_on_both_sweeps(path, cuda_required, monkeypatch):
+    """The tiled sweep (tile-colour sub-phases, cell claims, warp-level pass
+    resolution) and the resident sweep against the oracle on a configuration
+    that is stationary by the sample: per-seed energy, mean interface, mean
+    and spread of the volumes, two-sample KS p > 0.01 over 160 seeds
+    (fixture tests/golden/fluct_oracle_summary.npz)."""
+    from scipy.stats import ks_2samp
+
+    from cpm import _cpm
+
+    if path == "tiled":
+        monkeypatch.setenv("CPM_GPU_FORCE_TILED", "1")
+    ref = np.load(os.path.join(HERE, "golden", "fluct_oracle_summary.npz"))
+    results = _cpm.run_many(_fluct_builders(ref["seeds"]), 2000, 1000, 1000, topology=False)
+    last = [r.samples[-1] for r in results]
+    v = np.stack([s.volume for s in last]).astype(np.float64)
+    i = np.stack([s.interface for s in last]).astype(np.float64)
+    gpu = {"energy": np.array([s.conservative_energy for s in last]), "mean_volume": v.mean(1),
+           "volume_std": v.std(1), "mean_interface": i.mean(1)}
+    pvals = {k: ks_2samp(np.asarray(ref[k]), gpu[k]).pvalue for k in gpu}
+    print(path, "KS p-values:", pvals)
+    for k, p in pvals.items():
+        assert p > 0.01, (k, pvals)
+    st = results[0].stats
+    if path == "tiled":
+        assert st["passes"] > 0 and st["spin_timeouts"] == 0
+        assert st["deferred"] <= 0.001 * st["nonnull"]
