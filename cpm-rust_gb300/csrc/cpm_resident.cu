@@ -238,59 +238,52 @@ struct Resident {
         for (int c = tid; c < n; c += RB) evaluate(c, mcs);
         __syncthreads();
         for (;;) {
-            // ---- fixpoint: final = every lower-key candidate on its cells is a final reject
+            // ---- finality. A pending candidate is final unless an accepting
+            // candidate lies in its lower closure (lower-key candidates
+            // sharing a cell, transitively): then every candidate before it
+            // in the sequential order leaves its cells as they are. Per cell,
+            // T = the lowest key of an accepting or tainted candidate on it;
+            // a candidate with a key above T on either cell is tainted and
+            // lowers T on both; iterate until T is stable. Rejects add
+            // nothing, so the iterations count cross-cell hops of accepts.
             for (int c = tid; c < n; c += RB) {
-                c_flags[c] &= ~F_FIN;
                 if (!(c_flags[c] & F_PEND)) continue;
                 const uint32_t cells = c_cells[c];
                 if (cells & 0xFFFFu) b0[cells & 0xFFFFu] = 0xFFFFFFFFu;
                 if (cells >> 16) b0[cells >> 16] = 0xFFFFFFFFu;
             }
             __syncthreads();
-            uint32_t* bc = b0;
-            uint32_t* bn = b1;
+            for (int c = tid; c < n; c += RB) {
+                const uint32_t fl = c_flags[c];
+                if (!(fl & F_PEND) || !(fl & F_ACC) || (fl & F_GUARD)) continue;
+                const uint32_t cells = c_cells[c], key = c_key[c];
+                if (cells & 0xFFFFu) atomicMin(&b0[cells & 0xFFFFu], key);
+                if (cells >> 16) atomicMin(&b0[cells >> 16], key);
+            }
             for (;;) {
-                for (int c = tid; c < n; c += RB) {
-                    const uint32_t fl = c_flags[c];
-                    if (!(fl & F_PEND)) continue;
-                    if ((fl & F_FIN) && !(fl & F_ACC) && !(fl & F_GUARD)) continue;  // final reject: not a blocker
-                    if ((fl & F_FIN) && (fl & F_GUARD)) continue;
-                    const uint32_t cells = c_cells[c], key = c_key[c];
-                    if (cells & 0xFFFFu) atomicMin(&bc[cells & 0xFFFFu], key);
-                    if (cells >> 16) atomicMin(&bc[cells >> 16], key);
-                }
                 __syncthreads();
                 int changed = 0;
                 for (int c = tid; c < n; c += RB) {
-                    uint32_t fl = c_flags[c];
-                    if (!(fl & F_PEND)) continue;
+                    if (!(c_flags[c] & F_PEND)) continue;
                     const uint32_t cells = c_cells[c], key = c_key[c];
                     const uint32_t L = cells & 0xFFFFu, G = cells >> 16;
-                    if (!(fl & F_FIN)) {
-                        if ((!L || key <= bc[L]) && (!G || key <= bc[G])) {
-                            fl |= F_FIN;
-                            c_flags[c] = fl;
-                            changed = 1;
-                        }
-                    }
-                    const bool blocker = !(fl & F_FIN) || ((fl & F_ACC) && !(fl & F_GUARD));
-                    if (blocker) {
-                        if (L) bn[L] = 0xFFFFFFFFu;
-                        if (G) bn[G] = 0xFFFFFFFFu;
-                    }
+                    const bool tainted = (L && key > b0[L]) || (G && key > b0[G]);
+                    if (!tainted) continue;
+                    if (L && atomicMin(&b0[L], key) > key) changed = 1;
+                    if (G && atomicMin(&b0[G], key) > key) changed = 1;
                 }
                 ct.iters++;
-                const int any = __syncthreads_or(changed);
-                uint32_t* tmp = bc; bc = bn; bn = tmp;
-                if (!any) break;
+                if (!__syncthreads_or(changed)) break;
             }
             // ---- apply the final candidates
             int left = 0;
             for (int c = tid; c < n; c += RB) {
                 uint32_t fl = c_flags[c];
                 if (!(fl & F_PEND)) continue;
-                if (!(fl & F_FIN)) { left = 1; continue; }
-                fl &= ~(F_PEND | F_FIN);
+                const uint32_t cells = c_cells[c], key = c_key[c];
+                const uint32_t L = cells & 0xFFFFu, G = cells >> 16;
+                if ((L && key > b0[L]) || (G && key > b0[G])) { left = 1; continue; }
+                fl &= ~F_PEND;
                 if (fl & F_GUARD) {
                     ct.guard++;
                 } else {

@@ -381,45 +381,35 @@ struct TileProc {
         ct.c_eval += t1 - t0;
         for (;;) {
             t0 = clock64();
+            // finality as in the resident sweep: final unless an accepting
+            // candidate lies in the lower closure (per-cell minimum key of
+            // accepting or tainted candidates, propagated across cells)
             for (int c = tid; c < n; c += TB) {
-                c_flags[c] &= ~T_FIN;
                 if (!(c_flags[c] & T_PEND)) continue;
                 const uint32_t cells = c_cells[c];
                 if (cells & 0xFFFFu) b0[cells & 0xFFFFu] = 0xFFFFFFFFu;
                 if (cells >> 16) b0[cells >> 16] = 0xFFFFFFFFu;
             }
             __syncthreads();
-            uint32_t* bc = b0;
-            uint32_t* bn = b1;
+            for (int c = tid; c < n; c += TB) {
+                const uint32_t fl = c_flags[c];
+                if (!(fl & T_PEND) || !(fl & T_ACC) || (fl & T_GUARD)) continue;
+                const uint32_t cells = c_cells[c], key = c_key[c];
+                if (cells & 0xFFFFu) atomicMin(&b0[cells & 0xFFFFu], key);
+                if (cells >> 16) atomicMin(&b0[cells >> 16], key);
+            }
             for (;;) {
-                for (int c = tid; c < n; c += TB) {
-                    const uint32_t fl = c_flags[c];
-                    if (!(fl & T_PEND)) continue;
-                    if ((fl & T_FIN) && (!(fl & T_ACC) || (fl & T_GUARD))) continue;
-                    const uint32_t cells = c_cells[c], key = c_key[c];
-                    if (cells & 0xFFFFu) atomicMin(&bc[cells & 0xFFFFu], key);
-                    if (cells >> 16) atomicMin(&bc[cells >> 16], key);
-                }
                 __syncthreads();
                 int changed = 0;
                 for (int c = tid; c < n; c += TB) {
-                    uint32_t fl = c_flags[c];
-                    if (!(fl & T_PEND)) continue;
+                    if (!(c_flags[c] & T_PEND)) continue;
                     const uint32_t cells = c_cells[c], key = c_key[c];
                     const uint32_t L = cells & 0xFFFFu, G = cells >> 16;
-                    if (!(fl & T_FIN) && (!L || key <= bc[L]) && (!G || key <= bc[G])) {
-                        fl |= T_FIN;
-                        c_flags[c] = fl;
-                        changed = 1;
-                    }
-                    if (!(fl & T_FIN) || ((fl & T_ACC) && !(fl & T_GUARD))) {
-                        if (L) bn[L] = 0xFFFFFFFFu;
-                        if (G) bn[G] = 0xFFFFFFFFu;
-                    }
+                    if (!((L && key > b0[L]) || (G && key > b0[G]))) continue;
+                    if (L && atomicMin(&b0[L], key) > key) changed = 1;
+                    if (G && atomicMin(&b0[G], key) > key) changed = 1;
                 }
-                const int any = __syncthreads_or(changed);
-                uint32_t* tmp = bc; bc = bn; bn = tmp;
-                if (!any) break;
+                if (!__syncthreads_or(changed)) break;
             }
             t1 = clock64();
             ct.c_fix += t1 - t0;
@@ -427,8 +417,10 @@ struct TileProc {
             for (int c = tid; c < n; c += TB) {
                 uint32_t fl = c_flags[c];
                 if (!(fl & T_PEND)) continue;
-                if (!(fl & T_FIN)) { left = 1; continue; }
-                fl &= ~(T_PEND | T_FIN);
+                const uint32_t cells = c_cells[c], key = c_key[c];
+                const uint32_t L = cells & 0xFFFFu, G = cells >> 16;
+                if ((L && key > b0[L]) || (G && key > b0[G])) { left = 1; continue; }
+                fl &= ~T_PEND;
                 if (fl & T_GUARD) ct.guard++;
                 else {
                     ct.evaluated++;
