@@ -164,6 +164,7 @@ def run_batch_bench(args):
     res = cpm.run_many(sims, burn, readout, interval)
     t_batch = time.perf_counter() - t0
     attempts = sum(r.stats["attempts"] for r in res)
+    split = {k: res[0].stats[k] / 1e6 for k in ("host_place_us", "host_prep_us", "device_us", "host_read_us")}
     # the plain loop: one theta per side (the sides are uniform over the set)
     loop_t = []
     for side in BATCH_SIDES:
@@ -184,6 +185,9 @@ def run_batch_bench(args):
         "plain_loop_sample": "one theta per side, each run alone through cpm.CPM.run; seconds per side " +
                              ", ".join(f"{s}:{t:.2f}" for s, t in zip(BATCH_SIDES, loop_t)),
         "speedup_vs_plain_loop": batch_sims_s / loop_sims_s,
+        "seconds_split": {"validation_and_placement": split["host_place_us"], "staging_upload_launch": split["host_prep_us"],
+                          "device": split["device_us"], "readouts": split["host_read_us"],
+                          "python_side": t_batch - sum(split.values())},
         "timed": "cpm.run_many(...) end to end: host placement, upload, one persistent launch, readouts",
     }
 

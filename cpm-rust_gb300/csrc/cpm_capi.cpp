@@ -11,6 +11,7 @@
 #include <map>
 #include <memory>
 #include <atomic>
+#include <chrono>
 #include <string>
 #include <thread>
 #include <vector>
@@ -723,14 +724,19 @@ extern "C" int cpm_run_many(const cpm_builder* const* builders, size_t n, uint64
     if (!builders || !out) return fail(CPM_E_ARG, "null argument");
     std::vector<Config> cfgs;
     std::vector<Initial> inits;
+    const auto t0 = std::chrono::steady_clock::now();
     int rc = prepare(builders, n, cfgs, inits, burn, readout, interval);
     if (rc) return rc;
+    const uint64_t place_us =
+        (uint64_t)std::chrono::duration_cast<std::chrono::microseconds>(std::chrono::steady_clock::now() - t0).count();
     ReadoutOptions ro;
     ro.include_lattice = include_lattice != 0;
     ro.topology = topology != 0;
     std::vector<Result> rs;
     const std::string msg = run_many(cfgs, inits, ro, rs);
     if (!msg.empty()) return fail(code_for(msg), msg);
+    for (auto& r : rs)
+        if (r.stats.size() > CPM_STAT_HOST_PLACE_US) r.stats[CPM_STAT_HOST_PLACE_US] = place_us;
     for (size_t i = 0; i < n; ++i) {
         auto r = std::make_unique<cpm_result>();
         r->r = std::move(rs[i]);

@@ -41,6 +41,12 @@ enum CpmStat {
     CPM_STAT_CYC_BAR_CLAIM = 23, // tiled sweep: cycles waiting in the grid barrier after the claims
     CPM_STAT_CYC_BAR_WRITE = 24, // tiled sweep: cycles waiting in the grid barrier after the write-back
     CPM_STAT_EXACT_DECISIONS = 25, // decisions the float bracket left to the FP64 computation
+    CPM_STAT_HOST_PREP_US = 26,  // run/run_batch/run_many: microseconds of upload and launch
+    CPM_STAT_DEVICE_US = 27,     // microseconds waiting for the device
+    CPM_STAT_HOST_READ_US = 28,  // microseconds of read-back and host readouts
+    CPM_STAT_CYC_RES_BUILD = 29,   // resident sweep: cycles building candidate lists (thread 0)
+    CPM_STAT_CYC_RES_RESOLVE = 30, // resident sweep: cycles resolving them (thread 0)
+    CPM_STAT_HOST_PLACE_US = 31,   // run_many: microseconds of validation and initial placement
     CPM_STAT_COUNT = 32
 };
 

@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -107,6 +108,10 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
                                const std::vector<int>& n_samples, const std::vector<int>& n_energy,
                                bool lattice_samples, cudaStream_t stream) {
     stream_ = stream;
+    // kernel attributes first: setting them later, while kernels of other
+    // streams run, could wait for those kernels
+    CUDA_TRY(cpmgpu::prepare_resident_kernels());
+    CUDA_TRY(cpmgpu::prepare_tiled_kernels());
     // Selects the global-memory sweep for every simulation (used by the
     // tests to exercise that path on small lattices).
     force_global_ = std::getenv("CPM_GPU_FORCE_GLOBAL") != nullptr;
@@ -163,13 +168,21 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
         o.it32lo = cv.take(nt * (size_t)tab_n[i] * 4);
         o.dj32 = cv.take((nt + 1) * (nt + 1) * (nt + 1) * 4);
         o.J32 = cv.take((nt + 1) * (nt + 1) * 4);
+        o.err = cv.take(8);
+    }
+    // run-window outputs after every input: the device writes them, so they
+    // are neither staged on the host nor uploaded
+    const size_t in_bytes = cv.off;
+    for (size_t i = 0; i < N; ++i) {
+        const SimLayout& L = layouts_[i];
+        Offs& o = offs[i];
+        const size_t n1 = (size_t)L.n_cells + 1, D = (size_t)L.g.D;
         o.energy = cv.take((size_t)std::max(1, L.n_energy) * 8);
         o.svol = cv.take((size_t)L.n_samples * n1 * 4);
         o.sitf = cv.take((size_t)L.n_samples * n1 * 4);
         o.ssp = cv.take((size_t)L.n_samples * n1 * D * 8);
         o.sso = cv.take((size_t)L.n_samples * n1 * D * D * 8);
         o.slat = lattice_samples ? cv.take((size_t)L.n_samples * L.g.n_sites * 4) : 0;
-        o.err = cv.take(8);
     }
     const uint64_t* t3 = nullptr;
     if (need_t3) {
@@ -183,8 +196,10 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
     device_bytes_ = std::max<size_t>(cv.off, 256) + std::max<size_t>(N, 1) * sizeof(SimDesc) + sizeof(int) * 16;
     (void)t3;
     // ---- host staging, then one upload per buffer
-    std::vector<char> stage(cv.off, 0);
-    for (size_t i = 0; i < N; ++i) {
+    std::vector<char> stage(in_bytes, 0);
+    // each simulation stages into its own region of `stage` and its own
+    // descriptor: host threads over simulations
+    auto stage_one = [&](size_t i) {
         const Config& c = configs[i];
         const SimLayout& L = layouts_[i];
         const Offs& o = offs[i];
@@ -335,9 +350,24 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
         s.sample_sum_outer = (int64_t*)(base + o.sso);
         s.sample_lattice = lattice_samples ? (uint32_t*)(base + o.slat) : nullptr;
         s.error = (int32_t*)(base + o.err);
+    };
+    {
+        const unsigned nthreads =
+            (unsigned)std::max<size_t>(1, std::min<size_t>(std::thread::hardware_concurrency(), N));
+        if (nthreads <= 1 || N < 8) {
+            for (size_t i = 0; i < N; ++i) stage_one(i);
+        } else {
+            std::atomic<size_t> next{0};
+            std::vector<std::thread> th;
+            for (unsigned t = 0; t < nthreads; ++t)
+                th.emplace_back([&] {
+                    for (size_t i; (i = next.fetch_add(1)) < N;) stage_one(i);
+                });
+            for (auto& t : th) t.join();
+        }
     }
-    h2d_bytes_ += cv.off + N * sizeof(SimDesc);
-    CUDA_TRY(cudaMemcpyAsync(arena_, stage.data(), cv.off, cudaMemcpyHostToDevice, stream_));
+    h2d_bytes_ += in_bytes + N * sizeof(SimDesc);
+    CUDA_TRY(cudaMemcpyAsync(arena_, stage.data(), in_bytes, cudaMemcpyHostToDevice, stream_));
     CUDA_TRY(cudaMemcpyAsync(d_descs_, descs_.data(), N * sizeof(SimDesc), cudaMemcpyHostToDevice, stream_));
     CUDA_TRY(cudaStreamSynchronize(stream_));
     return "";
@@ -672,86 +702,106 @@ static void cell_summary(int D, uint32_t id, uint32_t vol, uint32_t itf, const i
 
 // Contact graph (state.rs:127-157) and labelling (labelling.rs:70-154) of
 // one lattice snapshot.
-static void topology_readouts(const Config& c, const Geometry& g, const std::vector<uint32_t>& padded, int n_cells,
-                              Sample& smp) {
+// Per-geometry tables of the topology readouts: canon[f] = the interior
+// padded index a padded index f stands for (itself inside, its periodic image
+// in a periodic halo, -1 in a fixed halo), and the stencils as flat offsets.
+struct TopoGeom {
+    std::vector<int32_t> canon;
+    std::vector<int64_t> eoff, coff, moff;
+};
+
+static TopoGeom topo_geom(const Config& c, const Geometry& g) {
+    TopoGeom t;
     const int D = c.D;
     auto offs = [&](int kind) {
         std::vector<int64_t> v;
         for (auto& o : stencil(kind, D)) v.push_back(o[0] * g.strides[0] + o[1] * g.strides[1] + o[2] * g.strides[2]);
         return v;
     };
-    const std::vector<int64_t> eoff = offs(c.energy_nbh);
-    const std::vector<int64_t> coff = offs(NBH_VON_NEUMANN);
-    const std::vector<int64_t> moff = offs(D == 2 ? NBH_MOORE : NBH_TWENTY_SIX);
-    auto interior = [&](int64_t f) {
-        for (int d = 0; d < D; ++d) {
-            const int64_t q = f / g.strides[d];
-            f %= g.strides[d];
-            if (q == 0 || q == g.pdims[d] - 1) return false;
-        }
-        return true;
-    };
-    auto wrapped = [&](int64_t f) {
+    t.eoff = offs(c.energy_nbh);
+    t.coff = offs(NBH_VON_NEUMANN);
+    t.moff = offs(D == 2 ? NBH_MOORE : NBH_TWENTY_SIX);
+    t.canon.assign((size_t)g.n_padded, -1);
+    int64_t p[3] = {0, 0, 0};
+    for (int64_t f = 0; f < g.n_padded; ++f) {
+        bool ok = true;
         int64_t ic[3] = {0, 0, 0};
         for (int d = 0; d < D; ++d) {
-            const int64_t q = f / g.strides[d];
-            f %= g.strides[d];
-            ic[d] = q == 0 ? g.dims[d] - 1 : (q == g.pdims[d] - 1 ? 0 : q - 1);
+            const int64_t q = p[d];
+            if (q == 0 || q == g.pdims[d] - 1) {
+                if (!g.periodic) { ok = false; break; }
+                ic[d] = q == 0 ? g.dims[d] - 1 : 0;
+            } else {
+                ic[d] = q - 1;
+            }
         }
-        return g.flat(ic);
-    };
-    // contact (sparse, canonical (min, max) pairs)
-    std::map<uint64_t, uint32_t> contact;
+        if (ok) t.canon[f] = (int32_t)g.flat(ic);
+        for (int d = D - 1; d >= 0; --d) { if (++p[d] < g.pdims[d]) break; p[d] = 0; }
+    }
+    return t;
+}
+
+// Contact graph and labelling of one sample (output.rs:304-337 with
+// labelling.rs:70-154): each unordered pair of energy-neighbouring sites of
+// different cells counted once, as (min, max) pairs in ascending order; the
+// cells with more than one von Neumann component; the medium's components
+// under the full stencil with their volumes and whether they touch a fixed
+// boundary.
+static void topology_readouts(const Config& c, const Geometry& g, const TopoGeom& tg,
+                              const std::vector<uint32_t>& padded, int n_cells, Sample& smp) {
+    const int D = c.D;
+    // contact: canonical pair keys, sorted and counted (the order std::map would give)
+    std::vector<uint64_t> keys;
+    keys.reserve((size_t)g.n_sites * tg.eoff.size() / 4 + 16);
     int64_t x[3] = {0, 0, 0};
     for (int64_t s = 0; s < g.n_sites; ++s) {
         const int64_t i = g.flat(x);
         const uint32_t ic = padded[i];
-        for (int64_t off : eoff) {
+        for (int64_t off : tg.eoff) {
             const int64_t j = i + off;
-            int64_t key;
-            bool has;
-            if (interior(j)) { key = j; has = true; }
-            else if (g.periodic) { key = wrapped(j); has = true; }
-            else { key = 0; has = false; }
-            if (has && key <= i) continue;
+            const int32_t key = tg.canon[j];
+            if (key >= 0 && key <= i) continue;
             const uint32_t jc = padded[j];
             if (jc == ic) continue;
             const uint32_t a = std::min(ic, jc), b = std::max(ic, jc);
-            contact[((uint64_t)a << 32) | b] += 1;
+            keys.push_back(((uint64_t)a << 32) | b);
         }
         for (int d = D - 1; d >= 0; --d) { if (++x[d] < g.dims[d]) break; x[d] = 0; }
     }
-    for (auto& kv : contact) {
-        smp.contact_a.push_back((uint32_t)(kv.first >> 32));
-        smp.contact_b.push_back((uint32_t)kv.first);
-        smp.contact_n.push_back(kv.second);
+    std::sort(keys.begin(), keys.end());
+    for (size_t k = 0; k < keys.size();) {
+        size_t e = k + 1;
+        while (e < keys.size() && keys[e] == keys[k]) ++e;
+        smp.contact_a.push_back((uint32_t)(keys[k] >> 32));
+        smp.contact_b.push_back((uint32_t)keys[k]);
+        smp.contact_n.push_back((uint32_t)(e - k));
+        k = e;
     }
     // labelling
     std::vector<char> vis((size_t)g.n_padded, 0);
     std::vector<uint32_t> comps(n_cells + 1, 0);
-    std::deque<int64_t> q;
+    std::vector<int64_t> q;
     x[0] = x[1] = x[2] = 0;
     for (int64_t s = 0; s < g.n_sites; ++s) {
         const int64_t seed = g.flat(x);
         for (int d = D - 1; d >= 0; --d) { if (++x[d] < g.dims[d]) break; x[d] = 0; }
         if (vis[seed]) continue;
         const uint32_t owner = padded[seed];
-        const std::vector<int64_t>& of = owner == 0 ? moff : coff;
+        const std::vector<int64_t>& of = owner == 0 ? tg.moff : tg.coff;
         vis[seed] = 1;
-        q.push_back(seed);
+        q.assign(1, seed);
         uint32_t vol = 0;
         bool touches = false;
         while (!q.empty()) {
-            const int64_t site = q.front();
-            q.pop_front();
+            const int64_t site = q.back();
+            q.pop_back();
             ++vol;
             for (int64_t off : of) {
-                const int64_t nb = site + off;
-                if (!interior(nb)) {
-                    if (owner == 0 && !g.periodic) touches = true;
-                    if (!g.periodic) continue;
+                const int32_t cn = tg.canon[site + off];
+                if (cn < 0) {  // fixed boundary
+                    if (owner == 0) touches = true;
+                    continue;
                 }
-                const int64_t cn = interior(nb) ? nb : wrapped(nb);
                 if (vis[cn] || padded[cn] != owner) continue;
                 vis[cn] = 1;
                 q.push_back(cn);
@@ -888,6 +938,7 @@ std::string assemble_result(const Config& c, const Initial& init, const DeviceSi
     const size_t n1 = (size_t)n + 1;
     std::vector<double> trace(energy.begin(), energy.begin() + nt);
     R.samples.resize(ns);
+    TopoGeom tg;
     for (int s = 0; s < ns; ++s) {
         Sample& S = R.samples[s];
         S.mcs = c.burn_in + (uint64_t)(s + 1) * c.interval;
@@ -899,7 +950,10 @@ std::string assemble_result(const Config& c, const Initial& init, const DeviceSi
         if (snapshots) {
             std::vector<uint32_t> interior(slat.begin() + (size_t)s * L.g.n_sites,
                                            slat.begin() + (size_t)(s + 1) * L.g.n_sites);
-            if (ro.topology) topology_readouts(c, L.g, pad_lattice(L.g, interior), n, S);
+            if (ro.topology) {
+                if (tg.canon.empty()) tg = topo_geom(c, L.g);
+                topology_readouts(c, L.g, tg, pad_lattice(L.g, interior), n, S);
+            }
             if (ro.include_lattice) { S.lattice = std::move(interior); S.has_lattice = true; }
         }
     }
@@ -947,13 +1001,17 @@ std::string run_many(const std::vector<Config>& configs, const std::vector<Initi
         ns[i] = plans[i].n_samples;
         ne[i] = nt[i] + ns[i];
     }
+    using clk = std::chrono::steady_clock;
+    const auto t0 = clk::now();
     DeviceSims dev;
     std::string err = dev.create(configs, initials, ns, ne, snapshots);
     if (!err.empty()) return err;
     err = dev.run(plans, device_grid);
     if (!err.empty()) return err;
+    const auto t1 = clk::now();
     err = dev.sync();
     if (!err.empty()) return err;
+    const auto t2 = clk::now();
     // ---- assemble results (host threads over simulations)
     std::atomic<size_t> next{0};
     std::vector<std::string> errs(N);
@@ -973,10 +1031,15 @@ std::string run_many(const std::vector<Config>& configs, const std::vector<Initi
         th.emplace_back([&, dev_id] { cudaSetDevice(dev_id); worker(); });
     for (auto& t : th) t.join();
     for (auto& e : errs) if (!e.empty()) return e;
+    const auto t3 = clk::now();
+    auto us = [](clk::duration d) { return (uint64_t)std::chrono::duration_cast<std::chrono::microseconds>(d).count(); };
     for (auto& R : out) {
         if (R.stats.size() < CPM_STAT_COUNT) R.stats.resize(CPM_STAT_COUNT, 0);
         R.stats[CPM_STAT_H2D_BYTES] = dev.h2d_bytes();
         R.stats[CPM_STAT_D2H_BYTES] = dev.d2h_bytes();
+        R.stats[CPM_STAT_HOST_PREP_US] = us(t1 - t0);
+        R.stats[CPM_STAT_DEVICE_US] = us(t2 - t1);
+        R.stats[CPM_STAT_HOST_READ_US] = us(t3 - t2);
     }
     return "";
 }

@@ -22,6 +22,8 @@
 //   device from the bitmask flood fill (simple_point.rs:242-276).
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include <mutex>
 #include "cpm_common.h"
 #include "cpm_device.cuh"
 #include "cpm_kernels.h"
@@ -531,10 +533,23 @@ cudaError_t launch_sweep(int Dd, int NEd, SimDesc* d_sims, const RunPlan* d_plan
                          const uint64_t* d_t3, int max_cells, int grid, cudaStream_t st) {
     const int in_smem = max_cells <= sweep_max_smem_cells();
     const size_t smem = in_smem ? sweep_smem_bytes(max_cells) : 0;
+    // the shared-memory limit is raised once per kernel and device (see
+    // prepare_resident_kernels)
+    static std::mutex mu;
+    static bool done[64][5] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
     CPM_DISPATCH(Dd, NEd, {
         auto k = sweep_kernel<D, NE, SWEEP_BLOCK>;
-        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(smem > 0 ? smem : 1024));
-        if (e != cudaSuccess) return e;
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            const int v = (D == 2 ? 0 : 2) + (NE == 8 || NE == 18 ? 1 : 0) + (NE == 26 ? 2 : 0);
+            if (dev < 0 || dev >= 64 || !done[dev][v]) {
+                cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+                if (e != cudaSuccess) return e;
+                if (dev >= 0 && dev < 64) done[dev][v] = true;
+            }
+        }
         k<<<grid, SWEEP_BLOCK, smem, st>>>(d_sims, d_plans, n_plans, d_next, d_t3, in_smem);
     });
     return cudaGetLastError();

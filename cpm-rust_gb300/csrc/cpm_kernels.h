@@ -24,6 +24,9 @@ cudaError_t launch_table3d(uint64_t* d_words, const uint32_t* d_face, const uint
 // variant 1 = 256 threads (two per SM) for simulations needing at most half
 // an SM's shared memory, variant 0 = 512 threads.
 int resident_variant(int64_t n_padded, int n_cells);
+// Raise the kernels' shared-memory limits once per device (before launches).
+cudaError_t prepare_resident_kernels();
+cudaError_t prepare_tiled_kernels();
 size_t resident_smem_bytes(int64_t n_padded, int n_cells);
 size_t resident_smem_limit();
 int resident_block(int variant);

@@ -28,6 +28,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "cpm_common.h"
 #include "cpm_device.cuh"
 #include "cpm_kernels.h"
@@ -116,7 +118,7 @@ __device__ __forceinline__ int site_r(const SimDesc& s, const PassInfoR& p, int 
 }
 
 struct CountersR {
-    unsigned long long attempts, nonnull, topo, guard, evaluated, accepted, rounds, iters;
+    unsigned long long attempts, nonnull, topo, guard, evaluated, accepted, rounds, iters, c_build, c_resolve;
 };
 
 template <int BLOCK>
@@ -336,6 +338,7 @@ struct Resident {
         while (start < p.n) {
             int len = min(CHUNK, p.n - start);
             for (;;) {
+                const long long t0 = clock64();
                 if (tid == 0) *s_n = 0;
                 __syncthreads();
                 unsigned long long nonnull = 0, topo = 0;
@@ -378,7 +381,10 @@ struct Resident {
                 ct.attempts += 0;  // attempts are counted per MCS (every site once)
                 ct.nonnull += nonnull;
                 ct.topo += topo;
+                const long long t1 = clock64();
+                ct.c_build += t1 - t0;
                 if (n > 0) resolve(n, mcs, ct);
+                ct.c_resolve += clock64() - t1;
                 break;
             }
             start += len;
@@ -433,7 +439,7 @@ __global__ void __launch_bounds__(RB, 512 / RB) resident_kernel(SimDesc* sims, c
             R.dirty[id] = 0;
         }
         __syncthreads();
-        CountersR ct = {0, 0, 0, 0, 0, 0, 0, 0};
+        CountersR ct = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
         uint64_t mcs = sd.mcs;
         auto one_mcs = [&](uint64_t m) {
             if (tid == 0) {
@@ -516,6 +522,8 @@ __global__ void __launch_bounds__(RB, 512 / RB) resident_kernel(SimDesc* sims, c
             atomicAdd(&sd.stats[CPM_STAT_ROUNDS], ct.rounds);
             atomicAdd(&sd.stats[CPM_STAT_PASSES], (unsigned long long)(mcs - sd.mcs) * sd.n_colors);
             atomicAdd(&sd.stats[9], sstat[9]);
+            atomicAdd(&sd.stats[CPM_STAT_CYC_RES_BUILD], ct.c_build);
+            atomicAdd(&sd.stats[CPM_STAT_CYC_RES_RESOLVE], ct.c_resolve);
             sims[plan.sim].mcs = mcs;
         }
         __syncthreads();
@@ -544,21 +552,43 @@ size_t resident_smem_bytes(int64_t n_padded, int n_cells) {
 }
 int resident_block(int variant) { return variant ? 256 : 512; }
 
+// The kernels' shared-memory limit is raised once per device, before any
+// launch: changing a function attribute while kernels run can wait for
+// them, which would serialise launches on different streams.
+cudaError_t prepare_resident_kernels() {
+    static std::mutex mu;
+    static bool done[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    if (dev >= 0 && dev < 64 && done[dev]) return cudaSuccess;
+    const int smem = (int)resident_smem_limit();
+#define RES_ATTR(D_, NE_)                                                                                    \
+    if ((e = cudaFuncSetAttribute(resident_kernel<D_, NE_, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
+                                  smem)) != cudaSuccess)                                                       \
+        return e;                                                                                              \
+    if ((e = cudaFuncSetAttribute(resident_kernel<D_, NE_, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
+                                  smem)) != cudaSuccess)                                                       \
+        return e;
+    RES_ATTR(2, 4)
+    RES_ATTR(2, 8)
+    RES_ATTR(3, 6)
+    RES_ATTR(3, 18)
+    RES_ATTR(3, 26)
+#undef RES_ATTR
+    if (dev >= 0 && dev < 64) done[dev] = true;
+    return cudaSuccess;
+}
+
 cudaError_t launch_resident(int Dd, int NEd, int variant, SimDesc* d_sims, const RunPlan* d_plans, int n_plans,
                             int* d_next, const uint64_t* d_t3, size_t smem, int grid, cudaStream_t st) {
+    cudaError_t e = prepare_resident_kernels();
+    if (e != cudaSuccess) return e;
 #define RES_CASE(I, D_, NE_)                                                                                   \
     case I: {                                                                                                  \
-        if (variant) {                                                                                         \
-            auto k = resident_kernel<D_, NE_, 256>;                                                             \
-            cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);     \
-            if (e != cudaSuccess) return e;                                                                    \
-            k<<<grid, 256, smem, st>>>(d_sims, d_plans, n_plans, d_next, d_t3);                                \
-        } else {                                                                                               \
-            auto k = resident_kernel<D_, NE_, 512>;                                                             \
-            cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);     \
-            if (e != cudaSuccess) return e;                                                                    \
-            k<<<grid, 512, smem, st>>>(d_sims, d_plans, n_plans, d_next, d_t3);                                \
-        }                                                                                                      \
+        if (variant) resident_kernel<D_, NE_, 256><<<grid, 256, smem, st>>>(d_sims, d_plans, n_plans, d_next, d_t3); \
+        else resident_kernel<D_, NE_, 512><<<grid, 512, smem, st>>>(d_sims, d_plans, n_plans, d_next, d_t3);        \
         break;                                                                                                 \
     }
     switch (res_index(Dd, NEd)) {
@@ -575,20 +605,14 @@ cudaError_t launch_resident(int Dd, int NEd, int variant, SimDesc* d_sims, const
 
 cudaError_t resident_occupancy(int Dd, int NEd, int variant, size_t smem, int* blocks_per_sm) {
     *blocks_per_sm = 1;
+    cudaError_t e = prepare_resident_kernels();
+    if (e != cudaSuccess) return e;
 #define OCC_CASE(I, D_, NE_)                                                                                  \
-    case I: {                                                                                                 \
-        cudaError_t e;                                                                                        \
-        if (variant) {                                                                                        \
-            auto k = resident_kernel<D_, NE_, 256>;                                                            \
-            e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);               \
-            if (e != cudaSuccess) return e;                                                                   \
-            return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k, 256, smem);                \
-        }                                                                                                     \
-        auto k = resident_kernel<D_, NE_, 512>;                                                                \
-        e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);                   \
-        if (e != cudaSuccess) return e;                                                                       \
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k, 512, smem);                    \
-    }
+    case I:                                                                                                   \
+        return variant ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, resident_kernel<D_, NE_, 256>, \
+                                                                       256, smem)                               \
+                       : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, resident_kernel<D_, NE_, 512>, \
+                                                                       512, smem);
     switch (res_index(Dd, NEd)) {
         OCC_CASE(0, 2, 4)
         OCC_CASE(1, 2, 8)

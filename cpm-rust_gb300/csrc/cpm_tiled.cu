@@ -29,6 +29,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
 #include <type_traits>
 
 #include "cpm_common.h"
@@ -999,15 +1000,33 @@ size_t tiled_smem_bytes(int max_box, int n_cells, int cl_cap, int D) {
 }
 int tiled_block() { return TB; }
 
+// Shared-memory limit raised once per device before any launch (see
+// prepare_resident_kernels).
+cudaError_t prepare_tiled_kernels() {
+    static std::mutex mu;
+    static bool done[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    if (dev >= 0 && dev < 64 && done[dev]) return cudaSuccess;
+    const int smem = 227 * 1024 - 4096;
+    if ((e = cudaFuncSetAttribute(tiled_kernel<2, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) ||
+        (e = cudaFuncSetAttribute(tiled_kernel<2, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) ||
+        (e = cudaFuncSetAttribute(tiled_kernel<3, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) ||
+        (e = cudaFuncSetAttribute(tiled_kernel<3, 18>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) ||
+        (e = cudaFuncSetAttribute(tiled_kernel<3, 26>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)))
+        return e;
+    if (dev >= 0 && dev < 64) done[dev] = true;
+    return cudaSuccess;
+}
+
 cudaError_t tiled_occupancy(int D, int NE, size_t smem, int* per_sm) {
     *per_sm = 0;
-#define TOCC(I, D_, NE_)                                                                                   \
-    case I: {                                                                                              \
-        auto k = tiled_kernel<D_, NE_>;                                                                     \
-        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);     \
-        if (e != cudaSuccess) return e;                                                                    \
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k, TB, smem);                         \
-    }
+    cudaError_t e = prepare_tiled_kernels();
+    if (e != cudaSuccess) return e;
+#define TOCC(I, D_, NE_) \
+    case I: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, tiled_kernel<D_, NE_>, TB, smem);
     switch (tiled_index(D, NE)) {
         TOCC(0, 2, 4)
         TOCC(1, 2, 8)
@@ -1029,7 +1048,7 @@ cudaError_t launch_tiled(int D, int NE, SimDesc* d_sim, uint64_t n_mcs, const in
 #define TLAUNCH(I, D_, NE_)                                                                                 \
     case I: {                                                                                               \
         auto k = tiled_kernel<D_, NE_>;                                                                      \
-        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);      \
+        cudaError_t e = prepare_tiled_kernels();                                                            \
         if (e != cudaSuccess) return e;                                                                     \
         void* args[] = {(void*)&d_sim, (void*)&n_mcs, (void*)&tg, (void*)&bar, (void*)&d_claims, (void*)&d_t3, \
                         (void*)&max_box, (void*)&tables_in_smem, (void*)&barrier_extra, (void*)&cl_cap};   \

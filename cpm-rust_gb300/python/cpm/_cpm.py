@@ -63,6 +63,12 @@ STAT_NAMES = (
     "cycles_barrier_claim",
     "cycles_barrier_write",
     "exact_decisions",
+    "host_prep_us",
+    "device_us",
+    "host_read_us",
+    "cycles_res_build",
+    "cycles_res_resolve",
+    "host_place_us",
 )
 
 
