@@ -42,8 +42,8 @@ enum CpmStat {
     CPM_STAT_CYC_BAR_WRITE = 24, // tiled sweep: cycles waiting in the grid barrier after the write-back
     CPM_STAT_EXACT_DECISIONS = 25, // decisions the float bracket left to the FP64 computation
     CPM_STAT_HOST_PREP_US = 26,  // run/run_batch/run_many: microseconds of upload and launch
-    CPM_STAT_DEVICE_US = 27,     // microseconds waiting for the device
-    CPM_STAT_HOST_READ_US = 28,  // microseconds of read-back and host readouts
+    CPM_STAT_DEVICE_US = 27,     // microseconds from the launch to the end of the device work
+    CPM_STAT_HOST_READ_US = 28,  // microseconds of read-back and host readouts after the device work (they overlap it)
     CPM_STAT_CYC_RES_BUILD = 29,   // resident sweep: cycles building candidate lists (thread 0)
     CPM_STAT_CYC_RES_RESOLVE = 30, // resident sweep: cycles resolving them (thread 0)
     CPM_STAT_HOST_PLACE_US = 31,   // run_many: microseconds of validation and initial placement
@@ -124,6 +124,7 @@ struct SimDesc {
     int64_t* sample_sum_outer;      // n_samples * (n_cells+1) * D * D
     uint32_t* sample_lattice;       // n_samples * n_sites (unpadded) or null
     int32_t* error;                 // first error code (0 = none)
+    uint32_t* done_flag;            // optional (host-mapped): set to 1 when a run plan of this simulation ends
 };
 
 // One unit of device work: a whole run plan for one simulation, replaying

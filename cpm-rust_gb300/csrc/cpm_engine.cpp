@@ -86,6 +86,7 @@ void DeviceSims::dev_free(void* p) {
 }
 
 DeviceSims::~DeviceSims() {
+    if (done_host_) cudaFreeHost(done_host_);
     for (auto a : aux_) cudaStreamDestroy(a);
     for (auto e : joins_) cudaEventDestroy(e);
     if (ev_fork_) cudaEventDestroy(ev_fork_);
@@ -193,6 +194,12 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
     CUDA_TRY(dev_alloc((void**)&arena_, std::max<size_t>(cv.off, 256)));
     CUDA_TRY(dev_alloc((void**)&d_descs_, std::max<size_t>(N, 1) * sizeof(SimDesc)));
     CUDA_TRY(dev_alloc((void**)&d_next_, sizeof(int) * 16));
+    uint32_t* done_dev = nullptr;
+    if (track_done_) {
+        CUDA_TRY(cudaHostAlloc((void**)&done_host_, std::max<size_t>(N, 1) * 4, cudaHostAllocMapped));
+        std::memset(done_host_, 0, std::max<size_t>(N, 1) * 4);
+        CUDA_TRY(cudaHostGetDevicePointer((void**)&done_dev, done_host_, 0));
+    }
     device_bytes_ = std::max<size_t>(cv.off, 256) + std::max<size_t>(N, 1) * sizeof(SimDesc) + sizeof(int) * 16;
     (void)t3;
     // ---- host staging, then one upload per buffer
@@ -350,6 +357,7 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
         s.sample_sum_outer = (int64_t*)(base + o.sso);
         s.sample_lattice = lattice_samples ? (uint32_t*)(base + o.slat) : nullptr;
         s.error = (int32_t*)(base + o.err);
+        s.done_flag = done_dev ? done_dev + i : nullptr;
     };
     {
         const unsigned nthreads =
@@ -1003,22 +1011,44 @@ std::string run_many(const std::vector<Config>& configs, const std::vector<Initi
     }
     using clk = std::chrono::steady_clock;
     const auto t0 = clk::now();
+    // kernels on a non-blocking stream: the read-backs (legacy-stream copies
+    // from the assembly threads) then do not wait for them
+    cudaStream_t st = nullptr;
+    CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    struct StreamGuard {
+        cudaStream_t s;
+        ~StreamGuard() { if (s) cudaStreamDestroy(s); }
+    } guard{st};
     DeviceSims dev;
-    std::string err = dev.create(configs, initials, ns, ne, snapshots);
+    dev.set_done_tracking(true);
+    std::string err = dev.create(configs, initials, ns, ne, snapshots, st);
     if (!err.empty()) return err;
     err = dev.run(plans, device_grid);
     if (!err.empty()) return err;
     const auto t1 = clk::now();
-    err = dev.sync();
-    if (!err.empty()) return err;
-    const auto t2 = clk::now();
-    // ---- assemble results (host threads over simulations)
+    // ---- assemble results while the device runs: host threads take the
+    // simulations in the order the persistent launch serves them (largest
+    // first) and start on each as soon as its done flag is set, or once the
+    // stream has finished (simulations on other sweeps, or an error, which
+    // dev.sync() reports below)
+    std::vector<size_t> order(N);
+    for (size_t i = 0; i < N; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+        return dev.layout(a).g.n_sites > dev.layout(b).g.n_sites;
+    });
     std::atomic<size_t> next{0};
     std::vector<std::string> errs(N);
     auto worker = [&]() {
         for (;;) {
-            const size_t i = next.fetch_add(1);
-            if (i >= N) return;
+            const size_t k = next.fetch_add(1);
+            if (k >= N) return;
+            const size_t i = order[k];
+            while (!dev.done(i)) {
+                const cudaError_t q = cudaStreamQuery(st);
+                if (q != cudaErrorNotReady) break;
+                std::this_thread::sleep_for(std::chrono::microseconds(50));
+            }
+            if (!dev.done(i)) cudaStreamSynchronize(st);
             errs[i] = assemble_result(configs[i], initials[i], dev, i, ns[i], nt[i], ro, out[i]);
         }
     };
@@ -1029,7 +1059,11 @@ std::string run_many(const std::vector<Config>& configs, const std::vector<Initi
     std::vector<std::thread> th;
     for (unsigned t = 0; t < nthreads; ++t)
         th.emplace_back([&, dev_id] { cudaSetDevice(dev_id); worker(); });
+    cudaStreamSynchronize(st);  // errors are reported by dev.sync() below
+    const auto t2 = clk::now();
     for (auto& t : th) t.join();
+    err = dev.sync();
+    if (!err.empty()) return err;
     for (auto& e : errs) if (!e.empty()) return e;
     const auto t3 = clk::now();
     auto us = [](clk::duration d) { return (uint64_t)std::chrono::duration_cast<std::chrono::microseconds>(d).count(); };

@@ -83,6 +83,11 @@ class DeviceSims {
     void set_stream_ordered(bool on) { stream_ordered_ = on; }
     // Caps the grid of tiled launches (the trajectory does not depend on it).
     void set_tiled_grid_cap(int cap) { tiled_grid_cap_ = cap; }
+    // Before create(): host-mapped per-simulation flags the resident sweep
+    // sets when a simulation's run plan ends, so its read-back can start
+    // while others still run.
+    void set_done_tracking(bool on) { track_done_ = on; }
+    bool done(size_t i) const { return done_host_ && ((volatile uint32_t*)done_host_)[i] != 0u; }
 
    private:
     std::vector<SimLayout> layouts_;
@@ -104,6 +109,8 @@ class DeviceSims {
     size_t device_bytes_ = 0;
     bool stream_ordered_ = false;
     int tiled_grid_cap_ = 0;
+    bool track_done_ = false;
+    uint32_t* done_host_ = nullptr;  // pinned, mapped
     std::vector<cudaStream_t> aux_;  // further kernel groups of one run
     std::vector<cudaEvent_t> joins_;
     cudaEvent_t ev_fork_ = nullptr;

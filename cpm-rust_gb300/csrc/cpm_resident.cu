@@ -527,6 +527,12 @@ __global__ void __launch_bounds__(RB, 512 / RB) resident_kernel(SimDesc* sims, c
             sims[plan.sim].mcs = mcs;
         }
         __syncthreads();
+        if (tid == 0 && sd.done_flag) {
+            // every write of this plan (state, samples, counters) before the flag
+            __threadfence_system();
+            *(volatile uint32_t*)sd.done_flag = 1u;
+        }
+        __syncthreads();
     }
 }
 
