@@ -423,6 +423,70 @@ extern "C" int cpm_result_sample_read(const cpm_result* r, size_t s, const cpm_s
     return ok();
 }
 
+extern "C" int cpm_result_samples_sizes(const cpm_result* r, cpm_samples_sizes* o) {
+    if (!r || !o) return fail(CPM_E_ARG, "null argument");
+    std::memset(o, 0, sizeof *o);
+    o->n_samples = r->r.samples.size();
+    o->n_cells = r->r.cell_type_index.size();
+    for (const Sample& S : r->r.samples) {
+        o->total_contact += S.contact_a.size();
+        o->total_fragmented += S.fragmented.size();
+        o->total_medium += S.medium_volumes.size();
+        o->has_lattice |= S.has_lattice ? 1 : 0;
+    }
+    return ok();
+}
+
+extern "C" int cpm_result_samples_read(const cpm_result* r, const cpm_samples_out* o) {
+    if (!r || !o) return fail(CPM_E_ARG, "null argument");
+    const int D = r->r.D;
+    const size_t n = r->r.cell_type_index.size();
+    size_t nc = 0, nf = 0, nm = 0, site0 = 0;
+    for (size_t s = 0; s < r->r.samples.size(); ++s) {
+        const Sample& S = r->r.samples[s];
+        if (o->mcs) o->mcs[s] = S.mcs;
+        if (o->conservative_energy) o->conservative_energy[s] = S.energy;
+        for (size_t i = 0; i < S.cells.size() && i < n; ++i) {
+            const CellSample& c = S.cells[i];
+            const size_t k = s * n + i;
+            if (o->ids) o->ids[k] = c.id;
+            if (o->volume) o->volume[k] = c.volume;
+            if (o->interface) o->interface[k] = c.interface;
+            for (int d = 0; d < D; ++d) {
+                if (o->centroid) o->centroid[k * D + d] = c.centroid[d];
+                if (o->eigenvalues) o->eigenvalues[k * D + d] = c.eigenvalues[d];
+            }
+            if (o->radius_of_gyration_sq) o->radius_of_gyration_sq[k] = c.rg2;
+            if (o->kappa_sq) o->kappa_sq[k] = c.kappa2;
+        }
+        if (o->contact_offsets) o->contact_offsets[s] = nc;
+        for (size_t k = 0; k < S.contact_a.size(); ++k, ++nc) {
+            if (o->contact_a) o->contact_a[nc] = S.contact_a[k];
+            if (o->contact_b) o->contact_b[nc] = S.contact_b[k];
+            if (o->contact_count) o->contact_count[nc] = S.contact_n[k];
+        }
+        if (o->fragmented_offsets) o->fragmented_offsets[s] = nf;
+        if (o->fragmented_cells && !S.fragmented.empty())
+            std::memcpy(o->fragmented_cells + nf, S.fragmented.data(), S.fragmented.size() * 4);
+        nf += S.fragmented.size();
+        if (o->medium_offsets) o->medium_offsets[s] = nm;
+        if (o->medium_component_volumes && !S.medium_volumes.empty())
+            std::memcpy(o->medium_component_volumes + nm, S.medium_volumes.data(), S.medium_volumes.size() * 4);
+        if (o->medium_component_touches_boundary && !S.medium_touches.empty())
+            std::memcpy(o->medium_component_touches_boundary + nm, S.medium_touches.data(), S.medium_touches.size());
+        nm += S.medium_volumes.size();
+        if (o->lattice && S.has_lattice) {
+            std::memcpy(o->lattice + site0, S.lattice.data(), S.lattice.size() * 4);
+            site0 += S.lattice.size();
+        }
+    }
+    const size_t ns = r->r.samples.size();
+    if (o->contact_offsets) o->contact_offsets[ns] = nc;
+    if (o->fragmented_offsets) o->fragmented_offsets[ns] = nf;
+    if (o->medium_offsets) o->medium_offsets[ns] = nm;
+    return ok();
+}
+
 extern "C" int cpm_result_stats(const cpm_result* r, uint64_t* out32) {
     if (!r || !out32) return fail(CPM_E_ARG, "null argument");
     std::memset(out32, 0, 32 * sizeof(uint64_t));

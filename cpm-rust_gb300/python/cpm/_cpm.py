@@ -170,7 +170,7 @@ EXPORTED_SYMBOLS = (
     "cpm_builder_initial_state", "cpm_builder_hashes", "cpm_derive_seed_u64",
     "cpm_run_mcs_noalloc",
     "cpm_serve_start", "cpm_serve_submit", "cpm_serve_poll", "cpm_serve_wait", "cpm_serve_cancel",
-    "cpm_serve_stats_get", "cpm_serve_stop",
+    "cpm_serve_stats_get", "cpm_serve_stop", "cpm_result_samples_sizes", "cpm_result_samples_read",
 )
 
 
@@ -230,6 +230,8 @@ def _load():
     L.cpm_builder_hashes.argtypes = [_P, U64, U64, U64, _P, SZ, _P, SZ, ctypes.c_char_p, ctypes.c_char_p]
     L.cpm_derive_seed_u64.argtypes = [U64, U64]
     L.cpm_derive_seed_u64.restype = U64
+    L.cpm_result_samples_sizes.argtypes = [_P, _P]
+    L.cpm_result_samples_read.argtypes = [_P, _P]
     L.cpm_serve_start.argtypes = [_P, ctypes.POINTER(_P)]
     L.cpm_serve_submit.argtypes = [_P, _P, U64, U64, U64, I32, I32, ctypes.POINTER(U64)]
     L.cpm_serve_poll.argtypes = [_P, U64, ctypes.POINTER(I32), ctypes.POINTER(_P), _P]
@@ -329,6 +331,70 @@ class RunResult:
     __slots__ = ("metadata", "status", "samples", "cell_type_index", "cell_type_names", "stats", "used_default")
 
 
+class SamplesSizesC(ctypes.Structure):
+    _fields_ = [("n_samples", ctypes.c_uint64), ("n_cells", ctypes.c_uint64), ("total_contact", ctypes.c_uint64),
+                ("total_fragmented", ctypes.c_uint64), ("total_medium", ctypes.c_uint64),
+                ("has_lattice", ctypes.c_int32), ("pad", ctypes.c_int32)]
+
+
+class SamplesOutC(ctypes.Structure):
+    _fields_ = [(name, _P) for name in (
+        "mcs", "conservative_energy", "ids", "volume", "interface", "centroid", "eigenvalues",
+        "radius_of_gyration_sq", "kappa_sq", "contact_offsets", "contact_a", "contact_b", "contact_count",
+        "fragmented_offsets", "fragmented_cells", "medium_offsets", "medium_component_volumes",
+        "medium_component_touches_boundary", "lattice",
+    )]
+
+
+def _read_samples(h, ns, n, D, grid):
+    """Every sample of a result from one bulk read (cpm_result_samples_read);
+    each Sample's arrays are views into the per-result arrays."""
+    if ns == 0:
+        return []
+    sz = SamplesSizesC()
+    _check(_lib.cpm_result_samples_sizes(h, ctypes.byref(sz)))
+    a = {
+        "mcs": np.zeros(ns, np.uint64), "conservative_energy": np.zeros(ns, np.float64),
+        "ids": np.zeros((ns, n), np.uint32), "volume": np.zeros((ns, n), np.uint32),
+        "interface": np.zeros((ns, n), np.uint32), "centroid": np.zeros((ns, n, D), np.float64),
+        "eigenvalues": np.zeros((ns, n, D), np.float64), "radius_of_gyration_sq": np.zeros((ns, n), np.float64),
+        "kappa_sq": np.zeros((ns, n), np.float64), "contact_offsets": np.zeros(ns + 1, np.uint64),
+        "contact_a": np.zeros(int(sz.total_contact), np.uint32), "contact_b": np.zeros(int(sz.total_contact), np.uint32),
+        "contact_count": np.zeros(int(sz.total_contact), np.uint32), "fragmented_offsets": np.zeros(ns + 1, np.uint64),
+        "fragmented_cells": np.zeros(int(sz.total_fragmented), np.uint32), "medium_offsets": np.zeros(ns + 1, np.uint64),
+        "medium_component_volumes": np.zeros(int(sz.total_medium), np.uint32),
+        "medium_component_touches_boundary": np.zeros(int(sz.total_medium), np.uint8),
+    }
+    lat = np.zeros((ns,) + tuple(grid), np.uint32) if sz.has_lattice else None
+    o = SamplesOutC()
+    for name, arr in a.items():
+        setattr(o, name, arr.ctypes.data if arr.size else None)
+    o.lattice = lat.ctypes.data if lat is not None else None
+    _check(_lib.cpm_result_samples_read(h, ctypes.byref(o)))
+    co, fo, mo = a["contact_offsets"].tolist(), a["fragmented_offsets"].tolist(), a["medium_offsets"].tolist()
+    frag = a["fragmented_cells"].tolist()
+    mvol = a["medium_component_volumes"].tolist()
+    mtouch = [bool(x) for x in a["medium_component_touches_boundary"]]
+    mcs, en = a["mcs"].tolist(), a["conservative_energy"].tolist()
+    out = []
+    for s in range(ns):
+        smp = Sample()
+        smp.mcs = int(mcs[s])
+        smp.conservative_energy = float(en[s])
+        smp.ids, smp.volume, smp.interface = a["ids"][s], a["volume"][s], a["interface"][s]
+        smp.centroid, smp.eigenvalues = a["centroid"][s], a["eigenvalues"][s]
+        smp.radius_of_gyration_sq, smp.kappa_sq = a["radius_of_gyration_sq"][s], a["kappa_sq"][s]
+        smp.fragmented_cells = frag[fo[s]:fo[s + 1]]
+        smp.medium_component_volumes = mvol[mo[s]:mo[s + 1]]
+        smp.medium_component_touches_boundary = mtouch[mo[s]:mo[s + 1]]
+        smp.lattice = lat[s] if lat is not None else None
+        c0, c1 = co[s], co[s + 1]
+        smp._contact_pairs = (a["contact_a"][c0:c1], a["contact_b"][c0:c1], a["contact_count"][c0:c1])
+        smp._contact = None
+        out.append(smp)
+    return out
+
+
 def _result_from_handle(h) -> RunResult:
     try:
         info = ResultInfo()
@@ -361,48 +427,7 @@ def _result_from_handle(h) -> RunResult:
             names.append(buf.value.decode("utf-8"))
         stats = np.zeros(32, dtype=np.uint64)
         _check(_lib.cpm_result_stats(h, _ptr(stats)))
-        samples = []
-        for s in range(int(info.n_samples)):
-            sz = SampleSizes()
-            _check(_lib.cpm_result_sample_sizes(h, s, ctypes.byref(sz)))
-            mcs = np.zeros(1, dtype=np.uint64)
-            en = np.zeros(1, dtype=np.float64)
-            ids = np.zeros(n, dtype=np.uint32)
-            vol = np.zeros(n, dtype=np.uint32)
-            itf = np.zeros(n, dtype=np.uint32)
-            cen = np.zeros((n, D), dtype=np.float64)
-            eig = np.zeros((n, D), dtype=np.float64)
-            rg2 = np.zeros(n, dtype=np.float64)
-            k2 = np.zeros(n, dtype=np.float64)
-            ca = np.zeros(int(sz.n_contact), dtype=np.uint32)
-            cb = np.zeros(int(sz.n_contact), dtype=np.uint32)
-            cn = np.zeros(int(sz.n_contact), dtype=np.uint32)
-            fr = np.zeros(int(sz.n_fragmented), dtype=np.uint32)
-            mv = np.zeros(int(sz.n_medium), dtype=np.uint32)
-            mt = np.zeros(int(sz.n_medium), dtype=np.uint8)
-            lat = np.zeros(grid, dtype=np.uint32) if sz.has_lattice else None
-            o = SampleOut()
-            for name, arr in (("mcs", mcs), ("conservative_energy", en), ("ids", ids), ("volume", vol),
-                              ("interface", itf), ("centroid", cen), ("eigenvalues", eig),
-                              ("radius_of_gyration_sq", rg2), ("kappa_sq", k2), ("contact_a", ca),
-                              ("contact_b", cb), ("contact_count", cn), ("fragmented_cells", fr),
-                              ("medium_component_volumes", mv), ("medium_component_touches_boundary", mt)):
-                setattr(o, name, arr.ctypes.data if arr.size else None)
-            o.lattice = lat.ctypes.data if lat is not None else None
-            _check(_lib.cpm_result_sample_read(h, s, ctypes.byref(o)))
-            smp = Sample()
-            smp.mcs = int(mcs[0])
-            smp.conservative_energy = float(en[0])
-            smp.ids, smp.volume, smp.interface = ids, vol, itf
-            smp.centroid, smp.eigenvalues = cen, eig
-            smp.radius_of_gyration_sq, smp.kappa_sq = rg2, k2
-            smp.fragmented_cells = fr.tolist()
-            smp.medium_component_volumes = mv.tolist()
-            smp.medium_component_touches_boundary = [bool(x) for x in mt]
-            smp.lattice = lat
-            smp._contact_pairs = (ca, cb, cn)
-            smp._contact = None
-            samples.append(smp)
+        samples = _read_samples(h, int(info.n_samples), n, D, grid)
         r = RunResult()
         r.metadata, r.status, r.samples = meta, status, samples
         r.cell_type_index, r.cell_type_names = cti, names

@@ -153,6 +153,35 @@ int cpm_result_cell_type_index(const cpm_result* r, uint32_t* out /* n_cells */)
 int cpm_result_cell_type_name(const cpm_result* r, size_t type_index, char* buf, size_t capacity);
 int cpm_result_sample_sizes(const cpm_result* r, size_t sample, cpm_sample_sizes* out);
 int cpm_result_sample_read(const cpm_result* r, size_t sample, const cpm_sample_out* out);
+
+/* All samples of a result in one call (the same fields as
+ * cpm_result_sample_read, samples back to back): the fixed-size fields as
+ * n_samples x n_cells (x D) arrays, the variable-size ones concatenated with
+ * n_samples + 1 offsets, lattices as n_samples x N_sites when present. No
+ * reference counterpart (a bulk form of the per-sample accessors). */
+typedef struct {
+    uint64_t n_samples, n_cells;
+    uint64_t total_contact, total_fragmented, total_medium;
+    int32_t has_lattice;
+    int32_t pad;
+} cpm_samples_sizes;
+int cpm_result_samples_sizes(const cpm_result* r, cpm_samples_sizes* out);
+
+typedef struct {
+    uint64_t* mcs;
+    double* conservative_energy;
+    uint32_t *ids, *volume, *interface;
+    double *centroid, *eigenvalues, *radius_of_gyration_sq, *kappa_sq;
+    uint64_t* contact_offsets;
+    uint32_t *contact_a, *contact_b, *contact_count;
+    uint64_t* fragmented_offsets;
+    uint32_t* fragmented_cells;
+    uint64_t* medium_offsets;
+    uint32_t* medium_component_volumes;
+    uint8_t* medium_component_touches_boundary;
+    uint32_t* lattice;
+} cpm_samples_out;
+int cpm_result_samples_read(const cpm_result* r, const cpm_samples_out* out);
 /* Device counters of the run (order: attempts, non-null, topology
  * rejections, guard rejections, evaluated, accepted, conflict rounds, colour
  * passes, timeouts, fixpoint iterations, h2d bytes, d2h bytes, deferred
