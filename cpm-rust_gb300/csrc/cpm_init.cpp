@@ -276,15 +276,60 @@ std::string initialize(const Config& c, Initial& out) {
     Xoshiro256pp rng(c.seed);
     std::vector<std::array<int64_t, 3>> seeds;
     seeds.reserve(n);
+    // Seeds in buckets at least min_sep wide per axis: a seed closer than
+    // min_sep to a candidate lies in the candidate's bucket or a neighbouring
+    // one (wrapping on periodic axes), so only those are compared. The
+    // verdict and the draws are those of comparing against every seed.
+    int nbk[3] = {1, 1, 1};
+    bool bucketed = true;
+    for (int d = 0; d < c.D; ++d) {
+        nbk[d] = std::max<int64_t>(1, (int64_t)std::floor((double)P.g.dims[d] / std::max(min_sep, 1e-9)));
+        if (nbk[d] < 3) bucketed = false;
+    }
+    std::vector<std::vector<int>> buckets(bucketed ? (size_t)nbk[0] * nbk[1] * nbk[2] : 0);
+    auto bucket_of = [&](const int64_t* x, int* b) {
+        for (int d = 0; d < 3; ++d) b[d] = d < c.D ? (int)(x[d] * nbk[d] / P.g.dims[d]) : 0;
+    };
+    auto too_close = [&](const std::array<int64_t, 3>& cand) {
+        if (!bucketed) {
+            for (auto& q : seeds)
+                if (!(P.distance(q.data(), cand.data()) >= min_sep)) return true;
+            return false;
+        }
+        int b[3];
+        bucket_of(cand.data(), b);
+        for (int dz = c.D > 2 ? -1 : 0; dz <= (c.D > 2 ? 1 : 0); ++dz)
+            for (int dy = -1; dy <= 1; ++dy)
+                for (int dx = -1; dx <= 1; ++dx) {
+                    int q[3] = {b[0] + dx, b[1] + dy, b[2] + dz};
+                    bool skip = false;
+                    for (int d = 0; d < c.D; ++d) {
+                        if (q[d] < 0 || q[d] >= nbk[d]) {
+                            if (!P.g.periodic) { skip = true; break; }
+                            q[d] = (q[d] + nbk[d]) % nbk[d];
+                        }
+                    }
+                    if (skip) continue;
+                    for (int k : buckets[((size_t)q[0] * nbk[1] + q[1]) * nbk[2] + q[2]])
+                        if (!(P.distance(seeds[k].data(), cand.data()) >= min_sep)) return true;
+                }
+        return false;
+    };
     for (int s = 0; s < n; ++s) {
         bool placed = false;
         for (int a = 0; a < 20000; ++a) {
             std::array<int64_t, 3> cand{0, 0, 0};
             for (int d = 0; d < c.D; ++d) cand[d] = (int64_t)rng.range(0, (uint64_t)P.g.dims[d]);
-            bool far = true;
-            for (auto& q : seeds)
-                if (!(P.distance(q.data(), cand.data()) >= min_sep)) { far = false; break; }
-            if (far) { seeds.push_back(cand); placed = true; break; }
+            if (!too_close(cand)) {
+                seeds.push_back(cand);
+                if (bucketed) {
+                    int b[3];
+                    bucket_of(cand.data(), b);
+                    buckets[((size_t)b[0] * nbk[1] + b[1]) * nbk[2] + b[2]].push_back((int)seeds.size() - 1);
+                }
+                placed = true;
+                break;
+            }
         }
         if (!placed) {
             char buf[64];
