@@ -222,14 +222,18 @@ extern "C" int cpm_builder_run(const cpm_builder* b, uint64_t burn, uint64_t rea
     if (!msg.empty()) return fail(CPM_E_CONFIG, msg);
     if ((e = check_supported(c))) return e;
     Initial init;
+    const auto t0 = std::chrono::steady_clock::now();
     msg = initialize(c, init);
     if (!msg.empty()) return fail(CPM_E_INIT, msg);
+    const uint64_t place_us =
+        (uint64_t)std::chrono::duration_cast<std::chrono::microseconds>(std::chrono::steady_clock::now() - t0).count();
     ReadoutOptions ro;
     ro.include_lattice = include_lattice != 0;
     ro.topology = true;
     std::vector<Result> rs;
     msg = run_many({c}, {init}, ro, rs);
     if (!msg.empty()) return fail(code_for(msg), msg);
+    if (rs[0].stats.size() > CPM_STAT_HOST_PLACE_US) rs[0].stats[CPM_STAT_HOST_PLACE_US] = place_us;
     auto r = std::make_unique<cpm_result>();
     r->r = std::move(rs[0]);
     if (used_default) *used_default = init.used_default;
@@ -547,8 +551,8 @@ extern "C" int cpm_engine_create(const cpm_builder* const* builders, size_t n, v
     auto e = std::make_unique<cpm_engine>();
     int rc = prepare(builders, n, e->configs, e->initials, 1, 1, 1);
     if (rc) return rc;
-    std::vector<int> zeros(n, 0), ones(n, 1);
-    const std::string msg = e->sims.create(e->configs, e->initials, zeros, ones, false, (cudaStream_t)stream);
+    std::vector<int> ones(n, 1);  // one sample slot (with its lattice) for cpm_engine_take_sample
+    const std::string msg = e->sims.create(e->configs, e->initials, ones, ones, true, (cudaStream_t)stream);
     if (!msg.empty()) return fail(code_for(msg), msg);
     if (cudaMalloc(&e->d_energy, sizeof(double)) != cudaSuccess) return fail(CPM_E_CUDA, "cudaMalloc failed");
     *out = e.release();
@@ -594,6 +598,33 @@ extern "C" int cpm_engine_run_mcs(cpm_engine* e, uint64_t n) {
     }
     const std::string msg = e->sims.run(plans);
     if (!msg.empty()) return fail(code_for(msg), msg);
+    return ok();
+}
+
+extern "C" int cpm_engine_take_sample(cpm_engine* e, size_t i, int32_t include_lattice, cpm_result** out) {
+    if (bad_sim(e, i) || !out) return fail(CPM_E_ARG, "bad engine or simulation index");
+    DeviceSims& S = e->sims;
+    const SimLayout& L = S.layout(i);
+    cudaError_t ce = cpmgpu::launch_sample(L.g.D, S.device_desc(i), 0, 1, L.g.n_sites, S.stream());
+    if (ce == cudaSuccess)
+        ce = cpmgpu::launch_energy(L.g.D, L.NE, S.device_desc(i), S.host_desc(i).energy_out, S.stream());
+    if (ce != cudaSuccess) return fail(CPM_E_CUDA, std::string("CUDA error: ") + cudaGetErrorString(ce));
+    std::vector<std::vector<Topo>> topo;
+    std::string msg = S.topology({i}, {1}, topo);
+    if (msg.empty()) msg = S.sync();
+    ReadoutOptions ro;
+    ro.include_lattice = include_lattice != 0;
+    ro.topology = true;
+    Result R;
+    if (msg.empty()) msg = assemble_result(e->configs[i], e->initials[i], S, i, 1, 0, ro, R);
+    uint64_t mcs = 0;
+    if (msg.empty()) msg = S.read_mcs(i, mcs);
+    if (!msg.empty()) return fail(code_for(msg), msg);
+    R.samples[0].mcs = mcs;
+    attach_topology(e->configs[i], topo[0], R);
+    auto r = std::make_unique<cpm_result>();
+    r->r = std::move(R);
+    *out = r.release();
     return ok();
 }
 

@@ -46,7 +46,7 @@ enum CpmStat {
     CPM_STAT_HOST_READ_US = 28,  // microseconds of read-back and host readouts after the device work (they overlap it)
     CPM_STAT_CYC_RES_BUILD = 29,   // resident sweep: cycles building candidate lists (thread 0)
     CPM_STAT_CYC_RES_RESOLVE = 30, // resident sweep: cycles resolving them (thread 0)
-    CPM_STAT_HOST_PLACE_US = 31,   // run_many: microseconds of validation and initial placement
+    CPM_STAT_HOST_PLACE_US = 31,   // run/run_many: microseconds of validation and initial placement
     CPM_STAT_COUNT = 32
 };
 
@@ -140,6 +140,25 @@ struct RunPlan {
     uint64_t readout_chunks;       // == n_samples
     int32_t write_samples;
     int32_t write_lattice;
+};
+
+// One lattice snapshot for the device topology readouts (cpm_readout.cu):
+// the snapshot and the scratch the readouts of its simulation reuse from
+// sample to sample. `tri` and `ncomp` are zero on entry and left zero.
+struct ReadoutItem {
+    const uint32_t* lat;  // n_sites, interior, last axis fastest
+    uint32_t* parent;     // n_sites: union-find forest
+    uint32_t* aux;        // n_sites: medium component volume at its root, bit 31 = touches a fixed boundary
+    uint32_t* tri;        // n_cells * (n_cells + 1) / 2: contact counts of the pairs a < b, row-major
+    uint32_t* ncomp;      // n_cells + 1: von Neumann components per cell id
+    int64_t n_sites;
+    int64_t tri_n;
+    int32_t dims[3];
+    int32_t D;
+    int32_t periodic;
+    int32_t n_cells;
+    int32_t energy_maxnz;  // energy stencil = offsets in {-1,0,1}^D with 1..energy_maxnz nonzero components
+    int32_t pad;
 };
 
 // Per-move record of the parity harness (same layout as the oracle's).

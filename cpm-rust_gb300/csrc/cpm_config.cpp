@@ -3,10 +3,12 @@
 // Error texts follow the reference word for word, because callers match on
 // them (tests/python/test_errors.py:8-51): config.rs:287-413,
 // cell.rs:40-65, builder.rs:35-96, theta.rs:93-147, batch.rs:26-45.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <sstream>
+#include <thread>
 
 #include "cpm_host.h"
 
@@ -256,7 +258,12 @@ void b3_chunk(const uint8_t* p, size_t n, uint64_t idx, bool root, uint32_t out[
     }
     std::memcpy(out, h, 32);
 }
-void b3_tree(const uint8_t* data, size_t len, uint64_t first, uint64_t count, bool root, uint32_t out[8]) {
+// Subtrees of at least this many chunks split their halves over two threads
+// (up to `spawn` levels deep): the tree's halves are independent.
+constexpr uint64_t B3_PAR_CHUNKS = 512;
+
+void b3_tree(const uint8_t* data, size_t len, uint64_t first, uint64_t count, bool root, uint32_t out[8],
+             int spawn = 0) {
     if (count == 1) {
         const size_t off = first * 1024;
         b3_chunk(data + off, len - off < 1024 ? len - off : 1024, first, root, out);
@@ -265,8 +272,14 @@ void b3_tree(const uint8_t* data, size_t len, uint64_t first, uint64_t count, bo
     uint64_t left = 1;
     while (left * 2 < count) left *= 2;
     uint32_t l[8], r[8];
-    b3_tree(data, len, first, left, false, l);
-    b3_tree(data, len, first + left, count - left, false, r);
+    if (spawn > 0 && count >= B3_PAR_CHUNKS) {
+        std::thread t([&] { b3_tree(data, len, first, left, false, l, spawn - 1); });
+        b3_tree(data, len, first + left, count - left, false, r, spawn - 1);
+        t.join();
+    } else {
+        b3_tree(data, len, first, left, false, l, spawn);
+        b3_tree(data, len, first + left, count - left, false, r, spawn);
+    }
     uint8_t blk[64];
     for (int i = 0; i < 8; ++i)
         for (int b = 0; b < 4; ++b) { blk[4 * i + b] = (uint8_t)(l[i] >> (8 * b)); blk[32 + 4 * i + b] = (uint8_t)(r[i] >> (8 * b)); }
@@ -276,7 +289,9 @@ void b3_tree(const uint8_t* data, size_t len, uint64_t first, uint64_t count, bo
 
 void blake3(const uint8_t* data, size_t len, uint8_t out[32]) {
     uint32_t h[8];
-    b3_tree(data, len, 0, len == 0 ? 1 : (len + 1023) / 1024, true, h);
+    int spawn = 0;
+    for (unsigned hw = std::thread::hardware_concurrency(); hw > 1 && spawn < 5; hw >>= 1) ++spawn;
+    b3_tree(data, len, 0, len == 0 ? 1 : (len + 1023) / 1024, true, h, spawn);
     for (int i = 0; i < 8; ++i)
         for (int b = 0; b < 4; ++b) out[4 * i + b] = (uint8_t)(h[i] >> (8 * b));
 }
@@ -311,10 +326,54 @@ static void json_str(std::string& o, const std::string& s) {
     }
     o += '"';
 }
+// Decimal digits of x at q; returns the end.
+static inline char* put_uint(char* q, uint64_t x) {
+    static const struct Pairs {
+        char d[200];
+        Pairs() { for (int i = 0; i < 100; ++i) { d[2 * i] = (char)('0' + i / 10); d[2 * i + 1] = (char)('0' + i % 10); } }
+    } P;
+    char tmp[20];
+    int k = 20;
+    while (x >= 100) {
+        const unsigned r = (unsigned)(x % 100);
+        x /= 100;
+        k -= 2;
+        std::memcpy(tmp + k, P.d + 2 * r, 2);
+    }
+    if (x >= 10) { k -= 2; std::memcpy(tmp + k, P.d + 2 * x, 2); }
+    else tmp[--k] = (char)('0' + x);
+    std::memcpy(q, tmp + k, (size_t)(20 - k));
+    return q + (20 - k);
+}
+
+// A JSON array of unsigned integers; large arrays are formatted in parallel
+// segments and joined.
 template <class T>
 static void json_uints(std::string& o, const std::vector<T>& v) {
+    const size_t n = v.size();
+    const size_t hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t parts = n >= (1u << 17) ? std::min<size_t>(hw, n >> 15) : 1;
+    std::vector<std::string> seg(parts);
+    auto fmt = [&](size_t p) {
+        const size_t a = n * p / parts, b = n * (p + 1) / parts;
+        std::string& s = seg[p];
+        s.resize((b - a) * 21);
+        char* q = &s[0];
+        for (size_t i = a; i < b; ++i) {
+            if (i) *q++ = ',';
+            q = put_uint(q, (uint64_t)v[i]);
+        }
+        s.resize((size_t)(q - s.data()));
+    };
+    std::vector<std::thread> th;
+    for (size_t p = 1; p < parts; ++p) th.emplace_back(fmt, p);
+    fmt(0);
+    for (auto& t : th) t.join();
+    size_t len = 2;
+    for (auto& s : seg) len += s.size();
+    o.reserve(o.size() + len);
     o += '[';
-    for (size_t i = 0; i < v.size(); ++i) { if (i) o += ','; o += std::to_string(v[i]); }
+    for (auto& s : seg) o += s;
     o += ']';
 }
 static std::string hex32(const uint8_t d[32]) {
@@ -368,7 +427,12 @@ std::string convention_hash(const Config& c) {
 
 // ModelHashView (config.rs:463-556).
 std::string model_hash(const Config& c, const std::vector<uint32_t>& lattice, const std::vector<uint32_t>& type_of) {
-    std::string o = "{\"convention_hash\":\"" + convention_hash(c) + "\",\"lattice\":";
+    return model_hash_with(convention_hash(c), lattice, type_of);
+}
+
+std::string model_hash_with(const std::string& conv, const std::vector<uint32_t>& lattice,
+                            const std::vector<uint32_t>& type_of) {
+    std::string o = "{\"convention_hash\":\"" + conv + "\",\"lattice\":";
     json_uints(o, lattice);
     o += ",\"cell_type_of\":";
     json_uints(o, type_of);

@@ -645,6 +645,185 @@ std::string DeviceSims::read_mcs(size_t i, uint64_t& mcs) const {
     return "";
 }
 
+// ---- topology readouts on the device (cpm_readout.cu) ----
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Energy stencil of a simulation as the readout kernels take it: offsets in
+// {-1,0,1}^D with at most this many nonzero components.
+static int energy_maxnz(int D, int NE) {
+    if (NE == 2 * D) return 1;  // von Neumann
+    if (NE == 18) return 2;     // Eighteen
+    return D;                   // Moore (2D), TwentySix (3D)
+}
+
+static uint64_t readout_units(int64_t n_sites, int n_cells) {
+    const uint64_t n = (uint64_t)n_cells, tri = n * (n + 1) / 2, U = (uint64_t)cpmgpu::readout_unit();
+    const uint64_t span = std::max<uint64_t>({(uint64_t)n_sites, tri, n + 1});
+    return (span + U - 1) / U;
+}
+
+static size_t readout_scratch(int64_t n_sites, int n_cells) {
+    const uint64_t n = (uint64_t)n_cells;
+    return align256((size_t)n_sites * 8) + align256(n * (n + 1) / 2 * 4) + align256((n + 1) * 4);
+}
+
+size_t topology_bytes(int64_t n_sites, int n_cells) {
+    // scratch, unit counters and offsets, and room for the output streams
+    return readout_scratch(n_sites, n_cells) + readout_units(n_sites, n_cells) * 36 + (size_t)n_sites * 4 +
+           (size_t)n_cells * 64 + 4096;
+}
+
+std::string DeviceSims::topology(const std::vector<size_t>& sims, const std::vector<int>& ns,
+                                 std::vector<std::vector<Topo>>& out) {
+    const size_t M = sims.size();
+    out.assign(M, {});
+    int max_ns = 0;
+    for (size_t m = 0; m < M; ++m) {
+        out[m].resize((size_t)std::max(0, ns[m]));
+        max_ns = std::max(max_ns, ns[m]);
+    }
+    if (max_ns <= 0) return "";
+    std::vector<size_t> base(M);
+    std::vector<int64_t> units(M);
+    size_t total = 0;
+    int64_t all_units = 0;
+    for (size_t m = 0; m < M; ++m) {
+        const size_t i = sims[m];
+        const SimLayout& L = layouts_[i];
+        if (ns[m] > 0 && !descs_[i].sample_lattice) return "topology readouts need the lattice samples";
+        if (L.g.n_sites >= ((int64_t)1 << 31)) return "lattice too large for the topology readouts (2^31 sites)";
+        base[m] = total;
+        total += readout_scratch(L.g.n_sites, L.n_cells);
+        units[m] = (int64_t)readout_units(L.g.n_sites, L.n_cells);
+        all_units += units[m];
+    }
+    struct Buf {
+        DeviceSims* d;
+        void* p = nullptr;
+        size_t cap = 0;
+        ~Buf() { if (p) d->dev_free(p); }
+        cudaError_t reserve(size_t need) {
+            if (need <= cap) return cudaSuccess;
+            if (p) d->dev_free(p);
+            p = nullptr;
+            cap = 0;
+            const cudaError_t e = d->dev_alloc(&p, need);
+            if (e == cudaSuccess) cap = need;
+            return e;
+        }
+    };
+    Buf scratch{this}, d_items{this}, d_prefix{this}, d_cnt{this}, d_off{this}, d_pairs{this}, d_med{this},
+        d_frag{this};
+    CUDA_TRY(scratch.reserve(std::max<size_t>(total, 256)));
+    CUDA_TRY(cudaMemsetAsync(scratch.p, 0, total, stream_));  // contact tables and component counts start at zero
+    CUDA_TRY(d_items.reserve(M * sizeof(ReadoutItem)));
+    CUDA_TRY(d_prefix.reserve((M + 1) * 8));
+    CUDA_TRY(d_cnt.reserve((size_t)std::max<int64_t>(all_units, 1) * 12));
+    CUDA_TRY(d_off.reserve((size_t)std::max<int64_t>(all_units, 1) * 24));
+    std::vector<ReadoutItem> items;
+    std::vector<int64_t> prefix;
+    std::vector<size_t> who;
+    std::vector<uint32_t> cnt, h_pairs, h_med, h_frag;
+    std::vector<uint64_t> off;
+    for (int s = 0; s < max_ns; ++s) {
+        items.clear();
+        who.clear();
+        prefix.assign(1, 0);
+        for (size_t m = 0; m < M; ++m) {
+            if (ns[m] <= s) continue;
+            const size_t i = sims[m];
+            const SimLayout& L = layouts_[i];
+            const uint64_t n = (uint64_t)L.n_cells, tri = n * (n + 1) / 2;
+            char* b = (char*)scratch.p + base[m];
+            ReadoutItem it;
+            std::memset(&it, 0, sizeof it);
+            it.lat = descs_[i].sample_lattice + (size_t)s * (size_t)L.g.n_sites;
+            it.parent = (uint32_t*)b;
+            it.aux = (uint32_t*)b + L.g.n_sites;
+            it.tri = (uint32_t*)(b + align256((size_t)L.g.n_sites * 8));
+            it.ncomp = (uint32_t*)(b + align256((size_t)L.g.n_sites * 8) + align256(tri * 4));
+            it.n_sites = L.g.n_sites;
+            it.tri_n = (int64_t)tri;
+            for (int d = 0; d < 3; ++d) it.dims[d] = d < L.g.D ? (int32_t)L.g.dims[d] : 1;
+            it.D = L.g.D;
+            it.periodic = L.g.periodic ? 1 : 0;
+            it.n_cells = L.n_cells;
+            it.energy_maxnz = energy_maxnz(L.g.D, L.NE);
+            items.push_back(it);
+            who.push_back(m);
+            prefix.push_back(prefix.back() + units[m]);
+        }
+        const int K = (int)items.size();
+        const int64_t T = prefix.back();
+        CUDA_TRY(cudaMemcpyAsync(d_items.p, items.data(), K * sizeof(ReadoutItem), cudaMemcpyHostToDevice, stream_));
+        CUDA_TRY(cudaMemcpyAsync(d_prefix.p, prefix.data(), (K + 1) * 8, cudaMemcpyHostToDevice, stream_));
+        CUDA_TRY(cudaMemsetAsync(d_cnt.p, 0, (size_t)T * 12, stream_));
+        const ReadoutItem* di = (const ReadoutItem*)d_items.p;
+        const int64_t* dp = (const int64_t*)d_prefix.p;
+        for (int pass = 0; pass < 4; ++pass)
+            CUDA_TRY(cpmgpu::launch_readout(pass, di, K, dp, T, (uint32_t*)d_cnt.p, nullptr, nullptr, nullptr,
+                                            nullptr, stream_));
+        cnt.resize((size_t)T * 3);
+        CUDA_TRY(cudaMemcpyAsync(cnt.data(), d_cnt.p, (size_t)T * 12, cudaMemcpyDeviceToHost, stream_));
+        CUDA_TRY(cudaStreamSynchronize(stream_));
+        off.resize((size_t)T * 3);
+        uint64_t acc[3] = {0, 0, 0};
+        for (int64_t u = 0; u < T; ++u)
+            for (int k = 0; k < 3; ++k) {
+                off[3 * u + k] = acc[k];
+                acc[k] += cnt[3 * u + k];
+            }
+        CUDA_TRY(d_pairs.reserve(std::max<size_t>(acc[0] * 12, 16)));
+        CUDA_TRY(d_med.reserve(std::max<size_t>(acc[1] * 4, 16)));
+        CUDA_TRY(d_frag.reserve(std::max<size_t>(acc[2] * 4, 16)));
+        CUDA_TRY(cudaMemcpyAsync(d_off.p, off.data(), (size_t)T * 24, cudaMemcpyHostToDevice, stream_));
+        CUDA_TRY(cpmgpu::launch_readout(4, di, K, dp, T, nullptr, (const uint64_t*)d_off.p, (uint32_t*)d_pairs.p,
+                                        (uint32_t*)d_med.p, (uint32_t*)d_frag.p, stream_));
+        h_pairs.resize(acc[0] * 3);
+        h_med.resize(acc[1]);
+        h_frag.resize(acc[2]);
+        if (acc[0]) CUDA_TRY(cudaMemcpyAsync(h_pairs.data(), d_pairs.p, acc[0] * 12, cudaMemcpyDeviceToHost, stream_));
+        if (acc[1]) CUDA_TRY(cudaMemcpyAsync(h_med.data(), d_med.p, acc[1] * 4, cudaMemcpyDeviceToHost, stream_));
+        if (acc[2]) CUDA_TRY(cudaMemcpyAsync(h_frag.data(), d_frag.p, acc[2] * 4, cudaMemcpyDeviceToHost, stream_));
+        CUDA_TRY(cudaStreamSynchronize(stream_));
+        d2h_bytes_ += (size_t)T * 12 + acc[0] * 12 + acc[1] * 4 + acc[2] * 4;
+        h2d_bytes_ += (size_t)K * sizeof(ReadoutItem) + (size_t)(K + 1) * 8 + (size_t)T * 24;
+        auto split = [&](int k) {
+            Topo& t = out[who[k]][s];
+            const int64_t ua = prefix[k], ub = prefix[k + 1];
+            auto lo = [&](int st) { return off[3 * ua + st]; };
+            auto hi = [&](int st) { return ub < T ? off[3 * ub + st] : acc[st]; };
+            const size_t np = hi(0) - lo(0);
+            t.contact_a.resize(np);
+            t.contact_b.resize(np);
+            t.contact_n.resize(np);
+            for (size_t q = 0; q < np; ++q) {
+                const uint32_t* e = &h_pairs[3 * (lo(0) + q)];
+                t.contact_a[q] = e[0];
+                t.contact_b[q] = e[1];
+                t.contact_n[q] = e[2];
+            }
+            for (uint64_t q = lo(1); q < hi(1); ++q) {
+                t.medium_volumes.push_back(h_med[q] & 0x7FFFFFFFu);
+                t.medium_touches.push_back((uint8_t)(h_med[q] >> 31));
+            }
+            t.fragmented.assign(h_frag.begin() + lo(2), h_frag.begin() + hi(2));
+        };
+        const int nth = (int)std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()), (unsigned)(K + 63) / 64);
+        if (nth <= 1) {
+            for (int k = 0; k < K; ++k) split(k);
+        } else {
+            std::atomic<int> nx{0};
+            auto run = [&] { for (int k; (k = nx.fetch_add(1)) < K;) split(k); };
+            std::vector<std::thread> th;
+            for (int t = 1; t < nth; ++t) th.emplace_back(run);
+            run();
+            for (auto& t : th) t.join();
+        }
+    }
+    return "";
+}
+
 std::string DeviceSims::write_state(size_t i, const std::vector<uint32_t>& padded, const std::vector<uint32_t>& vol,
                                     const std::vector<uint32_t>& itf, const std::vector<int64_t>* sp,
                                     const std::vector<int64_t>* so) {
@@ -706,120 +885,6 @@ static void cell_summary(int D, uint32_t id, uint32_t vol, uint32_t itf, const i
     o.kappa2 = sum > 0.0 ? (dd / (dd - 1.0)) * (sq / (sum * sum)) - 1.0 / (dd - 1.0) : 0.0;
     o.rg2 = sum;
     for (int i = 0; i < D; ++i) o.eigenvalues[i] = e[i];
-}
-
-// Contact graph (state.rs:127-157) and labelling (labelling.rs:70-154) of
-// one lattice snapshot.
-// Per-geometry tables of the topology readouts: canon[f] = the interior
-// padded index a padded index f stands for (itself inside, its periodic image
-// in a periodic halo, -1 in a fixed halo), and the stencils as flat offsets.
-struct TopoGeom {
-    std::vector<int32_t> canon;
-    std::vector<int64_t> eoff, coff, moff;
-};
-
-static TopoGeom topo_geom(const Config& c, const Geometry& g) {
-    TopoGeom t;
-    const int D = c.D;
-    auto offs = [&](int kind) {
-        std::vector<int64_t> v;
-        for (auto& o : stencil(kind, D)) v.push_back(o[0] * g.strides[0] + o[1] * g.strides[1] + o[2] * g.strides[2]);
-        return v;
-    };
-    t.eoff = offs(c.energy_nbh);
-    t.coff = offs(NBH_VON_NEUMANN);
-    t.moff = offs(D == 2 ? NBH_MOORE : NBH_TWENTY_SIX);
-    t.canon.assign((size_t)g.n_padded, -1);
-    int64_t p[3] = {0, 0, 0};
-    for (int64_t f = 0; f < g.n_padded; ++f) {
-        bool ok = true;
-        int64_t ic[3] = {0, 0, 0};
-        for (int d = 0; d < D; ++d) {
-            const int64_t q = p[d];
-            if (q == 0 || q == g.pdims[d] - 1) {
-                if (!g.periodic) { ok = false; break; }
-                ic[d] = q == 0 ? g.dims[d] - 1 : 0;
-            } else {
-                ic[d] = q - 1;
-            }
-        }
-        if (ok) t.canon[f] = (int32_t)g.flat(ic);
-        for (int d = D - 1; d >= 0; --d) { if (++p[d] < g.pdims[d]) break; p[d] = 0; }
-    }
-    return t;
-}
-
-// Contact graph and labelling of one sample (output.rs:304-337 with
-// labelling.rs:70-154): each unordered pair of energy-neighbouring sites of
-// different cells counted once, as (min, max) pairs in ascending order; the
-// cells with more than one von Neumann component; the medium's components
-// under the full stencil with their volumes and whether they touch a fixed
-// boundary.
-static void topology_readouts(const Config& c, const Geometry& g, const TopoGeom& tg,
-                              const std::vector<uint32_t>& padded, int n_cells, Sample& smp) {
-    const int D = c.D;
-    // contact: canonical pair keys, sorted and counted (the order std::map would give)
-    std::vector<uint64_t> keys;
-    keys.reserve((size_t)g.n_sites * tg.eoff.size() / 4 + 16);
-    int64_t x[3] = {0, 0, 0};
-    for (int64_t s = 0; s < g.n_sites; ++s) {
-        const int64_t i = g.flat(x);
-        const uint32_t ic = padded[i];
-        for (int64_t off : tg.eoff) {
-            const int64_t j = i + off;
-            const int32_t key = tg.canon[j];
-            if (key >= 0 && key <= i) continue;
-            const uint32_t jc = padded[j];
-            if (jc == ic) continue;
-            const uint32_t a = std::min(ic, jc), b = std::max(ic, jc);
-            keys.push_back(((uint64_t)a << 32) | b);
-        }
-        for (int d = D - 1; d >= 0; --d) { if (++x[d] < g.dims[d]) break; x[d] = 0; }
-    }
-    std::sort(keys.begin(), keys.end());
-    for (size_t k = 0; k < keys.size();) {
-        size_t e = k + 1;
-        while (e < keys.size() && keys[e] == keys[k]) ++e;
-        smp.contact_a.push_back((uint32_t)(keys[k] >> 32));
-        smp.contact_b.push_back((uint32_t)keys[k]);
-        smp.contact_n.push_back((uint32_t)(e - k));
-        k = e;
-    }
-    // labelling
-    std::vector<char> vis((size_t)g.n_padded, 0);
-    std::vector<uint32_t> comps(n_cells + 1, 0);
-    std::vector<int64_t> q;
-    x[0] = x[1] = x[2] = 0;
-    for (int64_t s = 0; s < g.n_sites; ++s) {
-        const int64_t seed = g.flat(x);
-        for (int d = D - 1; d >= 0; --d) { if (++x[d] < g.dims[d]) break; x[d] = 0; }
-        if (vis[seed]) continue;
-        const uint32_t owner = padded[seed];
-        const std::vector<int64_t>& of = owner == 0 ? tg.moff : tg.coff;
-        vis[seed] = 1;
-        q.assign(1, seed);
-        uint32_t vol = 0;
-        bool touches = false;
-        while (!q.empty()) {
-            const int64_t site = q.back();
-            q.pop_back();
-            ++vol;
-            for (int64_t off : of) {
-                const int32_t cn = tg.canon[site + off];
-                if (cn < 0) {  // fixed boundary
-                    if (owner == 0) touches = true;
-                    continue;
-                }
-                if (vis[cn] || padded[cn] != owner) continue;
-                vis[cn] = 1;
-                q.push_back(cn);
-            }
-        }
-        if (owner == 0) { smp.medium_volumes.push_back(vol); smp.medium_touches.push_back(touches); }
-        else comps[owner] += 1;
-    }
-    for (int id = 1; id <= n_cells; ++id)
-        if (comps[id] > 1) smp.fragmented.push_back((uint32_t)id);
 }
 
 // output.rs:388-420
@@ -925,7 +990,6 @@ RunPlan plan_for(const Config& c, int sim, bool write_lattice) {
 // topology readouts, the status, the metadata hashes and the counters.
 std::string assemble_result(const Config& c, const Initial& init, const DeviceSims& dev, size_t i, int ns, int nt,
                             const ReadoutOptions& ro, Result& R) {
-    const bool snapshots = ro.include_lattice || ro.topology;
     const SimLayout& L = dev.layout(i);
     R = Result();
     R.D = c.D;
@@ -936,7 +1000,7 @@ std::string assemble_result(const Config& c, const Initial& init, const DeviceSi
     std::vector<uint32_t> sv, si, slat;
     std::vector<int64_t> ssp, sso;
     std::vector<double> energy;
-    std::string e = dev.read_samples(i, ns, sv, si, ssp, sso, snapshots ? &slat : nullptr);
+    std::string e = dev.read_samples(i, ns, sv, si, ssp, sso, ro.include_lattice ? &slat : nullptr);
     if (e.empty()) e = dev.read_energy(i, energy);
     if (e.empty()) e = dev.read_stats(i, R.stats);
     std::vector<uint32_t> fin;
@@ -946,7 +1010,6 @@ std::string assemble_result(const Config& c, const Initial& init, const DeviceSi
     const size_t n1 = (size_t)n + 1;
     std::vector<double> trace(energy.begin(), energy.begin() + nt);
     R.samples.resize(ns);
-    TopoGeom tg;
     for (int s = 0; s < ns; ++s) {
         Sample& S = R.samples[s];
         S.mcs = c.burn_in + (uint64_t)(s + 1) * c.interval;
@@ -955,17 +1018,13 @@ std::string assemble_result(const Config& c, const Initial& init, const DeviceSi
         for (int id = 1; id <= n; ++id)
             cell_summary(D, (uint32_t)id, sv[s * n1 + id], si[s * n1 + id], &ssp[(s * n1 + id) * D],
                          &sso[(s * n1 + id) * D * D], S.cells[id - 1]);
-        if (snapshots) {
-            std::vector<uint32_t> interior(slat.begin() + (size_t)s * L.g.n_sites,
-                                           slat.begin() + (size_t)(s + 1) * L.g.n_sites);
-            if (ro.topology) {
-                if (tg.canon.empty()) tg = topo_geom(c, L.g);
-                topology_readouts(c, L.g, tg, pad_lattice(L.g, interior), n, S);
-            }
-            if (ro.include_lattice) { S.lattice = std::move(interior); S.has_lattice = true; }
+        if (ro.include_lattice) {
+            S.lattice.assign(slat.begin() + (size_t)s * L.g.n_sites, slat.begin() + (size_t)(s + 1) * L.g.n_sites);
+            S.has_lattice = true;
         }
     }
-    R.status = status_of(c, trace, R.samples, n, ro.topology);
+    if (!ro.topology) R.status = status_of(c, trace, R.samples, n, false);
+    R.energy_trace = std::move(trace);
     // metadata (output.rs:66-78): hashes of the final state
     std::vector<uint32_t> fin_int((size_t)L.g.n_sites);
     int64_t x[3] = {0, 0, 0};
@@ -982,12 +1041,26 @@ std::string assemble_result(const Config& c, const Initial& init, const DeviceSi
     R.metadata.cpm_version = "0.2.0+gb300";
     R.metadata.convention_version = 1;
     R.metadata.convention_hash = convention_hash(c);
-    R.metadata.model_hash = model_hash(c, fin_int, init.type_of);
+    R.metadata.model_hash = model_hash_with(R.metadata.convention_hash, fin_int, init.type_of);
     R.metadata.seed = c.seed;
     R.metadata.seed_policy = "independent";
     R.metadata.derived_phi = (double)(uint32_t)occupied / (double)L.g.n_sites;
     R.metadata.theta_layout_version = 1;
     return "";
+}
+
+void attach_topology(const Config& c, std::vector<Topo>& topo, Result& R) {
+    for (size_t s = 0; s < R.samples.size() && s < topo.size(); ++s) {
+        Sample& S = R.samples[s];
+        Topo& t = topo[s];
+        S.contact_a = std::move(t.contact_a);
+        S.contact_b = std::move(t.contact_b);
+        S.contact_n = std::move(t.contact_n);
+        S.fragmented = std::move(t.fragmented);
+        S.medium_volumes = std::move(t.medium_volumes);
+        S.medium_touches = std::move(t.medium_touches);
+    }
+    R.status = status_of(c, R.energy_trace, R.samples, (int)R.cell_type_index.size(), true);
 }
 
 std::string run_many(const std::vector<Config>& configs, const std::vector<Initial>& initials, const ReadoutOptions& ro,
@@ -1059,12 +1132,31 @@ std::string run_many(const std::vector<Config>& configs, const std::vector<Initi
     std::vector<std::thread> th;
     for (unsigned t = 0; t < nthreads; ++t)
         th.emplace_back([&, dev_id] { cudaSetDevice(dev_id); worker(); });
+    // topology readouts on the device, queued behind the sweeps
+    std::vector<std::vector<Topo>> topo;
+    std::string terr;
+    if (ro.topology) {
+        std::vector<size_t> all(N);
+        for (size_t i = 0; i < N; ++i) all[i] = i;
+        terr = dev.topology(all, ns, topo);
+    }
     cudaStreamSynchronize(st);  // errors are reported by dev.sync() below
     const auto t2 = clk::now();
     for (auto& t : th) t.join();
     err = dev.sync();
     if (!err.empty()) return err;
+    if (!terr.empty()) return terr;
     for (auto& e : errs) if (!e.empty()) return e;
+    if (ro.topology) {
+        std::atomic<size_t> nx{0};
+        auto attach = [&]() {
+            for (size_t i; (i = nx.fetch_add(1)) < N;) attach_topology(configs[i], topo[i], out[i]);
+        };
+        std::vector<std::thread> ta;
+        for (unsigned t = 1; t < nthreads; ++t) ta.emplace_back(attach);
+        attach();
+        for (auto& t : ta) t.join();
+    }
     const auto t3 = clk::now();
     auto us = [](clk::duration d) { return (uint64_t)std::chrono::duration_cast<std::chrono::microseconds>(d).count(); };
     for (auto& R : out) {

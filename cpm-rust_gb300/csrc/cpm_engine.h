@@ -27,6 +27,16 @@ struct SimLayout {
     bool lattice_samples = false;
 };
 
+// Topology readouts of one sample (output.rs:304-337): the contact graph as
+// (a < b, count) in ascending order, fragmented cell ids in ascending order,
+// medium components in discovery order.
+struct Topo {
+    std::vector<uint32_t> contact_a, contact_b, contact_n;
+    std::vector<uint32_t> fragmented;
+    std::vector<uint32_t> medium_volumes;
+    std::vector<uint8_t> medium_touches;
+};
+
 class DeviceSims {
    public:
     DeviceSims() = default;
@@ -68,6 +78,11 @@ class DeviceSims {
                              std::vector<int64_t>& sp, std::vector<int64_t>& so, std::vector<uint32_t>* lattice) const;
     std::string read_stats(size_t i, std::vector<uint64_t>& stats) const;
     std::string read_mcs(size_t i, uint64_t& mcs) const;
+    // Topology readouts of the first ns[m] lattice snapshots of simulation
+    // sims[m] (needs lattice samples), computed on the device on the
+    // object's stream after the work already queued there; blocking.
+    std::string topology(const std::vector<size_t>& sims, const std::vector<int>& ns,
+                         std::vector<std::vector<Topo>>& out);
     // Writes sigma/V/I (harness use: set an arbitrary state).
     std::string write_state(size_t i, const std::vector<uint32_t>& padded, const std::vector<uint32_t>& vol,
                             const std::vector<uint32_t>& itf, const std::vector<int64_t>* sp = nullptr,
@@ -122,9 +137,16 @@ class DeviceSims {
 // number of burn-in energy-trace points it records.
 RunPlan plan_for(const Config& c, int sim, bool write_lattice);
 int trace_points(uint64_t burn_in, uint64_t interval, uint64_t start);
-// Reads simulation i back after its run window and builds its result.
+// Reads simulation i back after its run window and builds its result. With
+// ro.topology the samples' topology and the status are left to
+// attach_topology.
 std::string assemble_result(const Config& c, const Initial& init, const DeviceSims& dev, size_t i, int ns, int nt,
                             const ReadoutOptions& ro, Result& R);
+// Moves one simulation's topology readouts into its samples and sets the
+// run status (which depends on them).
+void attach_topology(const Config& c, std::vector<Topo>& topo, Result& R);
+// Device bytes DeviceSims::topology needs for one simulation.
+size_t topology_bytes(int64_t n_sites, int n_cells);
 
 // The 8 MiB 3D simple-point table of the current device (generated once).
 const uint64_t* device_table3d(std::string& err);

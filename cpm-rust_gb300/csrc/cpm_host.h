@@ -70,6 +70,9 @@ std::string theta_inject(Config& c, const double* theta);  // "" on success
 // config.rs:479-556 — BLAKE3 over the serde_json views.
 std::string convention_hash(const Config& c);
 std::string model_hash(const Config& c, const std::vector<uint32_t>& lattice, const std::vector<uint32_t>& type_of);
+// The same, given the configuration's convention hash.
+std::string model_hash_with(const std::string& convention_hash, const std::vector<uint32_t>& lattice,
+                            const std::vector<uint32_t>& type_of);
 void blake3(const uint8_t* data, size_t len, uint8_t out[32]);
 uint64_t derive_seed_u64(uint64_t master, uint64_t index);
 
@@ -143,6 +146,7 @@ struct Result {
     std::vector<std::string> cell_type_names;
     bool used_default = false;
     std::vector<uint64_t> stats;  // CPM_STAT_* counters
+    std::vector<double> energy_trace;  // burn-in energy trace (the status reads it)
 };
 
 // Readout knobs: what each sample carries besides the per-cell summary.

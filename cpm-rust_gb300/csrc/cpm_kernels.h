@@ -44,4 +44,17 @@ cudaError_t launch_tiled(int D, int NE, SimDesc* d_sim, uint64_t n_mcs, const in
                          int barrier_extra, int cl_cap, size_t smem, int grid, cudaStream_t st);
 // Copies one sample (V, I, position sums, optional lattice) of simulation d_sim.
 cudaError_t launch_sample(int D, const SimDesc* d_sim, int sample, int write_lattice, int64_t n_sites, cudaStream_t st);
+// Topology readouts of lattice snapshots (cpm_readout.cu). Work is cut into
+// units of readout_unit() indices per item (sites, contact-pair slots and cell
+// ids share the unit grid); `d_prefix` (n_items + 1) holds each item's first
+// unit. Pass 0 counts contacts, 1 builds the forest inside each unit, 2 joins
+// across units, 3 finds roots and counts, per unit, the entries each output
+// stream will hold (d_unit_cnt: 3 per unit, zero on entry); pass 4 writes the
+// streams in index order at the exclusive prefix sums d_unit_off (3 per
+// unit): contact (a, b, count) triples, medium component words, fragmented
+// cell ids.
+int readout_unit();
+cudaError_t launch_readout(int pass, const ReadoutItem* d_items, int n_items, const int64_t* d_prefix,
+                           int64_t total_units, uint32_t* d_unit_cnt, const uint64_t* d_unit_off, uint32_t* d_pairs,
+                           uint32_t* d_medium, uint32_t* d_frag, cudaStream_t st);
 }  // namespace cpmgpu

@@ -44,6 +44,7 @@ size_t estimate_bytes(const Config& c, const Initial& init, int ns, int ne, bool
     b += (size_t)std::max(1, ne) * 8;
     b += (size_t)ns * n1 * (8 + 8 * D + 8 * D * D);
     if (snapshots) b += (size_t)ns * (size_t)g.n_sites * 4;
+    if (snapshots && ns > 0) b += topology_bytes(g.n_sites, (int)init.type_of.size());
     return b + 64 * 256 + sizeof(SimDesc) + 64;
 }
 
@@ -178,6 +179,7 @@ std::string Server::admit(Req& r) {
     std::string e = r.dev->create({r.c}, {r.init}, {r.ns}, {r.ns + r.nt}, snapshots, r.stream);
     if (!e.empty()) return e;
     r.times.device_bytes = r.dev->device_bytes();
+    if (r.ro.topology && r.ns > 0) r.times.device_bytes += topology_bytes(r.dev->layout(0).g.n_sites, r.dev->layout(0).n_cells);
     e = r.dev->run({r.full});
     if (!e.empty()) return e;
     ce = cudaLaunchHostFunc(r.stream, &Server::device_done, &r);
@@ -200,7 +202,12 @@ void Server::finish(Req* rp) {
         std::lock_guard<std::mutex> lk(mu_);
         cancelled = r.cancel;
     }
-    if (e.empty() && !cancelled) e = assemble_result(r.c, r.init, *r.dev, 0, r.ns, r.nt, r.ro, r.result);
+    if (e.empty() && !cancelled) {
+        std::vector<std::vector<Topo>> topo;
+        if (r.ro.topology) e = r.dev->topology({0}, {r.ns}, topo);
+        if (e.empty()) e = assemble_result(r.c, r.init, *r.dev, 0, r.ns, r.nt, r.ro, r.result);
+        if (e.empty() && r.ro.topology) attach_topology(r.c, topo[0], r.result);
+    }
     release(r);
     std::lock_guard<std::mutex> lk(mu_);
     st_.bytes_in_use -= r.times.device_bytes;

@@ -165,7 +165,7 @@ EXPORTED_SYMBOLS = (
     "cpm_engine_create", "cpm_engine_size", "cpm_engine_sim_info", "cpm_engine_run_mcs", "cpm_engine_synchronize",
     "cpm_engine_mcs", "cpm_engine_read_lattice", "cpm_engine_read_padded", "cpm_engine_read_cells",
     "cpm_engine_energy", "cpm_engine_recount_check", "cpm_engine_stats", "cpm_engine_write_state",
-    "cpm_engine_evaluate_moves", "cpm_engine_commit_moves", "cpm_engine_destroy",
+    "cpm_engine_evaluate_moves", "cpm_engine_commit_moves", "cpm_engine_take_sample", "cpm_engine_destroy",
     "cpm_run_many",
     "cpm_builder_initial_state", "cpm_builder_hashes", "cpm_derive_seed_u64",
     "cpm_run_mcs_noalloc",
@@ -220,6 +220,7 @@ def _load():
     L.cpm_engine_energy.argtypes = [_P, SZ, ctypes.POINTER(D)]
     L.cpm_engine_recount_check.argtypes = [_P, SZ, ctypes.POINTER(I32), _P, _P]
     L.cpm_engine_stats.argtypes = [_P, SZ, _P]
+    L.cpm_engine_take_sample.argtypes = [_P, SZ, I32, ctypes.POINTER(_P)]
     L.cpm_engine_write_state.argtypes = [_P, SZ, _P, _P, _P, _P, _P]
     L.cpm_engine_evaluate_moves.argtypes = [_P, SZ, SZ, _P, _P, _P, _P]
     L.cpm_engine_commit_moves.argtypes = [_P, SZ, SZ, _P, _P]
@@ -652,6 +653,13 @@ class Engine:
         s = np.zeros(32, np.uint64)
         _check(_lib.cpm_engine_stats(self._h, i, _ptr(s)))
         return {name: int(s[k]) for k, name in enumerate(STAT_NAMES)}
+
+    def take_sample(self, i=0, include_lattice=False):
+        """One Sample of the current state (output.rs:304-337), every readout
+        computed on the device; its energy is the global energy of the state."""
+        h = _P()
+        _check(_lib.cpm_engine_take_sample(self._h, i, 1 if include_lattice else 0, ctypes.byref(h)))
+        return _result_from_handle(h).samples[0]
 
     def write_state(self, padded, volume, interface, sum_position=None, sum_outer=None, i=0):
         p = np.ascontiguousarray(padded, dtype=np.uint32)

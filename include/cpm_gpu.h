@@ -244,6 +244,12 @@ int cpm_engine_energy(const cpm_engine* e, size_t sim, double* out);
  * (checker.rs:36-83); *ok = 1 iff it equals the incrementally kept state. */
 int cpm_engine_recount_check(const cpm_engine* e, size_t sim, int32_t* ok, uint32_t* volume, uint32_t* interface);
 int cpm_engine_stats(const cpm_engine* e, size_t sim, uint64_t* out32);
+/* One sample of the current state (output.rs:304-337 `take_sample`, the
+ * `cpm_sample` seam): per-cell volume, interface, centroid and gyration,
+ * the contact graph and the labelling, all computed on the device, returned
+ * as a result with one sample (its energy is the device's global energy of
+ * the state, its mcs the MCS completed so far). Free with cpm_result_free. */
+int cpm_engine_take_sample(cpm_engine* e, size_t sim, int32_t include_lattice, cpm_result** out);
 /* Parity harness: overwrite the dynamic state, decide moves without
  * committing them, or apply moves in order with the sweep's commit. */
 int cpm_engine_write_state(cpm_engine* e, size_t sim, const uint32_t* padded, const uint32_t* volume,

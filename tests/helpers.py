@@ -97,3 +97,52 @@ def random_interior_targets(sim: O.OracleSim, n, rng):
     for d in range(sim.spec.D):
         flat += (rng.integers(0, grid[d], n) + 1) * st[d]
     return flat
+
+
+def contact_reference(lat, periodic, offsets):
+    """Independent count of the contact graph: unordered pairs of neighbouring
+    sites of different cells (each pair once), and for a fixed boundary each
+    (site, outward offset) of a cell as a contact with the medium."""
+    from collections import Counter
+
+    lat = np.asarray(lat)
+    D = lat.ndim
+    cnt = Counter()
+    idx = np.indices(lat.shape).reshape(D, -1).T
+    flat = lat.ravel()
+    shape = np.array(lat.shape)
+    for off in offsets:
+        nb = idx + np.asarray(off)
+        if periodic:
+            nb = nb % shape
+            inside = np.ones(len(idx), bool)
+        else:
+            inside = np.all((nb >= 0) & (nb < shape), axis=1)
+        src = np.ravel_multi_index(idx.T, lat.shape)
+        for k in np.flatnonzero(inside):
+            j = np.ravel_multi_index(nb[k], lat.shape)
+            if j <= src[k]:
+                continue
+            a, b = flat[src[k]], flat[j]
+            if a != b:
+                cnt[(min(a, b), max(a, b))] += 1
+        if not periodic:
+            for k in np.flatnonzero(~inside):
+                a = flat[src[k]]
+                if a != 0:
+                    cnt[(0, a)] += 1
+    return cnt
+
+
+def energy_offsets(model):
+    """The energy stencil as coordinate offsets (neighborhood.rs order)."""
+    import itertools
+
+    D = model.D
+    full = [o for o in itertools.product((-1, 0, 1), repeat=D) if any(o)]
+    kind = model.energy or NBH_DEFAULT[D]
+    if kind == "von_neumann":
+        return [o for o in full if sum(map(abs, o)) == 1]
+    if kind == "eighteen":
+        return [o for o in full if sum(map(abs, o)) <= 2]
+    return full

@@ -223,46 +223,11 @@ def test_default_placement_warning_policy(cuda_required):
     assert len(res.samples) == 1
 
 
-def _contact_reference(lat, periodic, offsets):
-    """Independent count of the contact graph: unordered pairs of neighbouring
-    sites of different cells (each pair once), and for a fixed boundary each
-    (site, outward offset) of a cell as a contact with the medium."""
-    from collections import Counter
-
-    lat = np.asarray(lat)
-    D = lat.ndim
-    cnt = Counter()
-    idx = np.indices(lat.shape).reshape(D, -1).T
-    flat = lat.ravel()
-    shape = np.array(lat.shape)
-    for off in offsets:
-        nb = idx + np.asarray(off)
-        if periodic:
-            nb = nb % shape
-            inside = np.ones(len(idx), bool)
-        else:
-            inside = np.all((nb >= 0) & (nb < shape), axis=1)
-        src = np.ravel_multi_index(idx.T, lat.shape)
-        for k in np.flatnonzero(inside):
-            j = np.ravel_multi_index(nb[k], lat.shape)
-            if j <= src[k]:
-                continue
-            a, b = flat[src[k]], flat[j]
-            if a != b:
-                cnt[(min(a, b), max(a, b))] += 1
-        if not periodic:
-            for k in np.flatnonzero(~inside):
-                a = flat[src[k]]
-                if a != 0:
-                    cnt[(0, a)] += 1
-    return cnt
-
-
 @pytest.mark.parametrize("name", ["2d_periodic", "2d_fixed", "3d_periodic"])
 def test_topology_readouts_match_an_independent_count_and_the_oracle(name, cuda_required):
     """Contact graph (independent count over the snapshot), fragmented cells
     and medium components (the oracle's labelling of the same state)."""
-    from helpers import Model, organoid_model, sorting_model
+    from helpers import Model, contact_reference, energy_offsets, organoid_model, sorting_model
 
     model = {"2d_periodic": lambda: sorting_model(side=40, seed=31),
              "2d_fixed": lambda: Model((36, 30), "fixed", [("a", 40, 30, 3.0, 0.6)], [[0, 6.5], [6.5, 2.2]], [12],
@@ -272,10 +237,10 @@ def test_topology_readouts_match_an_independent_count_and_the_oracle(name, cuda_
 
     _, res = model.builder(warn=False).run(20, 40, 20, 1)
     sim = model.oracle()
-    offsets = [tuple(int(v) for v in o) for o in _energy_offsets(model)]
+    offsets = [tuple(int(v) for v in o) for o in energy_offsets(model)]
     for s in res.samples:
         lat = np.asarray(s.lattice)
-        ref = _contact_reference(lat, model.boundary == "periodic", offsets)
+        ref = contact_reference(lat, model.boundary == "periodic", offsets)
         a, b, n = s.contact_pairs
         got = {(int(x), int(y)): int(z) for x, y, z in zip(a, b, n)}
         assert got == dict(ref)
@@ -287,17 +252,3 @@ def test_topology_readouts_match_an_independent_count_and_the_oracle(name, cuda_
         assert list(s.fragmented_cells) == list(want["fragmented"])
         assert list(s.medium_component_volumes) == list(want["medium_volumes"])
         assert list(s.medium_component_touches_boundary) == list(want["medium_touches"])
-
-
-def _energy_offsets(model):
-    """The energy stencil as coordinate offsets (neighborhood.rs order)."""
-    import itertools
-
-    D = model.D
-    full = [o for o in itertools.product((-1, 0, 1), repeat=D) if any(o)]
-    kind = model.energy
-    if kind == "von_neumann":
-        return [o for o in full if sum(map(abs, o)) == 1]
-    if kind == "eighteen":
-        return [o for o in full if sum(map(abs, o)) <= 2]
-    return full
