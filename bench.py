@@ -16,7 +16,8 @@ attempts per second.
   stream), lattice already resident in HBM; L2 (129 MB) is flushed by a
   256 MB write between timed steps.
 * e2e: the same metric through the public API `cpm.CPM(...).run(...)`
-  (host placement, upload, device run, download, host readouts) per step.
+  (host placement, upload, device run, download, readouts) per step; a
+  step is one whole run of the workload's 20,000 MCS window (`--e2e-mcs`).
 * roofline: algorithmic HBM bytes per attempt = 4 + 4*f_acc (sigma read
   once, written on accept) times the attempts of one launch, over the
   launch's average duration, against the measured copy bandwidth.
@@ -597,18 +598,20 @@ def run_gpu(args, rank, world, dist):
         for i in range(args.e2e_steps + 1):
             sim = build_public(SEED + 100 + i)
             torch.cuda.synchronize()
+            mcs = args.e2e_mcs if i else min(args.e2e_mcs, 100)  # i == 0: a short warm-up call
             t0 = time.perf_counter()
-            res = sim.run(burn_in_mcs=0, readout_mcs=args.e2e_mcs, sampling_interval_mcs=args.e2e_mcs)
+            res = sim.run(burn_in_mcs=0, readout_mcs=mcs, sampling_interval_mcs=mcs)
             torch.cuda.synchronize()
             dt = time.perf_counter() - t0
             if i == 0:
-                continue  # warm-up call
+                continue
             times.append(dt)
             h2d += res.stats["h2d_bytes"]
             d2h += res.stats["d2h_bytes"]
         n = len(times)
         e2e = {"value": n * args.e2e_mcs * n_sites / sum(times), "unit": "attempts/s",
                "h2d_bytes_per_step": h2d // n, "d2h_bytes_per_step": d2h // n,
+               "seconds_per_step": sum(times) / n,
                "step": f"cpm.CPM(...).run(burn_in_mcs=0, readout_mcs={args.e2e_mcs}, sampling_interval_mcs={args.e2e_mcs})"}
 
     if rank != 0:
@@ -664,9 +667,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--mcs-per-step", type=int, default=50)
     ap.add_argument("--e2e-steps", type=int, default=2)
-    ap.add_argument("--e2e-mcs", type=int, default=1000)
+    ap.add_argument("--e2e-mcs", type=int, default=20000, help="MCS of each end-to-end run (the workload's window)")
     ap.add_argument("--cpu-mcs", type=int, default=200)
-    ap.add_argument("--ref-mcs", type=int, default=40)
+    ap.add_argument("--ref-mcs", type=int, default=200, help="MCS per host thread and step of the reference arm")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--batch-n", type=int, default=4096, help="thetas of the batch workload (0 skips it)")
     ap.add_argument("--batch-mcs", type=lambda v: tuple(int(x) for x in v.split(",")), default=(2000, 2000, 100),

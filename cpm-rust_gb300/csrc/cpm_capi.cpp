@@ -6,6 +6,7 @@
 // theta helpers. Results wrap cpmhost::Result (convert.rs:27-256).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -441,8 +442,7 @@ extern "C" int cpm_result_samples_sizes(const cpm_result* r, cpm_samples_sizes* 
     return ok();
 }
 
-extern "C" int cpm_result_samples_read(const cpm_result* r, const cpm_samples_out* o) {
-    if (!r || !o) return fail(CPM_E_ARG, "null argument");
+static void samples_read(const cpm_result* r, const cpm_samples_out* o) {
     const int D = r->r.D;
     const size_t n = r->r.cell_type_index.size();
     size_t nc = 0, nf = 0, nm = 0, site0 = 0;
@@ -488,6 +488,27 @@ extern "C" int cpm_result_samples_read(const cpm_result* r, const cpm_samples_ou
     if (o->contact_offsets) o->contact_offsets[ns] = nc;
     if (o->fragmented_offsets) o->fragmented_offsets[ns] = nf;
     if (o->medium_offsets) o->medium_offsets[ns] = nm;
+}
+
+extern "C" int cpm_result_samples_read(const cpm_result* r, const cpm_samples_out* o) {
+    if (!r || !o) return fail(CPM_E_ARG, "null argument");
+    samples_read(r, o);
+    return ok();
+}
+
+extern "C" int cpm_results_samples_read(const cpm_result* const* rs, size_t n, const cpm_samples_out* outs) {
+    if (n && (!rs || !outs)) return fail(CPM_E_ARG, "null argument");
+    for (size_t i = 0; i < n; ++i)
+        if (!rs[i]) return fail(CPM_E_ARG, "null result");
+    std::atomic<size_t> next{0};
+    auto work = [&] {
+        for (size_t i; (i = next.fetch_add(1)) < n;) samples_read(rs[i], &outs[i]);
+    };
+    const size_t nt = std::min<size_t>(std::max(1u, std::thread::hardware_concurrency()), (n + 7) / 8);
+    std::vector<std::thread> th;
+    for (size_t t = 1; t < nt; ++t) th.emplace_back(work);
+    work();
+    for (auto& t : th) t.join();
     return ok();
 }
 

@@ -171,6 +171,7 @@ EXPORTED_SYMBOLS = (
     "cpm_run_mcs_noalloc",
     "cpm_serve_start", "cpm_serve_submit", "cpm_serve_poll", "cpm_serve_wait", "cpm_serve_cancel",
     "cpm_serve_stats_get", "cpm_serve_stop", "cpm_result_samples_sizes", "cpm_result_samples_read",
+    "cpm_results_samples_read",
 )
 
 
@@ -233,6 +234,7 @@ def _load():
     L.cpm_derive_seed_u64.restype = U64
     L.cpm_result_samples_sizes.argtypes = [_P, _P]
     L.cpm_result_samples_read.argtypes = [_P, _P]
+    L.cpm_results_samples_read.argtypes = [_P, SZ, _P]
     L.cpm_serve_start.argtypes = [_P, ctypes.POINTER(_P)]
     L.cpm_serve_submit.argtypes = [_P, _P, U64, U64, U64, I32, I32, ctypes.POINTER(U64)]
     L.cpm_serve_poll.argtypes = [_P, U64, ctypes.POINTER(I32), ctypes.POINTER(_P), _P]
@@ -347,96 +349,147 @@ class SamplesOutC(ctypes.Structure):
     )]
 
 
-def _read_samples(h, ns, n, D, grid):
-    """Every sample of a result from one bulk read (cpm_result_samples_read);
-    each Sample's arrays are views into the per-result arrays."""
-    if ns == 0:
-        return []
-    sz = SamplesSizesC()
-    _check(_lib.cpm_result_samples_sizes(h, ctypes.byref(sz)))
-    a = {
-        "mcs": np.zeros(ns, np.uint64), "conservative_energy": np.zeros(ns, np.float64),
-        "ids": np.zeros((ns, n), np.uint32), "volume": np.zeros((ns, n), np.uint32),
-        "interface": np.zeros((ns, n), np.uint32), "centroid": np.zeros((ns, n, D), np.float64),
-        "eigenvalues": np.zeros((ns, n, D), np.float64), "radius_of_gyration_sq": np.zeros((ns, n), np.float64),
-        "kappa_sq": np.zeros((ns, n), np.float64), "contact_offsets": np.zeros(ns + 1, np.uint64),
-        "contact_a": np.zeros(int(sz.total_contact), np.uint32), "contact_b": np.zeros(int(sz.total_contact), np.uint32),
-        "contact_count": np.zeros(int(sz.total_contact), np.uint32), "fragmented_offsets": np.zeros(ns + 1, np.uint64),
-        "fragmented_cells": np.zeros(int(sz.total_fragmented), np.uint32), "medium_offsets": np.zeros(ns + 1, np.uint64),
-        "medium_component_volumes": np.zeros(int(sz.total_medium), np.uint32),
-        "medium_component_touches_boundary": np.zeros(int(sz.total_medium), np.uint8),
-    }
-    lat = np.zeros((ns,) + tuple(grid), np.uint32) if sz.has_lattice else None
-    o = SamplesOutC()
-    for name, arr in a.items():
-        setattr(o, name, arr.ctypes.data if arr.size else None)
-    o.lattice = lat.ctypes.data if lat is not None else None
-    _check(_lib.cpm_result_samples_read(h, ctypes.byref(o)))
-    co, fo, mo = a["contact_offsets"].tolist(), a["fragmented_offsets"].tolist(), a["medium_offsets"].tolist()
-    frag = a["fragmented_cells"].tolist()
-    mvol = a["medium_component_volumes"].tolist()
-    mtouch = [bool(x) for x in a["medium_component_touches_boundary"]]
-    mcs, en = a["mcs"].tolist(), a["conservative_energy"].tolist()
-    out = []
-    for s in range(ns):
-        smp = Sample()
-        smp.mcs = int(mcs[s])
-        smp.conservative_energy = float(en[s])
-        smp.ids, smp.volume, smp.interface = a["ids"][s], a["volume"][s], a["interface"][s]
-        smp.centroid, smp.eigenvalues = a["centroid"][s], a["eigenvalues"][s]
-        smp.radius_of_gyration_sq, smp.kappa_sq = a["radius_of_gyration_sq"][s], a["kappa_sq"][s]
-        smp.fragmented_cells = frag[fo[s]:fo[s + 1]]
-        smp.medium_component_volumes = mvol[mo[s]:mo[s + 1]]
-        smp.medium_component_touches_boundary = mtouch[mo[s]:mo[s + 1]]
-        smp.lattice = lat[s] if lat is not None else None
-        c0, c1 = co[s], co[s + 1]
-        smp._contact_pairs = (a["contact_a"][c0:c1], a["contact_b"][c0:c1], a["contact_count"][c0:c1])
-        smp._contact = None
-        out.append(smp)
-    return out
+# cpm_samples_out fields: (name, dtype, extent) with extent "s" = samples,
+# "s1" = samples + 1 offsets, "sn" = samples x cells, "snD" = samples x cells
+# x D, "c"/"f"/"m" = the concatenated contact / fragmented / medium lists.
+_SAMPLE_FIELDS = (
+    ("mcs", np.uint64, "s"), ("conservative_energy", np.float64, "s"), ("ids", np.uint32, "sn"),
+    ("volume", np.uint32, "sn"), ("interface", np.uint32, "sn"), ("centroid", np.float64, "snD"),
+    ("eigenvalues", np.float64, "snD"), ("radius_of_gyration_sq", np.float64, "sn"), ("kappa_sq", np.float64, "sn"),
+    ("contact_offsets", np.uint64, "s1"), ("contact_a", np.uint32, "c"), ("contact_b", np.uint32, "c"),
+    ("contact_count", np.uint32, "c"), ("fragmented_offsets", np.uint64, "s1"), ("fragmented_cells", np.uint32, "f"),
+    ("medium_offsets", np.uint64, "s1"), ("medium_component_volumes", np.uint32, "m"),
+    ("medium_component_touches_boundary", np.uint8, "m"),
+)
+
+
+def _read_samples_many(hs, dims):
+    """The samples of many results: one array per field for all of them,
+    filled by one cpm_results_samples_read call (spread over the host's
+    cores); every Sample's arrays are views into those arrays."""
+    N = len(hs)
+    sizes = []
+    for h, (ns, _, _, _) in zip(hs, dims):
+        sz = SamplesSizesC()
+        if ns:
+            _check(_lib.cpm_result_samples_sizes(h, ctypes.byref(sz)))
+        sizes.append(sz)
+    counts = []
+    for (ns, n, D, _), sz in zip(dims, sizes):
+        counts.append({"s": ns, "s1": ns + 1 if ns else 0, "sn": ns * n, "snD": ns * n * D,
+                       "c": int(sz.total_contact), "f": int(sz.total_fragmented), "m": int(sz.total_medium)})
+    big, starts = {}, {}
+    for name, dt, ext in _SAMPLE_FIELDS:
+        st, t = [], 0
+        for c in counts:
+            st.append(t)
+            t += c[ext]
+        big[name], starts[name] = np.zeros(t, dt), st
+    lat_n = [ns * int(np.prod(grid)) if sz.has_lattice else 0 for (ns, _, _, grid), sz in zip(dims, sizes)]
+    lat_start = np.concatenate([[0], np.cumsum(lat_n)]).astype(np.int64).tolist()
+    big_lat = np.zeros(lat_start[-1], np.uint32)
+    outs = (SamplesOutC * max(N, 1))()
+    for k in range(N):
+        o = outs[k]
+        for name, dt, ext in _SAMPLE_FIELDS:
+            if counts[k][ext]:
+                setattr(o, name, big[name].ctypes.data + starts[name][k] * big[name].itemsize)
+        if lat_n[k]:
+            o.lattice = big_lat.ctypes.data + lat_start[k] * 4
+    if N:
+        harr = (_P * N)(*hs)
+        _check(_lib.cpm_results_samples_read(ctypes.cast(harr, _P), N, ctypes.cast(outs, _P)))
+    result = []
+    for k, ((ns, n, D, grid), c) in enumerate(zip(dims, counts)):
+        if ns == 0:
+            result.append([])
+            continue
+        a = {name: big[name][starts[name][k]:starts[name][k] + c[ext]] for name, _, ext in _SAMPLE_FIELDS}
+        for name in ("ids", "volume", "interface", "radius_of_gyration_sq", "kappa_sq"):
+            a[name] = a[name].reshape(ns, n)
+        for name in ("centroid", "eigenvalues"):
+            a[name] = a[name].reshape(ns, n, D)
+        lat = big_lat[lat_start[k]:lat_start[k + 1]].reshape((ns,) + tuple(grid)) if lat_n[k] else None
+        co, fo, mo = a["contact_offsets"].tolist(), a["fragmented_offsets"].tolist(), a["medium_offsets"].tolist()
+        frag = a["fragmented_cells"].tolist()
+        mvol = a["medium_component_volumes"].tolist()
+        mtouch = [bool(x) for x in a["medium_component_touches_boundary"]]
+        mcs, en = a["mcs"].tolist(), a["conservative_energy"].tolist()
+        ca, cb, cc = a["contact_a"], a["contact_b"], a["contact_count"]
+        out = []
+        for s in range(ns):
+            smp = Sample()
+            smp.mcs = int(mcs[s])
+            smp.conservative_energy = float(en[s])
+            smp.ids, smp.volume, smp.interface = a["ids"][s], a["volume"][s], a["interface"][s]
+            smp.centroid, smp.eigenvalues = a["centroid"][s], a["eigenvalues"][s]
+            smp.radius_of_gyration_sq, smp.kappa_sq = a["radius_of_gyration_sq"][s], a["kappa_sq"][s]
+            smp.fragmented_cells = frag[fo[s]:fo[s + 1]]
+            smp.medium_component_volumes = mvol[mo[s]:mo[s + 1]]
+            smp.medium_component_touches_boundary = mtouch[mo[s]:mo[s + 1]]
+            smp.lattice = lat[s] if lat is not None else None
+            c0, c1 = co[s], co[s + 1]
+            smp._contact_pairs = (ca[c0:c1], cb[c0:c1], cc[c0:c1])
+            smp._contact = None
+            out.append(smp)
+        result.append(out)
+    return result
+
+
+def _result_head(h):
+    """Everything of a result but its samples, and the samples' dimensions."""
+    info = ResultInfo()
+    _check(_lib.cpm_result_info_get(h, ctypes.byref(info)))
+    D, n = info.dim, int(info.n_cells)
+    grid = tuple(int(info.grid[d]) for d in range(D))
+    md = MetadataC()
+    _check(_lib.cpm_result_metadata_get(h, ctypes.byref(md)))
+    meta = RunMetadata()
+    meta.cpm_version = md.cpm_version.decode()
+    meta.convention_version = int(md.convention_version)
+    meta.convention_hash = md.convention_hash.decode()
+    meta.model_hash = md.model_hash.decode()
+    meta.seed = int(md.seed)
+    meta.seed_policy = md.seed_policy.decode()
+    meta.derived_phi = float(md.derived_phi)
+    meta.theta_layout_version = int(md.theta_layout_version)
+    st = StatusC()
+    _check(_lib.cpm_result_status_get(h, ctypes.byref(st)))
+    status = Status()
+    status.kind = st.kind.decode()
+    status.cell_id = int(st.cell_id) if st.has_cell else None
+    status.at_mcs = int(st.at_mcs) if st.has_cell else None
+    cti = np.zeros(n, dtype=np.uint32)
+    _check(_lib.cpm_result_cell_type_index(h, _ptr(cti)))
+    names = []
+    buf = ctypes.create_string_buffer(4096)
+    for t in range(info.n_types):
+        _check(_lib.cpm_result_cell_type_name(h, t, buf, 4096))
+        names.append(buf.value.decode("utf-8"))
+    stats = np.zeros(32, dtype=np.uint64)
+    _check(_lib.cpm_result_stats(h, _ptr(stats)))
+    r = RunResult()
+    r.metadata, r.status, r.samples = meta, status, []
+    r.cell_type_index, r.cell_type_names = cti, names
+    r.used_default = bool(info.used_default)
+    r.stats = {name: int(v) for name, v in zip(STAT_NAMES, stats.tolist())}
+    return r, (int(info.n_samples), n, D, grid)
+
+
+def _results_from_handles(hs) -> list:
+    """Python results of result handles (freed here, also on errors)."""
+    try:
+        heads = [_result_head(h) for h in hs]
+        for (r, _), smp in zip(heads, _read_samples_many(hs, [d for _, d in heads])):
+            r.samples = smp
+        return [r for r, _ in heads]
+    finally:
+        for h in hs:
+            _lib.cpm_result_free(h)
 
 
 def _result_from_handle(h) -> RunResult:
-    try:
-        info = ResultInfo()
-        _check(_lib.cpm_result_info_get(h, ctypes.byref(info)))
-        D, n = info.dim, int(info.n_cells)
-        grid = tuple(int(info.grid[d]) for d in range(D))
-        md = MetadataC()
-        _check(_lib.cpm_result_metadata_get(h, ctypes.byref(md)))
-        meta = RunMetadata()
-        meta.cpm_version = md.cpm_version.decode()
-        meta.convention_version = int(md.convention_version)
-        meta.convention_hash = md.convention_hash.decode()
-        meta.model_hash = md.model_hash.decode()
-        meta.seed = int(md.seed)
-        meta.seed_policy = md.seed_policy.decode()
-        meta.derived_phi = float(md.derived_phi)
-        meta.theta_layout_version = int(md.theta_layout_version)
-        st = StatusC()
-        _check(_lib.cpm_result_status_get(h, ctypes.byref(st)))
-        status = Status()
-        status.kind = st.kind.decode()
-        status.cell_id = int(st.cell_id) if st.has_cell else None
-        status.at_mcs = int(st.at_mcs) if st.has_cell else None
-        cti = np.zeros(n, dtype=np.uint32)
-        _check(_lib.cpm_result_cell_type_index(h, _ptr(cti)))
-        names = []
-        buf = ctypes.create_string_buffer(4096)
-        for t in range(info.n_types):
-            _check(_lib.cpm_result_cell_type_name(h, t, buf, 4096))
-            names.append(buf.value.decode("utf-8"))
-        stats = np.zeros(32, dtype=np.uint64)
-        _check(_lib.cpm_result_stats(h, _ptr(stats)))
-        samples = _read_samples(h, int(info.n_samples), n, D, grid)
-        r = RunResult()
-        r.metadata, r.status, r.samples = meta, status, samples
-        r.cell_type_index, r.cell_type_names = cti, names
-        r.used_default = bool(info.used_default)
-        r.stats = {name: int(stats[i]) for i, name in enumerate(STAT_NAMES)}
-        return r
-    finally:
-        _lib.cpm_result_free(h)
+    return _results_from_handles([h])[0]
 
 
 # ----------------------------------------------------------------- builder
@@ -518,7 +571,7 @@ class CPM:
             _u64(burn_in_mcs, "burn_in_mcs"), _u64(readout_mcs, "readout_mcs"),
             _u64(sampling_interval_mcs, "sampling_interval_mcs"), _u64(master_seed, "master_seed"),
             int(bool(include_lattice)), ctypes.byref(anyd), ctypes.cast(out, _P)))
-        return bool(anyd.value), [_result_from_handle(_P(out[i])) for i in range(len(rows))]
+        return bool(anyd.value), _results_from_handles([_P(out[i]) for i in range(len(rows))])
 
     def initial_state(self):
         """Host-only placement (no device work): (lattice, cell_type_of, used_default)."""
@@ -573,7 +626,7 @@ def run_many(builders, burn_in_mcs, readout_mcs, sampling_interval_mcs, include_
     _check(_lib.cpm_run_many(ctypes.cast(hs, _P), len(builders), _u64(burn_in_mcs, "burn_in_mcs"),
                              _u64(readout_mcs, "readout_mcs"), _u64(sampling_interval_mcs, "sampling_interval_mcs"),
                              int(bool(include_lattice)), int(bool(topology)), ctypes.cast(out, _P)))
-    return [_result_from_handle(_P(out[i])) for i in range(len(builders))]
+    return _results_from_handles([_P(out[i]) for i in range(len(builders))])
 
 
 class Engine:

@@ -182,6 +182,9 @@ typedef struct {
     uint32_t* lattice;
 } cpm_samples_out;
 int cpm_result_samples_read(const cpm_result* r, const cpm_samples_out* out);
+/* cpm_result_samples_read for n results at once (results[i] into outs[i]),
+ * spread over the host's cores: the read-back of a whole batch. */
+int cpm_results_samples_read(const cpm_result* const* results, size_t n, const cpm_samples_out* outs);
 /* Device counters of the run (order: attempts, non-null, topology
  * rejections, guard rejections, evaluated, accepted, conflict rounds, colour
  * passes, timeouts, fixpoint iterations, h2d bytes, d2h bytes, deferred
