@@ -199,11 +199,8 @@ static int resolve(const cpm_builder* b, uint64_t burn, uint64_t readout, uint64
 }
 
 static int check_supported(const Config& c) {
-    if (c.acceptance != ACC_METROPOLIS)
-        return fail(CPM_E_UNSUPPORTED, "acceptance = \"metropolis_hastings\" is a test instrument of the reference and is not run by the GB300 engine");
     if (c.proposal != PROP_UNIFORM)
         return fail(CPM_E_UNSUPPORTED, "proposal = \"edge_list\" is not run by the GB300 engine (use \"uniform\")");
-    if (c.active.act) return fail(CPM_E_UNSUPPORTED, "the Act energy term is not run by the GB300 engine");
     return ok();
 }
 
@@ -646,6 +643,23 @@ extern "C" int cpm_engine_take_sample(cpm_engine* e, size_t i, int32_t include_l
     auto r = std::make_unique<cpm_result>();
     r->r = std::move(R);
     *out = r.release();
+    return ok();
+}
+
+extern "C" int cpm_engine_write_act_state(cpm_engine* e, size_t i, const uint32_t* birth, uint64_t mcs) {
+    if (bad_sim(e, i)) return fail(CPM_E_ARG, "bad engine or simulation index");
+    std::vector<uint32_t> b;
+    if (birth) b.assign(birth, birth + e->sims.layout(i).g.n_padded);
+    const std::string msg = e->sims.write_act_state(i, birth ? &b : nullptr, mcs);
+    return msg.empty() ? ok() : fail(msg.rfind("CUDA", 0) == 0 ? CPM_E_CUDA : CPM_E_ARG, msg);
+}
+
+extern "C" int cpm_engine_read_birth(const cpm_engine* e, size_t i, uint32_t* out) {
+    if (bad_sim(e, i) || !out) return fail(CPM_E_ARG, "bad engine or simulation index");
+    std::vector<uint32_t> b;
+    const std::string msg = e->sims.read_birth(i, b);
+    if (!msg.empty()) return fail(msg.rfind("CUDA", 0) == 0 ? CPM_E_CUDA : CPM_E_ARG, msg);
+    std::memcpy(out, b.data(), b.size() * 4);
     return ok();
 }
 

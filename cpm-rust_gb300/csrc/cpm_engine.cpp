@@ -127,7 +127,7 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
     table2d(t2);
     bool need_t3 = false;
     // ---- sizes
-    struct Offs { size_t sigma, adh, vol, itf, sp, so, slots, stats, J, lv, li, tv, ti, vt, it, dj, vt32, it32, vt32lo, it32lo, dj32, J32, energy, svol, sitf, ssp, sso, slat, err; };
+    struct Offs { size_t sigma, adh, vol, itf, sp, so, slots, stats, J, lv, li, tv, ti, vt, it, dj, vt32, it32, vt32lo, it32lo, dj32, J32, la, ma, birth, energy, svol, sitf, ssp, sso, slat, err; };
     std::vector<int> tab_n(N);
     std::vector<Offs> offs(N);
     Carve cv;
@@ -169,6 +169,10 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
         o.it32lo = cv.take(nt * (size_t)tab_n[i] * 4);
         o.dj32 = cv.take((nt + 1) * (nt + 1) * (nt + 1) * 4);
         o.J32 = cv.take((nt + 1) * (nt + 1) * 4);
+        // Act term: per-type parameters and the per-site acquisition MCS (zero)
+        o.la = c.active.act ? cv.take(nt * 8) : 0;
+        o.ma = c.active.act ? cv.take(nt * 4) : 0;
+        o.birth = c.active.act ? cv.take((size_t)L.g.n_padded * 4) : 0;
         o.err = cv.take(8);
     }
     // run-window outputs after every input: the device writes them, so they
@@ -232,6 +236,10 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
             std::memcpy(stage.data() + o.li + t * 8, &li, 8);
             std::memcpy(stage.data() + o.tv + t * 4, &c.types[t].target_volume, 4);
             std::memcpy(stage.data() + o.ti + t * 4, &c.types[t].target_interface, 4);
+            if (c.active.act) {
+                std::memcpy(stage.data() + o.la + t * 8, &c.types[t].lambda_act, 8);
+                std::memcpy(stage.data() + o.ma + t * 4, &c.types[t].max_act, 4);
+            }
         }
         // Exact term tables: the device adds these values where it would
         // otherwise compute lambda * ((x - target) * (x - target)) and
@@ -328,6 +336,11 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
         char* base = arena_;
         s.sigma = (uint32_t*)(base + o.sigma);
         s.adh_of = (const uint16_t*)(base + o.adh);
+        s.acceptance = c.acceptance == ACC_METROPOLIS ? 0 : 1;
+        s.act = c.active.act ? 1 : 0;
+        s.lambda_act = c.active.act ? (const double*)(base + o.la) : nullptr;
+        s.max_act = c.active.act ? (const uint32_t*)(base + o.ma) : nullptr;
+        s.birth = c.active.act ? (uint32_t*)(base + o.birth) : nullptr;
         s.volume = (uint32_t*)(base + o.vol);
         s.interface = (uint32_t*)(base + o.itf);
         s.sum_pos = (int64_t*)(base + o.sp);
@@ -385,6 +398,8 @@ DeviceSims::Path DeviceSims::path(size_t i) const {
     const SimLayout& L = layouts_[i];
     if (force_global_) return GLOBAL;
     if (L.n_cells >= 65535) return GLOBAL;
+    // Metropolis-Hastings acceptance and the Act term run on the global sweep only
+    if (descs_[i].acceptance || descs_[i].act) return GLOBAL;
     int dims[3] = {(int)L.g.dims[0], (int)L.g.dims[1], (int)L.g.dims[2]}, nt[3] = {1, 1, 1}, max_box = 0;
     const bool tiled_ok = cpmgpu::tiled_plan(L.g.D, dims, L.g.periodic, nt, &max_box) &&
                           cpmgpu::tiled_smem_bytes(max_box, L.n_cells, 0, L.g.D) <= cpmgpu::resident_smem_limit();
@@ -636,6 +651,26 @@ std::string DeviceSims::read_stats(size_t i, std::vector<uint64_t>& stats) const
     stats.resize(CPM_STAT_COUNT);
     d2h_bytes_ += CPM_STAT_COUNT * 8;
     CUDA_TRY(cudaMemcpy(stats.data(), descs_[i].stats, CPM_STAT_COUNT * 8, cudaMemcpyDeviceToHost));
+    return "";
+}
+
+std::string DeviceSims::write_act_state(size_t i, const std::vector<uint32_t>* birth, uint64_t mcs) {
+    if (birth) {
+        if (!descs_[i].birth) return "write_act_state: the Act term is not active";
+        if (birth->size() != (size_t)layouts_[i].g.n_padded) return "write_act_state: size mismatch";
+        h2d_bytes_ += birth->size() * 4;
+        CUDA_TRY(cudaMemcpy(descs_[i].birth, birth->data(), birth->size() * 4, cudaMemcpyHostToDevice));
+    }
+    descs_[i].mcs = mcs;
+    CUDA_TRY(cudaMemcpy(&d_descs_[i].mcs, &mcs, 8, cudaMemcpyHostToDevice));
+    return "";
+}
+
+std::string DeviceSims::read_birth(size_t i, std::vector<uint32_t>& birth) const {
+    if (!descs_[i].birth) return "read_birth: the Act term is not active";
+    birth.resize((size_t)layouts_[i].g.n_padded);
+    d2h_bytes_ += birth.size() * 4;
+    CUDA_TRY(cudaMemcpy(birth.data(), descs_[i].birth, birth.size() * 4, cudaMemcpyDeviceToHost));
     return "";
 }
 
@@ -1069,9 +1104,7 @@ std::string run_many(const std::vector<Config>& configs, const std::vector<Initi
     out.assign(N, Result());
     if (N == 0) return "";
     for (auto& c : configs) {
-        if (c.acceptance != ACC_METROPOLIS) return "acceptance = metropolis_hastings is not supported by the GB300 engine";
         if (c.proposal != PROP_UNIFORM) return "proposal = edge_list is not supported by the GB300 engine";
-        if (c.active.act) return "the Act energy term is not supported by the GB300 engine";
     }
     const bool snapshots = ro.include_lattice || ro.topology;
     std::vector<RunPlan> plans(N);

@@ -78,6 +78,10 @@ class DeviceSims {
                              std::vector<int64_t>& sp, std::vector<int64_t>& so, std::vector<uint32_t>* lattice) const;
     std::string read_stats(size_t i, std::vector<uint64_t>& stats) const;
     std::string read_mcs(size_t i, uint64_t& mcs) const;
+    // Act term state (harness use): the per-site acquisition MCS and the
+    // completed-MCS counter.
+    std::string write_act_state(size_t i, const std::vector<uint32_t>* birth, uint64_t mcs);
+    std::string read_birth(size_t i, std::vector<uint32_t>& birth) const;
     // Topology readouts of the first ns[m] lattice snapshots of simulation
     // sims[m] (needs lattice samples), computed on the device on the
     // object's stream after the work already queued there; blocking.

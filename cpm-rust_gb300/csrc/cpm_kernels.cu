@@ -211,9 +211,14 @@ __device__ void color_pass(const SimDesc& s, const PassInfo& p, uint64_t mcs, ui
                 if (L != 0 && volume[L] <= s.min_cell_volume) { ct.guard_reject++; continue; }
                 ct.evaluated++;
                 int dl = 0, dg = 0;
-                const bool acc = decide_move<NE, uint32_t>(s, sig, adh_of, volume, interface, t, L, G, PhiloxDraw{s.seed, mcs, (uint32_t)t}, dl, dg);
+                const PhiloxDraw draw{s.seed, mcs, (uint32_t)t};
+                double dh_total = 0.0;
+                const bool acc = (s.acceptance || s.act)
+                                     ? decide_modes<NE>(s, sig, t, t + s.copy_off[k], L, G, mcs, draw, dl, dg, dh_total)
+                                     : decide_move<NE, uint32_t>(s, sig, adh_of, volume, interface, t, L, G, draw, dl, dg);
                 if (acc) {
                     commit_move<D, uint32_t>(s, sig, volume, interface, s.sum_pos, s.sum_outer, x, L, G, dl, dg);
+                    if (s.act) s.birth[t] = (uint32_t)mcs;  // energy.rs:453-458
                     ct.accepted++;
                 }
             }
@@ -365,7 +370,17 @@ __global__ void evaluate_moves_kernel(const SimDesc* simp, int64_t n, const int6
             o.topology_ok = preserves_topology<D, uint32_t>(s, s.sigma, t, o.losing, s.table2d, t3);
             if (o.topology_ok) {
                 o.volume_guard_ok = !(o.losing != 0 && s.volume[o.losing] <= s.min_cell_volume);
-                if (o.volume_guard_ok) {
+                if (o.volume_guard_ok && (s.acceptance || s.act)) {
+                    o.evaluated = 1;
+                    int dl = 0, dg = 0;
+                    double dh = 0.0;
+                    o.accepted = decide_modes<NE>(s, s.sigma, t, o.source_flat, o.losing, o.gaining, s.mcs, GivenDraw{u[i]},
+                                                  dl, dg, dh);
+                    o.accepted_sweep = o.accepted;
+                    o.delta_i_losing = dl;
+                    o.delta_i_gaining = dg;
+                    o.delta_h = dh;
+                } else if (o.volume_guard_ok) {
                     o.evaluated = 1;
                     const DeltaOut d = delta_h<NE, uint32_t>(s, s.sigma, s.adh_of, s.volume, s.interface, t, o.losing, o.gaining);
                     o.delta_i_losing = d.dl;
@@ -395,6 +410,7 @@ __global__ void commit_moves_kernel(const SimDesc* simp, int64_t n, const int64_
         int x[3];
         coords_of<D>(s, t, x);
         commit_move<D, uint32_t>(s, s.sigma, s.volume, s.interface, s.sum_pos, s.sum_outer, x, L, G, d.dl, d.dg);
+        if (s.act) s.birth[t] = (uint32_t)s.mcs;
     }
 }
 

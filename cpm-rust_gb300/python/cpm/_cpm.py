@@ -165,7 +165,8 @@ EXPORTED_SYMBOLS = (
     "cpm_engine_create", "cpm_engine_size", "cpm_engine_sim_info", "cpm_engine_run_mcs", "cpm_engine_synchronize",
     "cpm_engine_mcs", "cpm_engine_read_lattice", "cpm_engine_read_padded", "cpm_engine_read_cells",
     "cpm_engine_energy", "cpm_engine_recount_check", "cpm_engine_stats", "cpm_engine_write_state",
-    "cpm_engine_evaluate_moves", "cpm_engine_commit_moves", "cpm_engine_take_sample", "cpm_engine_destroy",
+    "cpm_engine_evaluate_moves", "cpm_engine_commit_moves", "cpm_engine_take_sample", "cpm_engine_write_act_state",
+    "cpm_engine_read_birth", "cpm_engine_destroy",
     "cpm_run_many",
     "cpm_builder_initial_state", "cpm_builder_hashes", "cpm_derive_seed_u64",
     "cpm_run_mcs_noalloc",
@@ -222,6 +223,8 @@ def _load():
     L.cpm_engine_recount_check.argtypes = [_P, SZ, ctypes.POINTER(I32), _P, _P]
     L.cpm_engine_stats.argtypes = [_P, SZ, _P]
     L.cpm_engine_take_sample.argtypes = [_P, SZ, I32, ctypes.POINTER(_P)]
+    L.cpm_engine_write_act_state.argtypes = [_P, SZ, _P, U64]
+    L.cpm_engine_read_birth.argtypes = [_P, SZ, _P]
     L.cpm_engine_write_state.argtypes = [_P, SZ, _P, _P, _P, _P, _P]
     L.cpm_engine_evaluate_moves.argtypes = [_P, SZ, SZ, _P, _P, _P, _P]
     L.cpm_engine_commit_moves.argtypes = [_P, SZ, SZ, _P, _P]
@@ -706,6 +709,17 @@ class Engine:
         s = np.zeros(32, np.uint64)
         _check(_lib.cpm_engine_stats(self._h, i, _ptr(s)))
         return {name: int(s[k]) for k, name in enumerate(STAT_NAMES)}
+
+    def write_act_state(self, birth=None, mcs=0, i=0):
+        """Act term harness: per-site acquisition MCS (padded indexing; None
+        keeps it) and the completed-MCS counter (energy.rs:329-471)."""
+        b = np.ascontiguousarray(birth, dtype=np.uint32) if birth is not None else None
+        _check(_lib.cpm_engine_write_act_state(self._h, i, _ptr(b) if b is not None else None, int(mcs)))
+
+    def read_birth(self, i=0):
+        out = np.zeros(int(self.info[i].n_padded), np.uint32)
+        _check(_lib.cpm_engine_read_birth(self._h, i, _ptr(out)))
+        return out
 
     def take_sample(self, i=0, include_lattice=False):
         """One Sample of the current state (output.rs:304-337), every readout

@@ -253,6 +253,12 @@ int cpm_engine_stats(const cpm_engine* e, size_t sim, uint64_t* out32);
  * as a result with one sample (its energy is the device's global energy of
  * the state, its mcs the MCS completed so far). Free with cpm_result_free. */
 int cpm_engine_take_sample(cpm_engine* e, size_t sim, int32_t include_lattice, cpm_result** out);
+/* Parity harness for the Act term (energy.rs:329-471): set the per-site
+ * acquisition MCS (n_padded values, padded indexing as `birth_mcs`; null
+ * keeps it) and the completed-MCS counter the activities are measured
+ * against; read the acquisition MCS back. */
+int cpm_engine_write_act_state(cpm_engine* e, size_t sim, const uint32_t* birth_padded, uint64_t mcs);
+int cpm_engine_read_birth(const cpm_engine* e, size_t sim, uint32_t* out /* n_padded */);
 /* Parity harness: overwrite the dynamic state, decide moves without
  * committing them, or apply moves in order with the sweep's commit. */
 int cpm_engine_write_state(cpm_engine* e, size_t sim, const uint32_t* padded, const uint32_t* volume,

@@ -513,6 +513,14 @@ struct Sim {
     int ntypes = 0;
     bool local_halo = false;
     std::string err;
+    // Modes of the same loop: acceptance (monte_carlo.rs:147-196; 0 =
+    // Metropolis, 1 = MetropolisHastings) and the Act term
+    // (energy.rs:329-471), off unless set.
+    int acceptance = 0;
+    bool act = false;
+    std::vector<double> lambda_act;  // per type
+    std::vector<uint32_t> max_act;   // per type
+    std::vector<uint32_t> birth;     // per padded site: MCS at which its owner acquired it
 
     int n_cells() const { return (int)type_of.size(); }
     int type_index_of(uint32_t id) const { return id == 0 ? -1 : (int)type_of[id - 1]; }
@@ -585,6 +593,55 @@ struct Sim {
     double total_delta(int64_t tf, uint32_t lo, uint32_t ga) const {
         return volume_delta(lo, ga) + interface_delta(tf, lo, ga) + adhesion_delta(tf, lo, ga);
     }
+    // ---- energy.rs:363-376 canonical_flat, 377-412 geometric_mean ----
+    int64_t act_canonical(int64_t f) const { return lat.periodic ? lat.wrapped_interior_flat(f) : f; }
+    double act_geometric_mean(int64_t site, uint32_t relevant, uint32_t mx) const {
+        const int64_t is = act_canonical(site);
+        double product = 1.0;
+        uint32_t count = 0;
+        auto consider = [&](int64_t f) {
+            const int64_t c = act_canonical(f);
+            if (lat.cells[c] != relevant) return;
+            const uint64_t b = birth[c];
+            const uint64_t elapsed = mcs > b ? mcs - b : 0;  // saturating_sub
+            const double activity = (double)((uint64_t)mx > elapsed ? (uint64_t)mx - elapsed : 0);
+            product *= activity;
+            count += 1;
+        };
+        consider(is);
+        for (int64_t off : copy_off) consider(is + off);
+        return std::pow(product, 1.0 / (double)count);
+    }
+    // energy.rs:441-451 ActTerm::delta (0 when the medium gains the site)
+    double act_delta(int64_t tf, int64_t sf, uint32_t lo, uint32_t ga) const {
+        if (ga == 0) return 0.0;
+        const int t = (int)type_of[ga - 1];
+        const double lambda = lambda_act[t];
+        const uint32_t mx = max_act[t];
+        const double gm_src = act_geometric_mean(sf, ga, mx);
+        const double gm_tgt = act_geometric_mean(tf, lo, mx);
+        return -(lambda / (double)mx) * (gm_src - gm_tgt);
+    }
+    // monte_carlo.rs:204-224 neighbour_counts over the copy stencil
+    void neighbour_counts(int64_t tf, uint32_t lo, uint32_t ga, int& na, int& nb) const {
+        na = nb = 0;
+        for (int64_t off : copy_off) {
+            const uint32_t c = lat.cells[tf + off];
+            na += c == lo;
+            nb += c == ga;
+        }
+    }
+    // monte_carlo.rs:147-196 decide_acceptance; `draw` yields gen::<f64>()
+    // and is called only where the reference draws.
+    template <class Draw> bool decide(int64_t tf, uint32_t lo, uint32_t ga, double dh, Draw draw) const {
+        if (acceptance == 0) return dh <= 0.0 || draw() < std::exp(-dh);
+        int na, nb;
+        neighbour_counts(tf, lo, ga, na, nb);
+        if (na == 0) return false;
+        const double ratio = ((double)na / (double)nb) * std::exp(-dh);
+        return draw() < std::fmin(ratio, 1.0);  // f64::min: a NaN operand yields the other
+    }
+
     // energy.rs:104-113, 203-212, 266-308: global energy for the checker.
     double global_energy() const {
         double v = 0.0;
@@ -698,6 +755,7 @@ struct Sim {
         if (ga) { volume[ga - 1] += 1; interface[ga - 1] = apply_delta(interface[ga - 1], dg); }
         update_position_sums(tf, lo, ga);
         refresh_after_commit(tf);
+        if (act) birth[tf] = (uint32_t)mcs;  // energy.rs:453-458
         energy += dh;
     }
 
@@ -722,7 +780,8 @@ struct Sim {
         r.delta_i_losing = (int32_t)std::round(dl);
         r.delta_i_gaining = (int32_t)std::round(dg);
         r.delta_h = total_delta(tf, r.losing, r.gaining);
-        r.accepted = r.delta_h <= 0.0 || u < std::exp(-r.delta_h);
+        if (act) r.delta_h = r.delta_h + act_delta(tf, r.source_flat, r.losing, r.gaining);
+        r.accepted = decide(tf, r.losing, r.gaining, r.delta_h, [u] { return u; });
     }
     bool attempt_at(int64_t tf) {
         const int k = (int)gen_range(rng, 0, copy_off.size());
@@ -732,7 +791,10 @@ struct Sim {
         if (!preserves_topology(tf, lo)) return false;
         if (lo != 0 && volume[lo - 1] <= cfg.min_cell_volume) return false;
         const double dh = total_delta(tf, lo, ga);
-        const bool acc = dh <= 0.0 || gen_f64(rng) < std::exp(-dh);
+        // Act steers the decision but never reaches the conservative energy
+        // (monte_carlo.rs:82-97)
+        const double dh_all = act ? dh + act_delta(tf, sf, lo, ga) : dh;
+        const bool acc = decide(tf, lo, ga, dh_all, [this] { return gen_f64(rng); });
         if (acc) commit(tf, lo, ga, dh);
         return acc;
     }
@@ -1122,6 +1184,30 @@ void* orc_new(int D, const int* grid, int periodic, int copy_kind, int energy_ki
     return s;
 }
 void orc_free(void* h) { delete (Sim*)h; }
+// Act term harness: acquisition MCS per padded site (null keeps it) and the
+// completed-MCS counter; the Act delta-H of one proposed copy.
+void orc_set_act_state(void* h, const uint32_t* birth, uint64_t mcs) {
+    Sim* s = (Sim*)h;
+    if (birth && s->act) std::copy(birth, birth + s->birth.size(), s->birth.begin());
+    s->mcs = mcs;
+}
+void orc_get_birth(void* h, uint32_t* out) { Sim* s = (Sim*)h; std::copy(s->birth.begin(), s->birth.end(), out); }
+double orc_act_delta(void* h, int64_t target_flat, int64_t source_flat) {
+    Sim* s = (Sim*)h;
+    return s->act_delta(target_flat, source_flat, s->lat.cells[target_flat], s->lat.cells[source_flat]);
+}
+// Acceptance (0 Metropolis, 1 MetropolisHastings) and the Act term (null
+// lambda_act = off); before the first MCS.
+void orc_set_modes(void* h, int acceptance, const double* lambda_act, const uint32_t* max_act) {
+    Sim* s = (Sim*)h;
+    s->acceptance = acceptance;
+    s->act = lambda_act != nullptr;
+    if (s->act) {
+        s->lambda_act.assign(lambda_act, lambda_act + s->ntypes);
+        s->max_act.assign(max_act, max_act + s->ntypes);
+        s->birth.assign((size_t)s->lat.n_padded(), 0u);
+    }
+}
 void orc_set_local_halo(void* h, int on) { ((Sim*)h)->local_halo = on != 0; }
 int orc_init_explicit(void* h, const uint32_t* lattice, int64_t n_sites, const uint32_t* cell_type_of, int n_cells, char* err, int errlen) {
     Sim* s = (Sim*)h;
@@ -1253,7 +1339,8 @@ int orc_run_many(int D, const int* grid, int periodic, int copy_kind, int energy
                  const uint64_t* cell_counts, const double* adhesion,
                  const uint32_t* explicit_lattice, const uint32_t* explicit_type_of, int explicit_n_cells,
                  int n_runs, const uint64_t* seeds, uint64_t burn_in, uint64_t readout, int threads, int local_halo,
-                 int max_cells, orc_cell_sample* out_cells, double* out_energy, int* out_n_cells) {
+                 int max_cells, orc_cell_sample* out_cells, double* out_energy, int* out_n_cells, int acceptance,
+                 const double* lambda_act, const uint32_t* max_act) {
     std::atomic<int> next{0}, failed{0};
     if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
     std::vector<std::thread> th;
@@ -1268,6 +1355,7 @@ int orc_run_many(int D, const int* grid, int periodic, int copy_kind, int energy
                                        seeds[r], 1, err, sizeof err);
                 if (!s) { failed++; out_n_cells[r] = 0; continue; }
                 s->local_halo = local_halo != 0;
+                orc_set_modes(s, acceptance, lambda_act, max_act);
                 bool ok = explicit_lattice
                               ? s->place_explicit(explicit_lattice, s->lat.n_sites(), explicit_type_of, explicit_n_cells)
                               : s->scatter_and_grow();

@@ -105,6 +105,11 @@ def lib():
                 ctypes.c_int, P, P, P, P, P, P, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_char_p, ctypes.c_int,
             ]
             L.orc_free.argtypes = [P]
+            L.orc_set_modes.argtypes = [P, ctypes.c_int, P, P]
+            L.orc_set_act_state.argtypes = [P, P, ctypes.c_uint64]
+            L.orc_get_birth.argtypes = [P, P]
+            L.orc_act_delta.argtypes = [P, ctypes.c_int64, ctypes.c_int64]
+            L.orc_act_delta.restype = ctypes.c_double
             L.orc_set_local_halo.argtypes = [P, ctypes.c_int]
             L.orc_init_explicit.argtypes = [P, P, ctypes.c_int64, P, ctypes.c_int, ctypes.c_char_p, ctypes.c_int]
             L.orc_init_default.argtypes = [P, ctypes.c_char_p, ctypes.c_int]
@@ -144,7 +149,7 @@ def lib():
                 ctypes.c_int, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                 ctypes.c_int, P, P, P, P, P, P, P, P, ctypes.c_int,
                 ctypes.c_int, P, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, ctypes.c_int,
-                ctypes.c_int, P, P, P,
+                ctypes.c_int, P, P, P, ctypes.c_int, P, P,
             ]
             _lib = L
         return _lib
@@ -158,7 +163,7 @@ class ModelSpec:
     """Plain description of one model configuration (the oracle's input)."""
 
     def __init__(self, grid, periodic, types, adhesion, cell_counts=None, copy="von_neumann",
-                 energy=None, connectivity="von_neumann", min_cell_volume=1):
+                 energy=None, connectivity="von_neumann", min_cell_volume=1, acceptance="metropolis", act=None):
         self.grid = [int(g) for g in grid]
         self.D = len(self.grid)
         self.periodic = bool(periodic)
@@ -170,6 +175,18 @@ class ModelSpec:
         self.energy = energy if energy is not None else ("moore" if self.D == 2 else "eighteen")
         self.connectivity = connectivity
         self.min_cell_volume = int(min_cell_volume)
+        # monte_carlo.rs:147-196: "metropolis" or "metropolis_hastings"
+        self.acceptance = acceptance
+        # energy.rs:329-471: None (off) or per type (lambda_act, max_act)
+        self.act = [tuple(a) for a in act] if act is not None else None
+
+    def mode_args(self):
+        """(acceptance code, lambda_act array or None, max_act array or None)."""
+        acc = {"metropolis": 0, "metropolis_hastings": 1}[self.acceptance]
+        if self.act is None:
+            return acc, None, None
+        return (acc, np.ascontiguousarray([a[0] for a in self.act], dtype=np.float64),
+                np.ascontiguousarray([a[1] for a in self.act], dtype=np.uint32))
 
     def arrays(self):
         n = len(self.types)
@@ -198,12 +215,28 @@ class OracleSim:
         if not h:
             raise ValueError(err.value.decode())
         self.h = ctypes.c_void_p(h)
+        acc, la, ma = spec.mode_args()
+        if acc or la is not None:
+            self._modes = (la, ma)
+            L.orc_set_modes(self.h, acc, _ptr(la) if la is not None else None, _ptr(ma) if ma is not None else None)
 
     def __del__(self):
         h = getattr(self, "h", None)
         if h is not None and _lib is not None:
             _lib.orc_free(h)
             self.h = None
+
+    def set_act_state(self, birth=None, mcs=0):
+        b = np.ascontiguousarray(birth, dtype=np.uint32) if birth is not None else None
+        lib().orc_set_act_state(self.h, _ptr(b) if b is not None else None, int(mcs))
+
+    def birth(self):
+        out = np.zeros(self.n_padded, np.uint32)
+        lib().orc_get_birth(self.h, _ptr(out))
+        return out
+
+    def act_delta(self, target_flat, source_flat):
+        return lib().orc_act_delta(self.h, int(target_flat), int(source_flat))
 
     def set_local_halo(self, on: bool):
         lib().orc_set_local_halo(self.h, int(on))
@@ -373,6 +406,7 @@ def run_many(spec: ModelSpec, seeds, burn_in: int, readout: int, threads: int = 
     (lattice, cell_type_of)); returns per-run last-sample cell summaries."""
     L = lib()
     grid, tv, ti, lv, li, cc, adh = spec.arrays()
+    acc, la, ma = spec.mode_args()
     seeds = np.ascontiguousarray(np.asarray(seeds, dtype=np.uint64))
     if max_cells is None:
         max_cells = int(sum(spec.cell_counts)) if explicit is None else len(explicit[1])
@@ -388,5 +422,6 @@ def run_many(spec: ModelSpec, seeds, burn_in: int, readout: int, threads: int = 
     failed = L.orc_run_many(spec.D, _ptr(grid), int(spec.periodic), NBH[spec.copy], NBH[spec.energy],
                             NBH[spec.connectivity], len(spec.types), _ptr(tv), _ptr(ti), _ptr(lv), _ptr(li),
                             _ptr(cc), _ptr(adh), elp, etp, en, seeds.size, _ptr(seeds), burn_in, readout,
-                            threads, int(local_halo), max_cells, _ptr(out_cells), _ptr(out_energy), _ptr(out_n))
+                            threads, int(local_halo), max_cells, _ptr(out_cells), _ptr(out_energy), _ptr(out_n),
+                            acc, _ptr(la) if la is not None else None, _ptr(ma) if ma is not None else None)
     return failed, out_cells.reshape(seeds.size, max_cells), out_energy, out_n

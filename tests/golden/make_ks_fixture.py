@@ -10,7 +10,13 @@ final energy; and (`fluct_oracle_summary.npz`) the per-seed summaries of a
 second configuration sized for the tiled sweep — 84x84 periodic, one type
 V*=40 I*=30 lambda_V=3 lambda_I=0.6, 80 cells, J=[[0,6.5],[6.5,2.2]],
 2000 burn-in + 1000 readout MCS, seeds 1..160 — whose state is stationary
-well before the sample. Usage: python tests/golden/make_ks_fixture.py
+well before the sample; and (`modes_oracle_summary.npz`, `--modes`) the
+same summaries for the loop's other modes on a 40x40 periodic lattice with
+one type (V*=40, I*=30, lambda_V=3, lambda_I=0.6, 20 cells,
+J=[[0,6.5],[6.5,2.2]], 1000 burn-in + 500 readout MCS, seeds 1..160): with
+Metropolis-Hastings acceptance (monte_carlo.rs:168-196) and with the Act
+term (energy.rs:329-471; lambda_act = 20, max_act = 20).
+Usage: python tests/golden/make_ks_fixture.py [--fluct | --modes]
 """
 
 import os
@@ -56,6 +62,32 @@ def fluct_main():
     print("wrote", os.path.join(HERE, "fluct_oracle_summary.npz"))
 
 
+MODES_SEEDS = 160
+MODES_BURN_IN, MODES_READOUT = 1000, 500
+MODES = {"mh": dict(acceptance="metropolis_hastings"), "act": dict(act=[(20.0, 20)])}
+
+
+def modes_spec(mode):
+    return O.ModelSpec((40, 40), True, [(40, 30, 3.0, 0.6)], [[0, 6.5], [6.5, 2.2]], cell_counts=[20], **MODES[mode])
+
+
+def modes_main():
+    seeds = np.arange(1, MODES_SEEDS + 1, dtype=np.uint64)
+    out = {"seeds": seeds}
+    for mode in MODES:
+        failed, cells, energy, n = O.run_many(modes_spec(mode), seeds, MODES_BURN_IN, MODES_READOUT, threads=0,
+                                              local_halo=True)
+        assert failed == 0 and np.all(n == 20)
+        v = cells["volume"].astype(np.float64)
+        i = cells["interface"].astype(np.float64)
+        out[f"{mode}_energy"] = energy
+        out[f"{mode}_mean_volume"] = v.mean(1)
+        out[f"{mode}_volume_std"] = v.std(1)
+        out[f"{mode}_mean_interface"] = i.mean(1)
+    np.savez_compressed(os.path.join(HERE, "modes_oracle_summary.npz"), **out)
+    print("wrote", os.path.join(HERE, "modes_oracle_summary.npz"))
+
+
 def main():
     seeds = np.arange(1, N_SEEDS + 1, dtype=np.uint64)
     failed, cells, energy, n = O.run_many(c1_spec(), seeds, BURN_IN, READOUT, threads=0, local_halo=True)
@@ -75,6 +107,9 @@ def main():
 if __name__ == "__main__":
     if "--fluct" in sys.argv:
         fluct_main()
+    elif "--modes" in sys.argv:
+        modes_main()
     else:
         main()
         fluct_main()
+        modes_main()

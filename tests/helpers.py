@@ -13,7 +13,10 @@ NBH_DEFAULT = {2: "moore", 3: "eighteen"}
 class Model:
     """A model description both engines can be built from."""
 
-    def __init__(self, grid, boundary, types, adhesion, counts=None, energy=None, seed=1):
+    def __init__(self, grid, boundary, types, adhesion, counts=None, energy=None, seed=1, acceptance="metropolis",
+                 act=None):
+        self.acceptance = acceptance  # "metropolis" or "metropolis_hastings"
+        self.act = [tuple(a) for a in act] if act is not None else None  # per type (lambda_act, max_act)
         self.grid = tuple(int(g) for g in grid)
         self.D = len(self.grid)
         self.boundary = boundary
@@ -25,7 +28,8 @@ class Model:
 
     def spec(self):
         return O.ModelSpec(self.grid, self.boundary == "periodic", [t[1:] for t in self.types], self.adhesion,
-                           cell_counts=self.counts, energy=self.energy or NBH_DEFAULT[self.D])
+                           cell_counts=self.counts, energy=self.energy or NBH_DEFAULT[self.D],
+                           acceptance=self.acceptance, act=self.act)
 
     def oracle(self, seed=None, lattice=None, cell_type_of=None, local_halo=True):
         sim = O.OracleSim(self.spec(), self.seed if seed is None else seed)
@@ -40,9 +44,14 @@ class Model:
         from cpm import _cpm
 
         b = _cpm.CPM(grid=list(self.grid), boundary=self.boundary, seed=self.seed if seed is None else seed,
-                     energy_neighborhood=self.energy)
-        for t in self.types:
-            b.register_cell_type(*t)
+                     energy_neighborhood=self.energy,
+                     acceptance=None if self.acceptance == "metropolis" else self.acceptance,
+                     active_terms={"act": True} if self.act is not None else None)
+        for k, t in enumerate(self.types):
+            if self.act is not None:
+                b.register_cell_type(*t, lambda_act=float(self.act[k][0]), max_act=int(self.act[k][1]))
+            else:
+                b.register_cell_type(*t)
         for t, n in zip(self.types, self.counts):
             b.add_cells(t[0], n)
         b.set_adhesion(self.adhesion)
