@@ -365,6 +365,15 @@ def run_serve_bench(args):
             lat[i] = tm["finished_s"] - tm["submitted_s"]
         wall = time.perf_counter() - t0
         stats = srv.stats()
+    # saturation: the same requests all submitted at once (what the server
+    # sustains when arrivals outpace it)
+    with cpm.Server() as srv:
+        t1 = time.perf_counter()
+        tickets = [srv.submit(sim, q["burn"], q["readout"], q["interval"]) for q, sim in zip(reqs, sims)]
+        for t in tickets:
+            st, res, tm = srv.wait(t)
+            assert st == "done", st
+        sat_wall = time.perf_counter() - t1
     lat = np.array(lat)
     alone = np.array(alone)
     ratio = lat / alone
@@ -382,6 +391,9 @@ def run_serve_bench(args):
         "attempts_per_s": float(sum(attempts)) / wall,
         "offered_attempts_per_s": float(sum(attempts)) / reqs[-1]["arrival"],
         "wall_s": wall,
+        "saturation": {"attempts_per_s": float(sum(attempts)) / sat_wall, "sims_per_s": len(reqs) / sat_wall,
+                       "wall_s": sat_wall, "isolated_sum_s": float(alone.sum()),
+                       "how": "all requests submitted at once"},
         "peak_active": stats["peak_active"],
         "peak_device_bytes": stats["peak_bytes"],
         "requests": [[q["D"], q["side"], q["burn"] + q["readout"], round(a, 3), round(m, 3)]

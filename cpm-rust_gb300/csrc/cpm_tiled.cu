@@ -518,12 +518,18 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
     __shared__ SimDesc gsd, lsd;
     __shared__ int s_n, s_tile, s_ncell, s_box_dims[3], s_gx0[3], s_tcnt[3];
     __shared__ int perm[8], sperm[27];
-    __shared__ uint32_t s_pkey[8];
+    __shared__ uint32_t s_pkey[27];
+    __shared__ int s_ncls[3];
     __shared__ unsigned long long sstat[8];
     const int tid = threadIdx.x;
     if (tid == 0) gsd = *simp;
     if (tid < 8) sstat[tid] = 0;
     __syncthreads();
+    // site colours per axis: the two parities, plus the last coordinate of
+    // an odd periodic axis as a third
+    if (tid < 3) s_ncls[tid] = tid < D ? ((gsd.periodic && (gsd.dims[tid] & 1)) ? 3 : 2) : 1;
+    __syncthreads();
+    const int n_cls = s_ncls[0] * s_ncls[1] * s_ncls[2];
     if (tables_in_smem && gsd.dj32 != nullptr) {
         // the float energy tables move next to the tile state (no global
         // loads in the common-case decision)
@@ -715,7 +721,7 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                 }
                 // the tile's site-colour order and pass keys
                 if (tid == 0) {
-                    const int ncol = 1 << D;
+                    const int ncol = n_cls;
                     for (int c = 0; c < ncol; ++c) sperm[c] = c;
                     for (int c = ncol - 1; c > 0; --c) {
                         const uint4 rr = aux_draw(g.seed, mcs, TAG_TILE, 2u + (uint32_t)k, (uint32_t)c);
@@ -723,7 +729,7 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                         const int t = sperm[c]; sperm[c] = sperm[j]; sperm[j] = t;
                     }
                 }
-                if (tid < (1 << D))
+                if (tid < n_cls)
                     s_pkey[tid] = aux_draw(g.seed, mcs, TAG_PASS, (uint32_t)(tid * 64 + ci), (uint32_t)k).x;
                 __syncthreads();
                 const int nc = s_ncell;
@@ -812,18 +818,42 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                 long long t_p0 = clock64();
                 cyc_stage += t_p0 - t_s0;
                 // site-colour passes of this tile, in the order staged with the box
-                const int ncol = 1 << D;
-                for (int pi = 0; pi < ncol; ++pi) {
-                    const int sc = sperm[pi];
-                    // local sites with global coordinate parity == colour bit
-                    int cnt[3], base[3];
+                for (int pi = 0; pi < n_cls; ++pi) {
+                    int sc = sperm[pi];
+                    // The local sites whose global coordinate has colour sc_d on
+                    // every axis d: the parity, or (odd periodic axis) 2 for the
+                    // last coordinate L-1, whose neighbour across the wrap (0)
+                    // has its parity. Per axis they are first_a + 2i for
+                    // i < cnt_a, then (past the wrap) base_b + 2(i - cnt_a).
+                    int cnt[3], base[3], cnt_a[3], base_b[3];
                     int n_class = 1;
                     for (int d = 0; d < D; ++d) {
-                        const int want = (sc >> d) & 1;
-                        const int g0 = ((s_gx0[d] % g.dims[d]) + g.dims[d]) % g.dims[d];
-                        const int first = (want - (g0 & 1)) & 1;  // first local offset with that parity
-                        base[d] = first;
-                        cnt[d] = s_tcnt[d] > first ? (s_tcnt[d] - first + 1) / 2 : 0;
+                        const int Ld = g.dims[d];
+                        const int want = sc % s_ncls[d];
+                        sc /= s_ncls[d];
+                        const int g0 = ((s_gx0[d] % Ld) + Ld) % Ld;
+                        const int tc = s_tcnt[d];
+                        if (s_ncls[d] == 2) {
+                            const int first = (want - (g0 & 1)) & 1;  // first local offset with that parity
+                            base[d] = first;
+                            cnt[d] = tc > first ? (tc - first + 1) / 2 : 0;
+                            cnt_a[d] = cnt[d];
+                            base_b[d] = 0;
+                        } else {
+                            const int w = Ld - g0;  // local offsets before the wrap: g0 + i <= L - 1
+                            if (want == 2) {
+                                base[d] = w - 1;
+                                cnt[d] = cnt_a[d] = w - 1 < tc ? 1 : 0;
+                                base_b[d] = 0;
+                            } else {
+                                const int end_a = w - 1 < tc ? w - 1 : tc;  // g0 + i < L - 1
+                                const int first = (want - (g0 & 1)) & 1;
+                                base[d] = first;
+                                cnt_a[d] = end_a > first ? (end_a - first + 1) / 2 : 0;
+                                base_b[d] = w + want;  // past the wrap: g = i - w
+                                cnt[d] = cnt_a[d] + (tc > base_b[d] ? (tc - base_b[d] + 1) / 2 : 0);
+                            }
+                        }
                         n_class *= cnt[d];
                     }
                     const uint32_t pass_key = s_pkey[pi];
@@ -841,7 +871,8 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                             for (int d = D - 1; d >= 0; --d) {
                                 const int i = r % cnt[d];
                                 r /= cnt[d];
-                                t += (base[d] + 2 * i + 1) * (int)lsd.strides[d];
+                                const int li = i < cnt_a[d] ? base[d] + 2 * i : base_b[d] + 2 * (i - cnt_a[d]);
+                                t += (li + 1) * (int)lsd.strides[d];
                             }
                             gf = (int)sgf[t];
                             kd = skd[t];
@@ -973,13 +1004,13 @@ static int tiled_index(int D, int NE) {
 }
 
 bool tiled_plan(int D, const int* dims, int periodic, int* nt, int* max_box) {
+    (void)periodic;  // odd periodic axes take a third site colour in the kernel
     int box = 1, klass = 1;
     // target tile widths: 21 in 2D (cells of ~50 sites are ~8 wide), 12 in
     // 3D (more tiles per colour: 8 colours there)
     const int target = D == 2 ? 21 : 12;
     for (int d = 0; d < D; ++d) {
         const int L = dims[d];
-        if (periodic && (L & 1)) return false;  // odd periodic axes need a third site colour
         int n = L / target;
         if (n & 1) n -= 1;
         // small 3D lattices: 4 tiles per axis (8 per colour) while tiles

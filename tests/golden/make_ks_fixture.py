@@ -16,7 +16,10 @@ one type (V*=40, I*=30, lambda_V=3, lambda_I=0.6, 20 cells,
 J=[[0,6.5],[6.5,2.2]], 1000 burn-in + 500 readout MCS, seeds 1..160): with
 Metropolis-Hastings acceptance (monte_carlo.rs:168-196) and with the Act
 term (energy.rs:329-471; lambda_act = 20, max_act = 20).
-Usage: python tests/golden/make_ks_fixture.py [--fluct | --modes]
+And (`odd_oracle_summary.npz`, `--odd`) a lattice with odd periodic sides,
+69x67, one type (V*=40, I*=30, lambda_V=3, lambda_I=0.6, 60 cells,
+J=[[0,6.5],[6.5,2.2]], 1000 burn-in + 500 readout MCS, seeds 1..96).
+Usage: python tests/golden/make_ks_fixture.py [--fluct | --modes | --odd]
 """
 
 import os
@@ -88,6 +91,25 @@ def modes_main():
     print("wrote", os.path.join(HERE, "modes_oracle_summary.npz"))
 
 
+ODD_SEEDS = 96
+ODD_BURN_IN, ODD_READOUT = 1000, 500
+
+
+def odd_spec():
+    return O.ModelSpec((69, 67), True, [(40, 30, 3.0, 0.6)], [[0, 6.5], [6.5, 2.2]], cell_counts=[60])
+
+
+def odd_main():
+    seeds = np.arange(1, ODD_SEEDS + 1, dtype=np.uint64)
+    failed, cells, energy, n = O.run_many(odd_spec(), seeds, ODD_BURN_IN, ODD_READOUT, threads=0, local_halo=True)
+    assert failed == 0 and np.all(n == 60)
+    v = cells["volume"].astype(np.float64)
+    i = cells["interface"].astype(np.float64)
+    np.savez_compressed(os.path.join(HERE, "odd_oracle_summary.npz"), seeds=seeds, energy=energy,
+                        mean_volume=v.mean(1), volume_std=v.std(1), mean_interface=i.mean(1))
+    print("wrote", os.path.join(HERE, "odd_oracle_summary.npz"))
+
+
 def main():
     seeds = np.arange(1, N_SEEDS + 1, dtype=np.uint64)
     failed, cells, energy, n = O.run_many(c1_spec(), seeds, BURN_IN, READOUT, threads=0, local_halo=True)
@@ -109,7 +131,10 @@ if __name__ == "__main__":
         fluct_main()
     elif "--modes" in sys.argv:
         modes_main()
+    elif "--odd" in sys.argv:
+        odd_main()
     else:
         main()
         fluct_main()
         modes_main()
+        odd_main()

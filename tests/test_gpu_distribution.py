@@ -96,3 +96,33 @@ def test_fluctuating_cells_match_oracle_on_both_sweeps(path, cuda_required, monk
     if path == "tiled":
         assert st["passes"] > 0 and st["spin_timeouts"] == 0
         assert st["deferred"] <= 0.001 * st["nonnull"]
+
+
+@pytest.mark.parametrize("path", ["tiled", "resident"])
+def test_odd_periodic_sides_match_oracle(path, cuda_required, monkeypatch):
+    """Odd periodic sides (69x67): the site colouring takes a third colour
+    for the last coordinate of each odd axis (its neighbour across the wrap
+    has its parity); per-seed summaries against the oracle's over 96 seeds
+    (fixture tests/golden/odd_oracle_summary.npz), KS p > 0.01."""
+    from scipy.stats import ks_2samp
+
+    from cpm import _cpm
+    from helpers import Model
+
+    if path == "tiled":
+        monkeypatch.setenv("CPM_GPU_FORCE_TILED", "1")
+    ref = np.load(os.path.join(HERE, "golden", "odd_oracle_summary.npz"))
+    builders = [Model((69, 67), "periodic", [("a", 40, 30, 3.0, 0.6)], [[0, 6.5], [6.5, 2.2]], [60],
+                      seed=int(s)).builder(warn=False) for s in ref["seeds"]]
+    results = _cpm.run_many(builders, 1000, 500, 500, topology=False)
+    last = [r.samples[-1] for r in results]
+    v = np.stack([s.volume for s in last]).astype(np.float64)
+    i = np.stack([s.interface for s in last]).astype(np.float64)
+    gpu = {"energy": np.array([s.conservative_energy for s in last]), "mean_volume": v.mean(1),
+           "volume_std": v.std(1), "mean_interface": i.mean(1)}
+    pvals = {k: ks_2samp(np.asarray(ref[k]), gpu[k]).pvalue for k in gpu}
+    print(path, "KS p-values:", pvals)
+    for k, p in pvals.items():
+        assert p > 0.01, (k, pvals)
+    if path == "tiled":
+        assert results[0].stats["passes"] > 0

@@ -308,6 +308,12 @@ TILED_MODELS = {
                                     [[0, 16, 16], [16, 3.3, 9.1], [16, 9.1, 2.7]], [25, 25], seed=13),
     "tiled_3d_periodic": lambda: organoid_model(side=32, counts=(30, 30), seed=14),
     "tiled_3d_fixed": lambda: organoid_model(side=32, boundary="fixed", energy="eighteen", counts=(20, 20), seed=15),
+    # odd periodic sides: a third site colour for the last coordinate of each odd axis
+    "tiled_2d_odd_periodic": lambda: Model((65, 63), "periodic", [("a", 50, 30, 5.0, 1.0), ("b", 50, 30, 5.0, 1.0)],
+                                           [[0, 16, 16], [16, 3.3, 9.1], [16, 9.1, 2.7]], [25, 25], seed=18),
+    "tiled_3d_odd_periodic": lambda: Model((33, 31, 35), "periodic", [("a", 60, 90, 2.0, 0.5), ("b", 60, 90, 2.0, 0.5)],
+                                           [[0, 16, 16], [16, 4, 9], [16, 9, 5]], [30, 30], energy="twenty_six",
+                                           seed=19),
 }
 
 
@@ -348,14 +354,17 @@ def test_tiled_sweep_keeps_exact_state(name, cuda_required, monkeypatch):
     assert np.array_equal(again.lattice(), lat)
 
 
-@pytest.mark.parametrize("D", [2, 3])
+@pytest.mark.parametrize("D", [2, 3, "2odd"])
 def test_tiled_sweep_independent_of_grid(D, cuda_required, monkeypatch):
     """Tiles, claims and priorities are functions of (seed, MCS, tile id): a
     grid with several tiles per CTA gives the same trajectory as one tile
     per CTA."""
     monkeypatch.setenv("CPM_GPU_FORCE_TILED", "1")
-    model = sorting_model(side=128, seed=16) if D == 2 else organoid_model(side=64, counts=(60, 60), seed=17)
-    n = 12 if D == 2 else 3
+    if D == "2odd":
+        model = Model((129, 127), "periodic", [("a", 50, 30, 5.0, 1.0)], [[0, 12], [12, 3]], [200], seed=20)
+    else:
+        model = sorting_model(side=128, seed=16) if D == 2 else organoid_model(side=64, counts=(60, 60), seed=17)
+    n = 3 if D == 3 else 12
     wide = _engine(model)
     wide.run_mcs(n)
     wide.synchronize()

@@ -221,3 +221,45 @@ def test_batch_workload_theta_round_trip():
         sim = bench.batch_sim(side, th, seed=3)
         assert sim.extract_theta() == th
         assert len(th) == len(sim.theta_names()) == 14
+
+
+def _tile_classes(L, g0, tc, periodic):
+    """The tiled sweep's site colours along one axis of a tile (the
+    arithmetic of the kernel's site-colour passes, restated): for each
+    colour, the local offsets it visits."""
+    ncls = 3 if periodic and L % 2 else 2
+    out = []
+    for want in range(ncls):
+        if ncls == 2:
+            first = (want - (g0 & 1)) & 1
+            cnt = (tc - first + 1) // 2 if tc > first else 0
+            out.append([first + 2 * i for i in range(cnt)])
+            continue
+        w = L - g0
+        if want == 2:
+            out.append([w - 1] if w - 1 < tc else [])
+            continue
+        end_a = w - 1 if w - 1 < tc else tc
+        first = (want - (g0 & 1)) & 1
+        cnt_a = (end_a - first + 1) // 2 if end_a > first else 0
+        base_b = w + want
+        cnt_b = (tc - base_b + 1) // 2 if tc > base_b else 0
+        out.append([first + 2 * i for i in range(cnt_a)] + [base_b + 2 * i for i in range(cnt_b)])
+    return out
+
+
+def test_tiled_site_colours_partition_the_tile_into_non_adjacent_sets():
+    """Every site of a tile is visited once per MCS, and no two sites of one
+    colour are neighbours, across the periodic wrap included (odd sides: the
+    last coordinate takes a third colour)."""
+    for L in list(range(3, 40)) + [127, 129]:
+        for periodic in (True, False):
+            for tc in range(1, L):
+                for g0 in range(L if periodic else 1):
+                    classes = _tile_classes(L, g0, tc, periodic)
+                    seen = sorted(i for c in classes for i in c)
+                    assert seen == list(range(tc)), (L, g0, tc, classes)
+                    for c in classes:
+                        gl = {(g0 + i) % L for i in c}
+                        for x in gl:
+                            assert (x + 1) % L not in gl or L == 1, (L, g0, tc, c)
