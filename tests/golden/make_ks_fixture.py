@@ -17,8 +17,9 @@ J=[[0,6.5],[6.5,2.2]], 1000 burn-in + 500 readout MCS, seeds 1..160): with
 Metropolis-Hastings acceptance (monte_carlo.rs:168-196) and with the Act
 term (energy.rs:329-471; lambda_act = 20, max_act = 20).
 And (`odd_oracle_summary.npz`, `--odd`) a lattice with odd periodic sides,
-69x67, one type (V*=40, I*=30, lambda_V=3, lambda_I=0.6, 60 cells,
-J=[[0,6.5],[6.5,2.2]], 1000 burn-in + 500 readout MCS, seeds 1..96).
+31x29, one type (V*=50, I*=75, lambda_V=10, lambda_I=2, 5 cells) whose cells
+repel (J=[[0,3],[3,12]]), so the state is stationary by the sample with no
+slow aggregation (2000 burn-in + 2000 readout MCS, seeds 1..96).
 Usage: python tests/golden/make_ks_fixture.py [--fluct | --modes | --odd]
 """
 
@@ -92,17 +93,17 @@ def modes_main():
 
 
 ODD_SEEDS = 96
-ODD_BURN_IN, ODD_READOUT = 1000, 500
+ODD_BURN_IN, ODD_READOUT = 2000, 2000
 
 
 def odd_spec():
-    return O.ModelSpec((69, 67), True, [(40, 30, 3.0, 0.6)], [[0, 6.5], [6.5, 2.2]], cell_counts=[60])
+    return O.ModelSpec((31, 29), True, [(50, 75, 10.0, 2.0)], [[0, 3], [3, 12]], cell_counts=[5])
 
 
 def odd_main():
     seeds = np.arange(1, ODD_SEEDS + 1, dtype=np.uint64)
     failed, cells, energy, n = O.run_many(odd_spec(), seeds, ODD_BURN_IN, ODD_READOUT, threads=0, local_halo=True)
-    assert failed == 0 and np.all(n == 60)
+    assert failed == 0 and np.all(n == 5)
     v = cells["volume"].astype(np.float64)
     i = cells["interface"].astype(np.float64)
     np.savez_compressed(os.path.join(HERE, "odd_oracle_summary.npz"), seeds=seeds, energy=energy,

@@ -100,10 +100,11 @@ def test_fluctuating_cells_match_oracle_on_both_sweeps(path, cuda_required, monk
 
 @pytest.mark.parametrize("path", ["tiled", "resident"])
 def test_odd_periodic_sides_match_oracle(path, cuda_required, monkeypatch):
-    """Odd periodic sides (69x67): the site colouring takes a third colour
+    """Odd periodic sides (31x29): the site colouring takes a third colour
     for the last coordinate of each odd axis (its neighbour across the wrap
     has its parity); per-seed summaries against the oracle's over 96 seeds
-    (fixture tests/golden/odd_oracle_summary.npz), KS p > 0.01."""
+    (fixture tests/golden/odd_oracle_summary.npz: repelling cells, stationary
+    by the sample), KS p > 0.01."""
     from scipy.stats import ks_2samp
 
     from cpm import _cpm
@@ -112,9 +113,9 @@ def test_odd_periodic_sides_match_oracle(path, cuda_required, monkeypatch):
     if path == "tiled":
         monkeypatch.setenv("CPM_GPU_FORCE_TILED", "1")
     ref = np.load(os.path.join(HERE, "golden", "odd_oracle_summary.npz"))
-    builders = [Model((69, 67), "periodic", [("a", 40, 30, 3.0, 0.6)], [[0, 6.5], [6.5, 2.2]], [60],
+    builders = [Model((31, 29), "periodic", [("a", 50, 75, 10.0, 2.0)], [[0, 3], [3, 12]], [5],
                       seed=int(s)).builder(warn=False) for s in ref["seeds"]]
-    results = _cpm.run_many(builders, 1000, 500, 500, topology=False)
+    results = _cpm.run_many(builders, 2000, 2000, 2000, topology=False)
     last = [r.samples[-1] for r in results]
     v = np.stack([s.volume for s in last]).astype(np.float64)
     i = np.stack([s.interface for s in last]).astype(np.float64)
