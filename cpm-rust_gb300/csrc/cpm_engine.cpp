@@ -1103,9 +1103,6 @@ std::string run_many(const std::vector<Config>& configs, const std::vector<Initi
     const size_t N = configs.size();
     out.assign(N, Result());
     if (N == 0) return "";
-    for (auto& c : configs) {
-        if (c.proposal != PROP_UNIFORM) return "proposal = edge_list is not supported by the GB300 engine";
-    }
     const bool snapshots = ro.include_lattice || ro.topology;
     std::vector<RunPlan> plans(N);
     std::vector<int> ns(N), ne(N), nt(N);

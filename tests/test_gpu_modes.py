@@ -142,3 +142,26 @@ def test_mode_distributions_match_oracle(mode, cuda_required):
     print(mode, "KS p-values:", pvals)
     for k, p in pvals.items():
         assert p > 0.01, (k, pvals)
+
+
+def test_edge_list_proposal_runs_the_uniform_chain(cuda_required):
+    """proposal = "edge_list" (monte_carlo.rs:336-352) is the Uniform chain
+    with its null attempts removed (edge_list.rs:1-16); the device sweep
+    runs the same chain for both, so the samples are identical and only the
+    convention hash records the choice."""
+    import cpm
+
+    def sim(proposal):
+        s = cpm.CPM(grid=(40, 40), boundary="periodic", seed=9, proposal=proposal)
+        s.register_cell_type("a", 40, 30, 3.0, 0.6)
+        s.add_cells("a", 12)
+        s.set_adhesion([[0, 6.5], [6.5, 2.2]])
+        s.initialize(warn_on_default_init=False)
+        return s.run(200, 200, 100)
+
+    u, e = sim("uniform"), sim("edge_list")
+    assert len(u.samples) == len(e.samples) == 2
+    for a, b in zip(u.samples, e.samples):
+        assert np.array_equal(a.volume, b.volume) and np.array_equal(a.interface, b.interface)
+        assert a.conservative_energy == b.conservative_energy
+    assert u.metadata.convention_hash != e.metadata.convention_hash
