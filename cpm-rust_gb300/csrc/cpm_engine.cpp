@@ -432,7 +432,9 @@ std::string DeviceSims::run_tiled(const RunPlan& p, const uint64_t* t3) {
     const int tables_in_smem = smem + tab <= cpmgpu::resident_smem_limit();
     if (tables_in_smem) smem += tab;
     int per_sm = 0, dev = 0, sms = 1;
-    CUDA_TRY(cpmgpu::tiled_occupancy(L.g.D, L.NE, smem, &per_sm));
+    int odd = 0;
+    for (int d = 0; d < L.g.D; ++d) odd |= L.g.periodic && (L.g.dims[d] & 1);
+    CUDA_TRY(cpmgpu::tiled_occupancy(L.g.D, L.NE, odd, smem, &per_sm));
     CUDA_TRY(cudaGetDevice(&dev));
     CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     int tiles = 1;
@@ -456,7 +458,7 @@ std::string DeviceSims::run_tiled(const RunPlan& p, const uint64_t* t3) {
         while (n > 0) {
             const uint64_t m = std::min<uint64_t>(n, 1ull << 18);
             CUDA_TRY(cudaMemsetAsync(d_bar_, 0, 64, stream_));
-            CUDA_TRY(cpmgpu::launch_tiled(L.g.D, L.NE, d_sim, m, nt, d_bar_, claims, t3, max_box, tables_in_smem,
+            CUDA_TRY(cpmgpu::launch_tiled(L.g.D, L.NE, odd, d_sim, m, nt, d_bar_, claims, t3, max_box, tables_in_smem,
                                           barrier_extra, cl_cap, smem, grid, stream_));
             n -= m;
         }

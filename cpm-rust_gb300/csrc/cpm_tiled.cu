@@ -81,7 +81,7 @@ __device__ __forceinline__ unsigned long long global_ns() {
 // within a launch (the host zeroes it), and acquire loads until it reaches
 // `epoch` * n. The wait gives up after 2 s of wall time, records the
 // timeout and returns false instead of hanging.
-__device__ bool grid_sync(BarrierState* b, unsigned int n, unsigned int& epoch) {
+static __device__ bool grid_sync(BarrierState* b, unsigned int n, unsigned int& epoch) {
     __shared__ int s_ok;
     ++epoch;
     __syncthreads();
@@ -505,12 +505,17 @@ __host__ __device__ inline TileShared tile_shared(int box_sites, int n_cells, in
 
 // Shared-memory copy of the float energy tables (J, adhesion differences,
 // term tables and their remainders): (n+1)^2 + (n+1)^3 + 4 n tab_n floats.
+#ifndef CPM_TILED_ODD_UNIT
 size_t tiled_table_bytes(int n_types, int tab_n) {
     const size_t n1 = (size_t)n_types + 1;
     return (n1 * n1 + n1 * n1 * n1 + 4 * (size_t)n_types * (size_t)tab_n) * 4;
 }
+#endif
 
-template <int D, int NE>
+// ODD: the lattice has an odd periodic side, whose last coordinate takes a
+// third site colour (compiled separately, so that the even-sided kernels
+// keep their two-colour index arithmetic).
+template <int D, int NE, bool ODD>
 __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_mcs, TileGrid tg_in, BarrierState* bar,
                                                    unsigned long long* claims, const uint64_t* t3, int max_box,
                                                    int tables_in_smem, int barrier_extra, int cl_cap) {
@@ -525,11 +530,11 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
     if (tid == 0) gsd = *simp;
     if (tid < 8) sstat[tid] = 0;
     __syncthreads();
-    // site colours per axis: the two parities, plus the last coordinate of
-    // an odd periodic axis as a third
-    if (tid < 3) s_ncls[tid] = tid < D ? ((gsd.periodic && (gsd.dims[tid] & 1)) ? 3 : 2) : 1;
+    // site colours per axis: the two parities, plus (ODD) the last
+    // coordinate of an odd periodic axis as a third
+    if (tid < 3) s_ncls[tid] = tid < D ? ((ODD && gsd.periodic && (gsd.dims[tid] & 1)) ? 3 : 2) : 1;
     __syncthreads();
-    const int n_cls = s_ncls[0] * s_ncls[1] * s_ncls[2];
+    const int n_cls = ODD ? s_ncls[0] * s_ncls[1] * s_ncls[2] : 1 << D;
     if (tables_in_smem && gsd.dj32 != nullptr) {
         // the float energy tables move next to the tile state (no global
         // loads in the common-case decision)
@@ -829,11 +834,12 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                     int n_class = 1;
                     for (int d = 0; d < D; ++d) {
                         const int Ld = g.dims[d];
-                        const int want = sc % s_ncls[d];
-                        sc /= s_ncls[d];
+                        const int nc_d = ODD ? s_ncls[d] : 2;
+                        const int want = ODD ? sc % nc_d : (sc >> d) & 1;
+                        if (ODD) sc /= nc_d;
                         const int g0 = ((s_gx0[d] % Ld) + Ld) % Ld;
                         const int tc = s_tcnt[d];
-                        if (s_ncls[d] == 2) {
+                        if (nc_d == 2) {
                             const int first = (want - (g0 & 1)) & 1;  // first local offset with that parity
                             base[d] = first;
                             cnt[d] = tc > first ? (tc - first + 1) / 2 : 0;
@@ -871,7 +877,7 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                             for (int d = D - 1; d >= 0; --d) {
                                 const int i = r % cnt[d];
                                 r /= cnt[d];
-                                const int li = i < cnt_a[d] ? base[d] + 2 * i : base_b[d] + 2 * (i - cnt_a[d]);
+                                const int li = !ODD || i < cnt_a[d] ? base[d] + 2 * i : base_b[d] + 2 * (i - cnt_a[d]);
                                 t += (li + 1) * (int)lsd.strides[d];
                             }
                             gf = (int)sgf[t];
@@ -1003,6 +1009,83 @@ static int tiled_index(int D, int NE) {
     return -1;
 }
 
+// The kernel variants of this unit: even site colouring here; odd periodic
+// sides in cpm_tiled_odd.cu, which compiles this file with
+// CPM_TILED_ODD_UNIT defined (two units build in parallel).
+#ifndef CPM_TILED_ODD_UNIT
+#define TILED_ODD false
+#define TILED_VARIANT(name) name##_even
+#else
+#define TILED_ODD true
+#define TILED_VARIANT(name) name##_odd
+#endif
+
+// Shared-memory limit raised once per device (see prepare_resident_kernels).
+cudaError_t TILED_VARIANT(prepare_tiled_kernels)() {
+    static std::mutex mu;
+    static bool done[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    if (dev >= 0 && dev < 64 && done[dev]) return cudaSuccess;
+    const int smem = 227 * 1024 - 4096;
+    if ((e = cudaFuncSetAttribute(tiled_kernel<2, 4, TILED_ODD>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) ||
+        (e = cudaFuncSetAttribute(tiled_kernel<2, 8, TILED_ODD>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) ||
+        (e = cudaFuncSetAttribute(tiled_kernel<3, 6, TILED_ODD>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) ||
+        (e = cudaFuncSetAttribute(tiled_kernel<3, 18, TILED_ODD>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) ||
+        (e = cudaFuncSetAttribute(tiled_kernel<3, 26, TILED_ODD>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)))
+        return e;
+    if (dev >= 0 && dev < 64) done[dev] = true;
+    return cudaSuccess;
+}
+
+cudaError_t TILED_VARIANT(tiled_occupancy)(int D, int NE, size_t smem, int* per_sm) {
+    *per_sm = 0;
+    cudaError_t e = TILED_VARIANT(prepare_tiled_kernels)();
+    if (e != cudaSuccess) return e;
+#define TOCC(I, D_, NE_) \
+    case I: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, tiled_kernel<D_, NE_, TILED_ODD>, TB, smem);
+    switch (tiled_index(D, NE)) {
+        TOCC(0, 2, 4)
+        TOCC(1, 2, 8)
+        TOCC(2, 3, 6)
+        TOCC(3, 3, 18)
+        TOCC(4, 3, 26)
+        default: return cudaErrorInvalidValue;
+    }
+#undef TOCC
+}
+
+cudaError_t TILED_VARIANT(launch_tiled)(int D, int NE, SimDesc* d_sim, uint64_t n_mcs, const int* nt,
+                                        void* d_barrier, unsigned long long* d_claims, const uint64_t* d_t3,
+                                        int max_box, int tables_in_smem, int barrier_extra, int cl_cap, size_t smem,
+                                        int grid, cudaStream_t st) {
+    TileGrid tg;
+    for (int d = 0; d < 3; ++d) { tg.nt[d] = d < D ? nt[d] : 1; tg.off[d] = 0; }
+    tg.colors = 1 << D;
+    BarrierState* bar = (BarrierState*)d_barrier;
+#define TLAUNCH(I, D_, NE_)                                                                                 \
+    case I: {                                                                                               \
+        auto k = tiled_kernel<D_, NE_, TILED_ODD>;                                                           \
+        cudaError_t e = TILED_VARIANT(prepare_tiled_kernels)();                                             \
+        if (e != cudaSuccess) return e;                                                                     \
+        void* args[] = {(void*)&d_sim, (void*)&n_mcs, (void*)&tg, (void*)&bar, (void*)&d_claims, (void*)&d_t3, \
+                        (void*)&max_box, (void*)&tables_in_smem, (void*)&barrier_extra, (void*)&cl_cap};   \
+        return cudaLaunchCooperativeKernel((const void*)k, dim3(grid), dim3(TB), args, smem, st);            \
+    }
+    switch (tiled_index(D, NE)) {
+        TLAUNCH(0, 2, 4)
+        TLAUNCH(1, 2, 8)
+        TLAUNCH(2, 3, 6)
+        TLAUNCH(3, 3, 18)
+        TLAUNCH(4, 3, 26)
+        default: return cudaErrorInvalidValue;
+    }
+#undef TLAUNCH
+}
+
+#ifndef CPM_TILED_ODD_UNIT
 bool tiled_plan(int D, const int* dims, int periodic, int* nt, int* max_box) {
     (void)periodic;  // odd periodic axes take a third site colour in the kernel
     int box = 1, klass = 1;
@@ -1032,69 +1115,26 @@ size_t tiled_smem_bytes(int max_box, int n_cells, int cl_cap, int D) {
 }
 int tiled_block() { return TB; }
 
-// Shared-memory limit raised once per device before any launch (see
-// prepare_resident_kernels).
 cudaError_t prepare_tiled_kernels() {
-    static std::mutex mu;
-    static bool done[64] = {};
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
-    std::lock_guard<std::mutex> lk(mu);
-    if (dev >= 0 && dev < 64 && done[dev]) return cudaSuccess;
-    const int smem = 227 * 1024 - 4096;
-    if ((e = cudaFuncSetAttribute(tiled_kernel<2, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) ||
-        (e = cudaFuncSetAttribute(tiled_kernel<2, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) ||
-        (e = cudaFuncSetAttribute(tiled_kernel<3, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) ||
-        (e = cudaFuncSetAttribute(tiled_kernel<3, 18>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) ||
-        (e = cudaFuncSetAttribute(tiled_kernel<3, 26>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)))
-        return e;
-    if (dev >= 0 && dev < 64) done[dev] = true;
-    return cudaSuccess;
+    cudaError_t e = prepare_tiled_kernels_even();
+    return e == cudaSuccess ? prepare_tiled_kernels_odd() : e;
 }
 
-cudaError_t tiled_occupancy(int D, int NE, size_t smem, int* per_sm) {
-    *per_sm = 0;
-    cudaError_t e = prepare_tiled_kernels();
-    if (e != cudaSuccess) return e;
-#define TOCC(I, D_, NE_) \
-    case I: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, tiled_kernel<D_, NE_>, TB, smem);
-    switch (tiled_index(D, NE)) {
-        TOCC(0, 2, 4)
-        TOCC(1, 2, 8)
-        TOCC(2, 3, 6)
-        TOCC(3, 3, 18)
-        TOCC(4, 3, 26)
-        default: return cudaErrorInvalidValue;
-    }
-#undef TOCC
+cudaError_t tiled_occupancy(int D, int NE, int odd, size_t smem, int* per_sm) {
+    return odd ? tiled_occupancy_odd(D, NE, smem, per_sm) : tiled_occupancy_even(D, NE, smem, per_sm);
 }
 
-cudaError_t launch_tiled(int D, int NE, SimDesc* d_sim, uint64_t n_mcs, const int* nt, void* d_barrier,
+cudaError_t launch_tiled(int D, int NE, int odd, SimDesc* d_sim, uint64_t n_mcs, const int* nt, void* d_barrier,
                          unsigned long long* d_claims, const uint64_t* d_t3, int max_box, int tables_in_smem,
                          int barrier_extra, int cl_cap, size_t smem, int grid, cudaStream_t st) {
-    TileGrid tg;
-    for (int d = 0; d < 3; ++d) { tg.nt[d] = d < D ? nt[d] : 1; tg.off[d] = 0; }
-    tg.colors = 1 << D;
-    BarrierState* bar = (BarrierState*)d_barrier;
-#define TLAUNCH(I, D_, NE_)                                                                                 \
-    case I: {                                                                                               \
-        auto k = tiled_kernel<D_, NE_>;                                                                      \
-        cudaError_t e = prepare_tiled_kernels();                                                            \
-        if (e != cudaSuccess) return e;                                                                     \
-        void* args[] = {(void*)&d_sim, (void*)&n_mcs, (void*)&tg, (void*)&bar, (void*)&d_claims, (void*)&d_t3, \
-                        (void*)&max_box, (void*)&tables_in_smem, (void*)&barrier_extra, (void*)&cl_cap};   \
-        return cudaLaunchCooperativeKernel((const void*)k, dim3(grid), dim3(TB), args, smem, st);            \
-    }
-    switch (tiled_index(D, NE)) {
-        TLAUNCH(0, 2, 4)
-        TLAUNCH(1, 2, 8)
-        TLAUNCH(2, 3, 6)
-        TLAUNCH(3, 3, 18)
-        TLAUNCH(4, 3, 26)
-        default: return cudaErrorInvalidValue;
-    }
-#undef TLAUNCH
+    return odd ? launch_tiled_odd(D, NE, d_sim, n_mcs, nt, d_barrier, d_claims, d_t3, max_box, tables_in_smem,
+                                  barrier_extra, cl_cap, smem, grid, st)
+               : launch_tiled_even(D, NE, d_sim, n_mcs, nt, d_barrier, d_claims, d_t3, max_box, tables_in_smem,
+                                   barrier_extra, cl_cap, smem, grid, st);
 }
+#endif
+
+#undef TILED_ODD
+#undef TILED_VARIANT
 
 }  // namespace cpmgpu
