@@ -198,16 +198,12 @@ static int resolve(const cpm_builder* b, uint64_t burn, uint64_t readout, uint64
     return ok();
 }
 
-// Every configuration the reference accepts runs here: the EdgeList
+// Every configuration the reference accepts runs here. The EdgeList
 // proposal (monte_carlo.rs:336-352) is, by the reference's own definition
-// (edge_list.rs:1-16), the Uniform chain with its null attempts removed;
-// the device sweep visits every site and a null attempt costs it one
+// (edge_list.rs:1-16), the Uniform chain with its null attempts removed; the
+// device sweep visits every site and a null attempt costs it one
 // comparison, so both proposals run the same device chain (the convention
 // hash still records which one was asked for).
-static int check_supported(const Config& c) {
-    (void)c;
-    return ok();
-}
 
 static int code_for(const std::string& e) {
     if (e.rfind("CUDA error", 0) == 0) return CPM_E_CUDA;
@@ -223,7 +219,6 @@ extern "C" int cpm_builder_run(const cpm_builder* b, uint64_t burn, uint64_t rea
     if (e) return e;
     std::string msg = validate(c);
     if (!msg.empty()) return fail(CPM_E_CONFIG, msg);
-    if ((e = check_supported(c))) return e;
     Initial init;
     const auto t0 = std::chrono::steady_clock::now();
     msg = initialize(c, init);
@@ -261,7 +256,6 @@ extern "C" int cpm_builder_run_batch(const cpm_builder* b, const double* thetas,
         th[i].assign(thetas + k, thetas + k + lens[i]);
         k += lens[i];
     }
-    if ((e = check_supported(c))) return e;
     ReadoutOptions ro;
     ro.include_lattice = include_lattice != 0;
     ro.topology = true;
@@ -547,7 +541,6 @@ static int prepare(const cpm_builder* const* builders, size_t n, std::vector<Con
         if (e) return e;
         std::string msg = validate(cfgs[i]);
         if (!msg.empty()) return fail(CPM_E_CONFIG, msg);
-        if ((e = check_supported(cfgs[i]))) return e;
     }
     // placements are independent: host threads over simulations; the first
     // failure in input order is reported
@@ -961,7 +954,6 @@ extern "C" int cpm_serve_submit(cpm_server* s, const cpm_builder* b, uint64_t bu
     if (rc) return rc;
     const std::string msg = validate(c);
     if (!msg.empty()) return fail(CPM_E_CONFIG, msg);
-    if ((rc = check_supported(c))) return rc;
     ReadoutOptions ro;
     ro.include_lattice = include_lattice != 0;
     ro.topology = topology != 0;
