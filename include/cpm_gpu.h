@@ -36,7 +36,7 @@ extern "C" {
 #define CPM_E_TIMEOUT 5     /* a bounded device or host wait gave up */
 #define CPM_E_BUDGET 6      /* serving admission: request exceeds the HBM budget */
 #define CPM_E_ARG 7         /* invalid argument (null pointer, index out of range, short buffer) */
-#define CPM_E_UNSUPPORTED 8 /* valid reference configuration the GB300 engine does not run */
+#define CPM_E_UNSUPPORTED 8 /* a request outside an entry point's domain (cpm_run_mcs_noalloc: 2D only) */
 
 /* Message of the last failing call on this thread ("" if none). */
 const char* cpm_last_error(void);
