@@ -110,3 +110,24 @@ def test_three_d_cavity(cuda_required):
     vols = list(s.medium_component_volumes)
     touches = list(s.medium_component_touches_boundary)
     assert 18 in vols and touches[vols.index(18)] is False
+
+
+@pytest.mark.parametrize("boundary", ["periodic", "fixed"])
+def test_edge_states(boundary, cuda_required):
+    """All medium (one component, no contacts); single-site cells on a
+    checkerboard (every cell alone, the medium cut into diagonal pieces
+    under von Neumann but one piece under the full stencil); a lattice full
+    of cells (no medium component at all)."""
+    n = 12
+    model = _model((8, 6), boundary, n)
+    s = _check(model, np.zeros((8, 6), np.uint32))
+    assert list(s.fragmented_cells) == [] and len(s.medium_component_volumes) == 1
+    lat = np.zeros((8, 6), np.uint32)
+    ids = iter(range(1, n + 1))
+    for r in range(0, 8, 2):
+        for c in range(0, 6, 2):
+            lat[r, c] = next(ids)
+    _check(model, lat)
+    full = (np.arange(48).reshape(8, 6) % n + 1).astype(np.uint32)
+    s = _check(model, full)
+    assert len(s.medium_component_volumes) == 0
