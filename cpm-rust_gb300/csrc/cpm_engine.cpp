@@ -90,7 +90,7 @@ DeviceSims::~DeviceSims() {
     for (auto a : aux_) cudaStreamDestroy(a);
     for (auto e : joins_) cudaEventDestroy(e);
     if (ev_fork_) cudaEventDestroy(ev_fork_);
-    for (void* p : {(void*)d_bar_, (void*)arena_, (void*)d_descs_, (void*)d_plans_, (void*)d_next_})
+    for (void* p : {(void*)d_bar_, (void*)d_reg_, (void*)arena_, (void*)d_descs_, (void*)d_plans_, (void*)d_next_})
         if (p) dev_free(p);
 }
 
@@ -397,13 +397,14 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
 DeviceSims::Path DeviceSims::path(size_t i) const {
     const SimLayout& L = layouts_[i];
     if (force_global_) return GLOBAL;
-    if (L.n_cells >= 65535) return GLOBAL;
     // Metropolis-Hastings acceptance and the Act term run on the global sweep only
     if (descs_[i].acceptance || descs_[i].act) return GLOBAL;
     int dims[3] = {(int)L.g.dims[0], (int)L.g.dims[1], (int)L.g.dims[2]}, nt[3] = {1, 1, 1}, max_box = 0;
     const bool tiled_ok = cpmgpu::tiled_plan(L.g.D, dims, L.g.periodic, nt, &max_box) &&
-                          cpmgpu::tiled_smem_bytes(max_box, L.n_cells, 0, L.g.D) <= cpmgpu::resident_smem_limit();
-    if (!force_tiled_ && cpmgpu::resident_smem_bytes(L.g.n_padded, L.n_cells) <= cpmgpu::resident_smem_limit()) {
+                          cpmgpu::tiled_smem_bytes(max_box, L.n_cells, 0, L.g.D, 0) <= cpmgpu::resident_smem_limit();
+    // the resident sweep keeps cell ids in 16 bits
+    if (!force_tiled_ && L.n_cells < 65535 &&
+        cpmgpu::resident_smem_bytes(L.g.n_padded, L.n_cells) <= cpmgpu::resident_smem_limit()) {
         // The path is a function of the simulation's own configuration, so a
         // simulation's trajectory is the same alone and inside any batch.
         // CPM_GPU_PREFER_TILED opts a simulation with at least 8 tiles per
@@ -422,14 +423,17 @@ std::string DeviceSims::run_tiled(const RunPlan& p, const uint64_t* t3) {
     const SimLayout& L = layouts_[p.sim];
     int dims[3] = {(int)L.g.dims[0], (int)L.g.dims[1], (int)L.g.dims[2]}, nt[3], max_box = 0;
     cpmgpu::tiled_plan(L.g.D, dims, L.g.periodic, nt, &max_box);
-    // position sums of up to 1024 listed cells per box in shared memory (as
-    // many as fit), then the energy tables if they fit beside the tile state
+    // the cell registry in shared memory if it fits beside all the box's
+    // position sums (else in HBM), position sums of up to 1024 listed cells
+    // per box in shared memory (as many as fit), then the energy tables if
+    // they fit beside the tile state
+    const size_t lim = cpmgpu::resident_smem_limit();
     int cl_cap = (int)std::min<int64_t>(std::min<int64_t>(max_box, L.n_cells), 1024);
-    while (cl_cap > 0 && cpmgpu::tiled_smem_bytes(max_box, L.n_cells, cl_cap, L.g.D) > cpmgpu::resident_smem_limit())
-        cl_cap /= 2;
-    size_t smem = cpmgpu::tiled_smem_bytes(max_box, L.n_cells, cl_cap, L.g.D);
+    const int reg_smem = cpmgpu::tiled_smem_bytes(max_box, L.n_cells, cl_cap, L.g.D, 1) <= lim ? 1 : 0;
+    while (cl_cap > 0 && cpmgpu::tiled_smem_bytes(max_box, L.n_cells, cl_cap, L.g.D, reg_smem) > lim) cl_cap /= 2;
+    size_t smem = cpmgpu::tiled_smem_bytes(max_box, L.n_cells, cl_cap, L.g.D, reg_smem);
     const size_t tab = cpmgpu::tiled_table_bytes(descs_[p.sim].n_types, descs_[p.sim].tab_n);
-    const int tables_in_smem = smem + tab <= cpmgpu::resident_smem_limit();
+    const int tables_in_smem = smem + tab <= lim;
     if (tables_in_smem) smem += tab;
     int per_sm = 0, dev = 0, sms = 1;
     int odd = 0;
@@ -450,6 +454,17 @@ std::string DeviceSims::run_tiled(const RunPlan& p, const uint64_t* t3) {
     // kernel records the timeout and returns; nothing else changes
     const int barrier_extra = std::getenv("CPM_GPU_TEST_BARRIER_TIMEOUT") ? 1 : 0;
     if (!d_bar_) CUDA_TRY(dev_alloc(&d_bar_, 64));
+    // each CTA's cell registry in HBM (when it is not in shared memory): a
+    // stamp and a box slot per cell id
+    const size_t reg = reg_smem ? 0 : 2 * (size_t)grid * (size_t)(L.n_cells + 1) * 4;
+    if (reg > reg_cap_) {
+        if (d_reg_) dev_free(d_reg_);
+        d_reg_ = nullptr;
+        reg_cap_ = 0;
+        CUDA_TRY(dev_alloc((void**)&d_reg_, reg));
+        reg_cap_ = reg;
+        device_bytes_ += reg;
+    }
     SimDesc* d_sim = d_descs_ + p.sim;
     unsigned long long* claims = descs_[p.sim].slots;
     auto chunk = [&](uint64_t n) -> std::string {
@@ -458,8 +473,9 @@ std::string DeviceSims::run_tiled(const RunPlan& p, const uint64_t* t3) {
         while (n > 0) {
             const uint64_t m = std::min<uint64_t>(n, 1ull << 18);
             CUDA_TRY(cudaMemsetAsync(d_bar_, 0, 64, stream_));
-            CUDA_TRY(cpmgpu::launch_tiled(L.g.D, L.NE, odd, d_sim, m, nt, d_bar_, claims, t3, max_box, tables_in_smem,
-                                          barrier_extra, cl_cap, smem, grid, stream_));
+            CUDA_TRY(cpmgpu::launch_tiled(L.g.D, L.NE, odd, d_sim, m, nt, d_bar_, claims, reg_smem ? nullptr : d_reg_,
+                                          t3, max_box, tables_in_smem, barrier_extra, cl_cap, reg_smem, smem, grid,
+                                          stream_, L.n_cells));
             n -= m;
         }
         return "";

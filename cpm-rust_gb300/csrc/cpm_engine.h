@@ -121,6 +121,8 @@ class DeviceSims {
     bool force_tiled_ = false;
     bool prefer_tiled_ = false;
     void* d_bar_ = nullptr;
+    uint32_t* d_reg_ = nullptr;  // tiled sweep: per-CTA cell registries
+    size_t reg_cap_ = 0;
     std::vector<size_t> tiled_ran_;
     std::string run_tiled(const RunPlan& p, const uint64_t* t3);
     uint64_t h2d_bytes_ = 0;

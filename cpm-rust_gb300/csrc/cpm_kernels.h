@@ -35,25 +35,30 @@ cudaError_t launch_resident(int D, int NE, int variant, SimDesc* d_sims, const R
 cudaError_t resident_occupancy(int D, int NE, int variant, size_t smem, int* blocks_per_sm);
 // Tiled cooperative sweep for large lattices (cpm_tiled.cu).
 bool tiled_plan(int D, const int* dims, int periodic, int* nt, int* max_box);
-size_t tiled_smem_bytes(int max_box, int n_cells, int cl_cap, int D);
+size_t tiled_smem_bytes(int max_box, int n_cells, int cl_cap, int D, int reg_smem);
 size_t tiled_table_bytes(int n_types, int tab_n);
 int tiled_block();
 // `odd`: the lattice has an odd periodic side (kernels of cpm_tiled_odd.cu).
+// `reg_smem`: each CTA's cell registry (stamps and box slots) in shared
+// memory; else `d_registry` holds it: 2 x grid x (n_cells + 1) words.
 cudaError_t tiled_occupancy(int D, int NE, int odd, size_t smem, int* per_sm);
 cudaError_t launch_tiled(int D, int NE, int odd, SimDesc* d_sim, uint64_t n_mcs, const int* nt, void* d_barrier,
-                         unsigned long long* d_claims, const uint64_t* d_t3, int max_box, int tables_in_smem,
-                         int barrier_extra, int cl_cap, size_t smem, int grid, cudaStream_t st);
+                         unsigned long long* d_claims, uint32_t* d_registry, const uint64_t* d_t3, int max_box,
+                         int tables_in_smem, int barrier_extra, int cl_cap, int reg_smem, size_t smem, int grid,
+                         cudaStream_t st, int n_cells);
 // The variants behind them (even site colouring / odd periodic sides).
 cudaError_t prepare_tiled_kernels_even();
 cudaError_t prepare_tiled_kernels_odd();
 cudaError_t tiled_occupancy_even(int D, int NE, size_t smem, int* per_sm);
 cudaError_t tiled_occupancy_odd(int D, int NE, size_t smem, int* per_sm);
 cudaError_t launch_tiled_even(int D, int NE, SimDesc* d_sim, uint64_t n_mcs, const int* nt, void* d_barrier,
-                              unsigned long long* d_claims, const uint64_t* d_t3, int max_box, int tables_in_smem,
-                              int barrier_extra, int cl_cap, size_t smem, int grid, cudaStream_t st);
+                              unsigned long long* d_claims, uint32_t* d_registry, const uint64_t* d_t3, int max_box,
+                              int tables_in_smem, int barrier_extra, int cl_cap, int reg_smem, size_t smem, int grid,
+                              cudaStream_t st, int n_cells);
 cudaError_t launch_tiled_odd(int D, int NE, SimDesc* d_sim, uint64_t n_mcs, const int* nt, void* d_barrier,
-                             unsigned long long* d_claims, const uint64_t* d_t3, int max_box, int tables_in_smem,
-                             int barrier_extra, int cl_cap, size_t smem, int grid, cudaStream_t st);
+                             unsigned long long* d_claims, uint32_t* d_registry, const uint64_t* d_t3, int max_box,
+                             int tables_in_smem, int barrier_extra, int cl_cap, int reg_smem, size_t smem, int grid,
+                             cudaStream_t st, int n_cells);
 // Copies one sample (V, I, position sums, optional lattice) of simulation d_sim.
 cudaError_t launch_sample(int D, const SimDesc* d_sim, int sample, int write_lattice, int64_t n_sites, cudaStream_t st);
 // Topology readouts of lattice snapshots (cpm_readout.cu). Work is cut into

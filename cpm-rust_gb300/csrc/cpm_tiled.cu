@@ -135,19 +135,22 @@ struct TileProc {
     int16_t* c_dl;
     const uint64_t* t3;
     int* s_n;
-    // position sums of the first cl_cap listed cells, staged in shared
-    // memory (slot[id] < cl_cap); other cells use HBM through L2
-    uint16_t* slot;
+    // The box holds box-local cell slots, not cell ids: slot s >= 1 is
+    // the cell clist[s - 1], slot 0 the medium; every per-cell array is
+    // indexed by slot. Position sums of the first cl_cap slots are staged in
+    // shared memory, the others live in HBM (through L2).
+    const uint32_t* clist;
     long long *ssp, *sso;
     int cl_cap;
 
-    __device__ __forceinline__ bool sums_of(uint32_t id, long long*& sp, long long*& so) const {
-        const uint32_t k = slot[id];
-        if ((int)k < cl_cap) {
+    __device__ __forceinline__ bool sums_of(uint32_t s, long long*& sp, long long*& so) const {
+        const int k = (int)s - 1;
+        if (k < cl_cap) {
             sp = ssp + (long long)k * D;
             so = sso + (long long)k * D * D;
             return true;
         }
+        const uint32_t id = clist[k];
         sp = (long long*)g.sum_pos + (long long)id * D;
         so = (long long*)g.sum_outer + (long long)id * D * D;
         return false;
@@ -462,7 +465,8 @@ struct TileProc {
 };
 
 struct TileShared {
-    uint32_t sig, skd, sgf, sz, vol, itf, b0, b1, adh, dirty, own, mod, seen, clist, slot, ssp, sso, c_site, c_key, c_cells,
+    uint32_t sig, sid, skd, sgf, sz, vol, itf, b0, b1, adh, dirty, own, mod, clist, ssp, sso, rseen, rslot, c_site, c_key,
+        c_cells,
         c_flags, c_gf, c_z, c_dl, total;
 };
 
@@ -471,10 +475,13 @@ __host__ __device__ inline uint32_t tl_take(uint32_t& off, uint64_t b) {
     off = (uint32_t)((off + b + 15) & ~(uint64_t)15);
     return o;
 }
-__host__ __device__ inline TileShared tile_shared(int box_sites, int n_cells, int cl_cap, int D) {
+// reg_smem: the cell registry (a stamp and a slot per cell id) is kept in
+// shared memory too (else in HBM, for lattices with many cells).
+__host__ __device__ inline TileShared tile_shared(int box_sites, int n_cells, int cl_cap, int D, bool reg_smem) {
     TileShared s;
     uint32_t off = 0;
-    const uint64_t n1 = (uint64_t)n_cells + 1;
+    // slots: the medium and at most one per box site (or per cell)
+    const uint64_t n1 = (uint64_t)(box_sites < n_cells ? box_sites : n_cells) + 1;
     s.sig = tl_take(off, (uint64_t)box_sites * 2);
     s.skd = tl_take(off, (uint64_t)box_sites);      // copy direction of each tile site's attempt
     s.sgf = tl_take(off, (uint64_t)box_sites * 4);  // its global flat index (the draw's counter)
@@ -487,11 +494,11 @@ __host__ __device__ inline TileShared tile_shared(int box_sites, int n_cells, in
     s.dirty = tl_take(off, n1);
     s.own = tl_take(off, n1);
     s.mod = tl_take(off, n1);
-    s.seen = tl_take(off, n1 * 4);
-    s.clist = tl_take(off, (uint64_t)(box_sites < n_cells ? box_sites : n_cells) * 4);
-    s.slot = tl_take(off, n1 * 2);
+    s.clist = tl_take(off, n1 * 4);
     s.ssp = tl_take(off, (uint64_t)cl_cap * D * 8);
     s.sso = tl_take(off, (uint64_t)cl_cap * D * D * 8);
+    s.rseen = tl_take(off, reg_smem ? ((uint64_t)n_cells + 1) * 4 : 0);
+    s.rslot = tl_take(off, reg_smem ? ((uint64_t)n_cells + 1) * 2 : 0);
     s.c_site = tl_take(off, TCMAX * 4);
     s.c_key = tl_take(off, TCMAX * 4);
     s.c_cells = tl_take(off, TCMAX * 4);
@@ -499,6 +506,10 @@ __host__ __device__ inline TileShared tile_shared(int box_sites, int n_cells, in
     s.c_gf = tl_take(off, TCMAX * 4);
     s.c_z = tl_take(off, TCMAX * 4);
     s.c_dl = tl_take(off, TCMAX * 2);
+    // the staged cell ids, before they become slots: only used while a box
+    // is staged, so they share the candidate arrays when they fit there
+    s.sid = (uint64_t)box_sites * 4 <= (uint64_t)(s.c_dl + TCMAX * 2 - s.c_site) ? s.c_site
+                                                                                   : tl_take(off, (uint64_t)box_sites * 4);
     s.total = off;
     return s;
 }
@@ -518,7 +529,8 @@ size_t tiled_table_bytes(int n_types, int tab_n) {
 template <int D, int NE, bool ODD>
 __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_mcs, TileGrid tg_in, BarrierState* bar,
                                                    unsigned long long* claims, const uint64_t* t3, int max_box,
-                                                   int tables_in_smem, int barrier_extra, int cl_cap) {
+                                                   int tables_in_smem, int barrier_extra, int cl_cap,
+                                                   int reg_smem, uint32_t* seen_all, uint32_t* slot_all) {
     extern __shared__ __align__(16) unsigned char sm[];
     __shared__ SimDesc gsd, lsd;
     __shared__ int s_n, s_tile, s_ncell, s_box_dims[3], s_gx0[3], s_tcnt[3];
@@ -538,7 +550,7 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
     if (tables_in_smem && gsd.dj32 != nullptr) {
         // the float energy tables move next to the tile state (no global
         // loads in the common-case decision)
-        float* tb = (float*)(sm + tile_shared(max_box, gsd.n_cells, cl_cap, D).total);
+        float* tb = (float*)(sm + tile_shared(max_box, gsd.n_cells, cl_cap, D, reg_smem != 0).total);
         const int n1 = gsd.n_types + 1, nj = n1 * n1, nd = n1 * n1 * n1, nv = gsd.n_types * gsd.tab_n;
         for (int q = tid; q < nj; q += TB) tb[q] = gsd.J32[q];
         for (int q = tid; q < nd; q += TB) tb[nj + q] = gsd.dj32[q];
@@ -565,11 +577,31 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
     const SimDesc& g = gsd;
     const int nblk = gridDim.x;
     const unsigned int arrivals = (unsigned int)(nblk + barrier_extra);  // barrier_extra: timeout test hook
-    {
-        uint32_t* seen0 = (uint32_t*)(sm + tile_shared(max_box, g.n_cells, cl_cap, D).seen);
-        for (int id = tid; id <= g.n_cells; id += TB) seen0[id] = 0u;
-        __syncthreads();
+    // This CTA's cell registry, per cell id: the stamp of the last tile that
+    // listed the cell (unique within a launch: at most 2^18 MCS x 8
+    // sub-phases x 1024 tiles per CTA; zeroed here) and its slot in that
+    // tile's box. In shared memory when it fits (reg_smem), else in HBM
+    // (n_cells + 1 words each per CTA).
+    const TileShared ts0 = tile_shared(max_box, g.n_cells, cl_cap, D, reg_smem != 0);
+    uint32_t* seen_g = seen_all + (size_t)blockIdx.x * (size_t)(g.n_cells + 1);
+    uint32_t* slot_g = slot_all + (size_t)blockIdx.x * (size_t)(g.n_cells + 1);
+    for (int id = tid; id <= g.n_cells; id += TB) {
+        if (reg_smem) ((uint32_t*)(sm + ts0.rseen))[id] = 0u;
+        else seen_g[id] = 0u;
     }
+    __syncthreads();
+    // first listing of `id` under `stamp`; its slot; the slot recorded
+    auto reg_first = [&](uint32_t id, uint32_t stamp) -> bool {
+        if (reg_smem) return atomicExch((uint32_t*)(sm + ts0.rseen) + id, stamp) != stamp;
+        return atomicExch(seen_g + id, stamp) != stamp;
+    };
+    auto reg_set = [&](uint32_t id, uint32_t sl) {
+        if (reg_smem) ((uint16_t*)(sm + ts0.rslot))[id] = (uint16_t)sl;
+        else slot_g[id] = sl;
+    };
+    auto reg_get = [&](uint32_t id) -> uint32_t {
+        return reg_smem ? (uint32_t)((const uint16_t*)(sm + ts0.rslot))[id] : __ldcg(slot_g + id);
+    };
     TileCounters ct = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     unsigned long long attempts = 0, tile_passes = 0;
     unsigned long long cyc_pass = 0, cyc_stage = 0, cyc_sync = 0, cyc_claim = 0, cyc_bar1 = 0, cyc_bar2 = 0;
@@ -611,10 +643,7 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                     tc[d] = 2 * q + ((color >> d) & 1);
                 }
             };
-            const TileShared ts = tile_shared(max_box, g.n_cells, cl_cap, D);
-            uint32_t* seen = (uint32_t*)(sm + ts.seen);
-            // seen[] stamps, unique within a launch (at most 2^18 MCS x 8
-            // sub-phases x 1024 slots; seen[] starts zeroed)
+            const TileShared ts = tile_shared(max_box, g.n_cells, cl_cap, D, reg_smem != 0);
             auto stamp_of = [&](int k) -> uint32_t {
                 return (uint32_t)((m * 8 + (uint64_t)ci) * 1024u + (uint32_t)(k / nblk)) + 1u;
             };
@@ -663,15 +692,17 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                               (uint8_t*)(sm + ts.mod), (uint32_t*)(sm + ts.c_site), (uint32_t*)(sm + ts.c_key),
                               (uint32_t*)(sm + ts.c_cells), (uint32_t*)(sm + ts.c_flags), (uint32_t*)(sm + ts.c_gf),
                               (uint32_t*)(sm + ts.c_z), (int16_t*)(sm + ts.c_dl), t3, &s_n,
-                              (uint16_t*)(sm + ts.slot), (long long*)(sm + ts.ssp), (long long*)(sm + ts.sso), cl_cap};
+                              clist, (long long*)(sm + ts.ssp), (long long*)(sm + ts.sso), cl_cap};
+            uint32_t* sid = (uint32_t*)(sm + ts.sid);
             uint8_t* skd = (uint8_t*)(sm + ts.skd);
             uint32_t* sgf = (uint32_t*)(sm + ts.sgf);
             uint32_t* sz = (uint32_t*)(sm + ts.sz);
-            // Stage the box of the current tile: sigma into shared memory,
-            // each distinct cell listed once (and claimed when `claim`),
-            // then the listed cells' V, I and type. Nothing writes sigma, V
-            // or I between the two grid barriers of a sub-phase, so staging
-            // may run before the claim barrier.
+            // Stage the box of the current tile: each distinct cell of the
+            // box listed once (and claimed when `claim`) and given the next
+            // slot, the box's sigma as slots, then the listed cells' V, I,
+            // type and position sums by slot. Nothing writes sigma, V or I
+            // between the two grid barriers of a sub-phase, so staging may
+            // run before the claim barrier.
             auto stage_box = [&](int k, bool claim, uint32_t salt) {
                 const unsigned long long key = base_key | (unsigned long long)k;
                 const uint32_t stamp = stamp_of(k) + salt;
@@ -703,10 +734,12 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                         const bool leader = (int)(threadIdx.x & 31) == __ffs(peers) - 1;
                         if (!valid) continue;
                         const int gf = gfs[u];
-                        P.sig[q] = (uint16_t)id;
-                        if (id && leader && atomicExch(&seen[id], stamp) != stamp) {
+                        sid[q] = id;
+                        if (id && leader && reg_first(id, stamp)) {
                             if (claim) atomicMin(claims + id, key);
-                            clist[atomicAdd(&s_ncell, 1)] = id;
+                            const int k1 = atomicAdd(&s_ncell, 1);
+                            clist[k1] = id;
+                            reg_set(id, (uint32_t)(k1 + 1));
                         }
                         // this MCS's draw of each tile site (site_draw keyed by the global flat index)
                         bool interior = true;
@@ -736,29 +769,34 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                 }
                 if (tid < n_cls)
                     s_pkey[tid] = aux_draw(g.seed, mcs, TAG_PASS, (uint32_t)(tid * 64 + ci), (uint32_t)k).x;
-                __syncthreads();
+                __syncthreads();  // every listing (and its slot write) is visible to the block
+#pragma unroll 4
+                for (int q = tid; q < box; q += TB) {
+                    const uint32_t id = sid[q];
+                    P.sig[q] = id ? (uint16_t)reg_get(id) : (uint16_t)0;
+                }
                 const int nc = s_ncell;
                 for (int i = tid; i <= nc; i += TB) {
-                    const uint32_t id = i < nc ? clist[i] : 0u;  // the medium rides along as entry nc
-                    P.vol[id] = __ldcg(g.volume + id);
-                    P.itf[id] = __ldcg(g.interface + id);
-                    P.adh[id] = g.adh_of[id];
-                    P.dirty[id] = 0;
-                    P.mod[id] = 0;
-                    P.slot[id] = (i < nc && i < cl_cap) ? (uint16_t)i : (uint16_t)0xFFFFu;
+                    const uint32_t id = i < nc ? clist[i] : 0u;  // the medium rides along as slot 0
+                    const int sl = i < nc ? i + 1 : 0;
+                    P.vol[sl] = __ldcg(g.volume + id);
+                    P.itf[sl] = __ldcg(g.interface + id);
+                    P.adh[sl] = g.adh_of[id];
+                    P.dirty[sl] = 0;
+                    P.mod[sl] = 0;
                     if (i < nc && i < cl_cap) {
                         for (int d = 0; d < D; ++d) P.ssp[i * D + d] = __ldcg(g.sum_pos + (int64_t)id * D + d);
                         for (int d = 0; d < D * D; ++d) P.sso[i * D * D + d] = __ldcg(g.sum_outer + (int64_t)id * D * D + d);
                     }
                 }
             };
-            // own[id]: the lowest claiming tile of this sub-phase is this one
+            // own[slot]: the lowest claiming tile of this sub-phase is this one
             auto read_claims = [&](int k) {
                 const unsigned long long key = base_key | (unsigned long long)k;
                 const int nc = s_ncell;
                 for (int i = tid; i <= nc; i += TB) {
                     const uint32_t id = i < nc ? clist[i] : 0u;
-                    P.own[id] = id == 0 || __ldcg(claims + id) == key;
+                    P.own[i < nc ? i + 1 : 0] = id == 0 || __ldcg(claims + id) == key;
                 }
                 __syncthreads();
             };
@@ -796,7 +834,7 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                             gf += (x + 1) * (int)g.strides[d];
                         }
                         const uint32_t id = __ldcg(g.sigma + gf);
-                        if (id && atomicExch(&seen[id], stamp) != stamp) atomicMin(claims + id, key);
+                        if (id && reg_first(id, stamp)) atomicMin(claims + id, key);
                     }
                     __syncthreads();
                 }
@@ -936,19 +974,20 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                         r /= s_box_dims[d];
                         if (li[d] == 0 || li[d] == s_box_dims[d] - 1) interior = false;
                     }
-                    const uint32_t id = P.sig[q];
                     if (interior) {
+                        const uint32_t sl = P.sig[q];
                         int xg[3];
                         P.gflat_of_box(q, xg);
-                        write_site<D, uint32_t>(g, g.sigma, xg, id);
+                        write_site<D, uint32_t>(g, g.sigma, xg, sl ? clist[sl - 1] : 0u);
                     }
                 }
                 __syncthreads();
                 for (int i = tid; i < s_ncell; i += TB) {
                     const uint32_t id = clist[i];
-                    if (P.own[id] && P.mod[id]) {
-                        __stcg(g.volume + id, P.vol[id]);
-                        __stcg(g.interface + id, P.itf[id]);
+                    const int sl = i + 1;
+                    if (P.own[sl] && P.mod[sl]) {
+                        __stcg(g.volume + id, P.vol[sl]);
+                        __stcg(g.interface + id, P.itf[sl]);
                         if (i < cl_cap) {
                             for (int d = 0; d < D; ++d) __stcg((long long*)g.sum_pos + (int64_t)id * D + d, P.ssp[i * D + d]);
                             for (int d = 0; d < D * D; ++d)
@@ -1058,20 +1097,25 @@ cudaError_t TILED_VARIANT(tiled_occupancy)(int D, int NE, size_t smem, int* per_
 }
 
 cudaError_t TILED_VARIANT(launch_tiled)(int D, int NE, SimDesc* d_sim, uint64_t n_mcs, const int* nt,
-                                        void* d_barrier, unsigned long long* d_claims, const uint64_t* d_t3,
-                                        int max_box, int tables_in_smem, int barrier_extra, int cl_cap, size_t smem,
-                                        int grid, cudaStream_t st) {
+                                        void* d_barrier, unsigned long long* d_claims, uint32_t* d_registry,
+                                        const uint64_t* d_t3, int max_box, int tables_in_smem, int barrier_extra,
+                                        int cl_cap, int reg_smem, size_t smem, int grid, cudaStream_t st,
+                                        int n_cells) {
     TileGrid tg;
     for (int d = 0; d < 3; ++d) { tg.nt[d] = d < D ? nt[d] : 1; tg.off[d] = 0; }
     tg.colors = 1 << D;
     BarrierState* bar = (BarrierState*)d_barrier;
+    // in HBM unless reg_smem: grid x (n_cells + 1) stamps, then as many slots
+    uint32_t* seen_all = d_registry;
+    uint32_t* slot_all = d_registry ? d_registry + (size_t)grid * (size_t)(n_cells + 1) : nullptr;
 #define TLAUNCH(I, D_, NE_)                                                                                 \
     case I: {                                                                                               \
         auto k = tiled_kernel<D_, NE_, TILED_ODD>;                                                           \
         cudaError_t e = TILED_VARIANT(prepare_tiled_kernels)();                                             \
         if (e != cudaSuccess) return e;                                                                     \
         void* args[] = {(void*)&d_sim, (void*)&n_mcs, (void*)&tg, (void*)&bar, (void*)&d_claims, (void*)&d_t3, \
-                        (void*)&max_box, (void*)&tables_in_smem, (void*)&barrier_extra, (void*)&cl_cap};   \
+                        (void*)&max_box, (void*)&tables_in_smem, (void*)&barrier_extra, (void*)&cl_cap,    \
+                        (void*)&reg_smem, (void*)&seen_all, (void*)&slot_all};                              \
         return cudaLaunchCooperativeKernel((const void*)k, dim3(grid), dim3(TB), args, smem, st);            \
     }
     switch (tiled_index(D, NE)) {
@@ -1107,11 +1151,12 @@ bool tiled_plan(int D, const int* dims, int periodic, int* nt, int* max_box) {
         klass *= (tmax + 1) / 2;
     }
     *max_box = box;
-    return box <= TMAX_BOX && klass <= TCMAX;
+    // box slots are 16-bit: at most 65535 cells in a box
+    return box <= TMAX_BOX && box <= 65535 && klass <= TCMAX;
 }
 
-size_t tiled_smem_bytes(int max_box, int n_cells, int cl_cap, int D) {
-    return tile_shared(max_box, n_cells, cl_cap, D).total;
+size_t tiled_smem_bytes(int max_box, int n_cells, int cl_cap, int D, int reg_smem) {
+    return tile_shared(max_box, n_cells, cl_cap, D, reg_smem != 0).total;
 }
 int tiled_block() { return TB; }
 
@@ -1125,12 +1170,13 @@ cudaError_t tiled_occupancy(int D, int NE, int odd, size_t smem, int* per_sm) {
 }
 
 cudaError_t launch_tiled(int D, int NE, int odd, SimDesc* d_sim, uint64_t n_mcs, const int* nt, void* d_barrier,
-                         unsigned long long* d_claims, const uint64_t* d_t3, int max_box, int tables_in_smem,
-                         int barrier_extra, int cl_cap, size_t smem, int grid, cudaStream_t st) {
-    return odd ? launch_tiled_odd(D, NE, d_sim, n_mcs, nt, d_barrier, d_claims, d_t3, max_box, tables_in_smem,
-                                  barrier_extra, cl_cap, smem, grid, st)
-               : launch_tiled_even(D, NE, d_sim, n_mcs, nt, d_barrier, d_claims, d_t3, max_box, tables_in_smem,
-                                   barrier_extra, cl_cap, smem, grid, st);
+                         unsigned long long* d_claims, uint32_t* d_registry, const uint64_t* d_t3, int max_box,
+                         int tables_in_smem, int barrier_extra, int cl_cap, int reg_smem, size_t smem, int grid,
+                         cudaStream_t st, int n_cells) {
+    return odd ? launch_tiled_odd(D, NE, d_sim, n_mcs, nt, d_barrier, d_claims, d_registry, d_t3, max_box,
+                                  tables_in_smem, barrier_extra, cl_cap, reg_smem, smem, grid, st, n_cells)
+               : launch_tiled_even(D, NE, d_sim, n_mcs, nt, d_barrier, d_claims, d_registry, d_t3, max_box,
+                                   tables_in_smem, barrier_extra, cl_cap, reg_smem, smem, grid, st, n_cells);
 }
 #endif
 

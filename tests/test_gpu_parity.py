@@ -403,3 +403,36 @@ def test_tiled_barrier_timeout_is_reported_and_the_context_survives(cuda_require
     good.synchronize()
     assert good.stats()["spin_timeouts"] == 0
     assert good.recount_check()[0]
+
+
+def test_tiled_sweep_with_more_cells_than_16_bits(cuda_required):
+    """The tiled sweep stages box-local cell slots, so a lattice may hold any
+    number of cells: 70,000 on 1024 x 1024 (beyond 16-bit ids) run exactly
+    (V/I recount, position sums against the lattice, adhesion energy
+    against a direct count)."""
+    model = Model((1024, 1024), "periodic", [("a", 12, 14, 2.0, 0.5)], [[0, 6], [6, 2]], [70000], seed=21)
+    eng = _engine(model, warn=False)
+    assert eng.info[0].n_cells == 70000
+    eng.run_mcs(4)
+    eng.synchronize()
+    ok, _, _ = eng.recount_check()
+    assert ok
+    st = eng.stats()
+    assert st["attempts"] == 4 * 1024 * 1024 and st["accepted"] > 0 and st["spin_timeouts"] == 0
+    lat = eng.lattice()
+    v, i, sp, so = eng.cells()
+    ids = lat.ravel().astype(np.int64)
+    coords = np.indices(lat.shape).reshape(2, -1)
+    for d in range(2):
+        sums = np.bincount(ids, weights=coords[d], minlength=70001)
+        assert np.all((sp[1:, d].astype(np.int64) - sums[1:].astype(np.int64)) % 1024 == 0)
+    # global energy: volume and interface terms from the recounted V/I, plus
+    # J over each unordered pair of Moore neighbours with different owners
+    e_vi = np.sum(2.0 * (v[1:].astype(np.float64) - 12) ** 2 + 0.5 * (i[1:].astype(np.float64) - 14) ** 2)
+    e_adh = 0.0
+    for dr, dc in ((0, 1), (1, -1), (1, 0), (1, 1)):
+        nb = np.roll(np.roll(lat, -dr, axis=0), -dc, axis=1)
+        diff = lat != nb
+        both = diff & (lat != 0) & (nb != 0)
+        e_adh += 2.0 * both.sum() + 6.0 * (diff & ~both).sum()
+    assert abs(eng.energy() - (e_vi + e_adh)) <= 1e-9 * (e_vi + e_adh)
