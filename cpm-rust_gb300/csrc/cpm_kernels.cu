@@ -17,7 +17,7 @@
 // evaluate_moves_kernel — per-move parity harness: decides a list of
 //   (target, copy direction, u) on a frozen state with the same device
 //   functions the sweep uses.
-// recount_kernel / energy — exact recounts used by the checker and samples.
+// recount_kernel / energy — exact recounts for the recount check and samples.
 // table3d_kernel — generates the 2^26-bit 3D simple-point table on the
 //   device from the bitmask flood fill (simple_point.rs:242-276).
 #include <cuda_runtime.h>
