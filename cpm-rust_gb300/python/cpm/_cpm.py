@@ -308,27 +308,89 @@ class Status:
 
 
 class Sample:
-    """PySample (convert.rs:54-95). ``contact`` is the dense
-    ``(n_cells+1, n_cells+1)`` upper-triangular uint32 matrix, built from the
-    engine's sparse pairs on first access."""
+    """PySample (convert.rs:54-95): one sample of a run. Its fields are views
+    into the arrays its result was read into, made on access. ``contact`` is
+    the dense ``(n_cells+1, n_cells+1)`` upper-triangular uint32 matrix,
+    built from the engine's sparse pairs on first access."""
 
-    __slots__ = ("mcs", "conservative_energy", "ids", "volume", "interface", "centroid", "eigenvalues",
-                 "radius_of_gyration_sq", "kappa_sq", "fragmented_cells", "medium_component_volumes",
-                 "medium_component_touches_boundary", "lattice", "_contact_pairs", "_contact")
+    __slots__ = ("_a", "_s", "_lat", "_x", "_contact")
+
+    def __init__(self, arrays, s, lattice, lists):
+        # arrays: the result's per-field arrays; lists: (contact offsets,
+        # fragmented offsets, medium offsets, fragmented ids, medium volumes,
+        # medium boundary flags, mcs, energies) as Python lists
+        self._a, self._s, self._lat, self._x, self._contact = arrays, s, lattice, lists, None
 
     @property
-    def contact(self):
-        if self._contact is None:
-            a, b, n = self._contact_pairs
-            m = np.zeros((len(self.ids) + 1, len(self.ids) + 1), dtype=np.uint32)
-            m[a.astype(np.int64), b.astype(np.int64)] = n
-            self._contact = m
-        return self._contact
+    def mcs(self):
+        return self._x[6][self._s]
+
+    @property
+    def conservative_energy(self):
+        return self._x[7][self._s]
+
+    @property
+    def ids(self):
+        return self._a["ids"][self._s]
+
+    @property
+    def volume(self):
+        return self._a["volume"][self._s]
+
+    @property
+    def interface(self):
+        return self._a["interface"][self._s]
+
+    @property
+    def centroid(self):
+        return self._a["centroid"][self._s]
+
+    @property
+    def eigenvalues(self):
+        return self._a["eigenvalues"][self._s]
+
+    @property
+    def radius_of_gyration_sq(self):
+        return self._a["radius_of_gyration_sq"][self._s]
+
+    @property
+    def kappa_sq(self):
+        return self._a["kappa_sq"][self._s]
+
+    @property
+    def fragmented_cells(self):
+        fo = self._x[1]
+        return self._x[3][fo[self._s]:fo[self._s + 1]]
+
+    @property
+    def medium_component_volumes(self):
+        mo = self._x[2]
+        return self._x[4][mo[self._s]:mo[self._s + 1]]
+
+    @property
+    def medium_component_touches_boundary(self):
+        mo = self._x[2]
+        return self._x[5][mo[self._s]:mo[self._s + 1]]
+
+    @property
+    def lattice(self):
+        return self._lat[self._s] if self._lat is not None else None
 
     @property
     def contact_pairs(self):
         """Sparse form of ``contact``: (a, b, count) arrays with a < b."""
-        return self._contact_pairs
+        co = self._x[0]
+        c0, c1 = co[self._s], co[self._s + 1]
+        return (self._a["contact_a"][c0:c1], self._a["contact_b"][c0:c1], self._a["contact_count"][c0:c1])
+
+    @property
+    def contact(self):
+        if self._contact is None:
+            a, b, n = self.contact_pairs
+            m = np.zeros((len(self.ids) + 1, len(self.ids) + 1), dtype=np.uint32)
+            m[a.astype(np.int64), b.astype(np.int64)] = n
+            self._contact = m
+        return self._contact
 
 
 class RunResult:
@@ -413,28 +475,11 @@ def _read_samples_many(hs, dims):
         for name in ("centroid", "eigenvalues"):
             a[name] = a[name].reshape(ns, n, D)
         lat = big_lat[lat_start[k]:lat_start[k + 1]].reshape((ns,) + tuple(grid)) if lat_n[k] else None
-        co, fo, mo = a["contact_offsets"].tolist(), a["fragmented_offsets"].tolist(), a["medium_offsets"].tolist()
-        frag = a["fragmented_cells"].tolist()
-        mvol = a["medium_component_volumes"].tolist()
-        mtouch = [bool(x) for x in a["medium_component_touches_boundary"]]
-        mcs, en = a["mcs"].tolist(), a["conservative_energy"].tolist()
-        ca, cb, cc = a["contact_a"], a["contact_b"], a["contact_count"]
-        out = []
-        for s in range(ns):
-            smp = Sample()
-            smp.mcs = int(mcs[s])
-            smp.conservative_energy = float(en[s])
-            smp.ids, smp.volume, smp.interface = a["ids"][s], a["volume"][s], a["interface"][s]
-            smp.centroid, smp.eigenvalues = a["centroid"][s], a["eigenvalues"][s]
-            smp.radius_of_gyration_sq, smp.kappa_sq = a["radius_of_gyration_sq"][s], a["kappa_sq"][s]
-            smp.fragmented_cells = frag[fo[s]:fo[s + 1]]
-            smp.medium_component_volumes = mvol[mo[s]:mo[s + 1]]
-            smp.medium_component_touches_boundary = mtouch[mo[s]:mo[s + 1]]
-            smp.lattice = lat[s] if lat is not None else None
-            c0, c1 = co[s], co[s + 1]
-            smp._contact_pairs = (ca[c0:c1], cb[c0:c1], cc[c0:c1])
-            smp._contact = None
-            out.append(smp)
+        lists = (a["contact_offsets"].tolist(), a["fragmented_offsets"].tolist(), a["medium_offsets"].tolist(),
+                 a["fragmented_cells"].tolist(), a["medium_component_volumes"].tolist(),
+                 [bool(x) for x in a["medium_component_touches_boundary"]], a["mcs"].tolist(),
+                 a["conservative_energy"].tolist())
+        out = [Sample(a, s, lat, lists) for s in range(ns)]
         result.append(out)
     return result
 
