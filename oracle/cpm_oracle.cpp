@@ -10,7 +10,11 @@
 // 113-131: V=[7,9], I=[28,32], energy bits 4638468362461406824, model_hash
 // 60ec713d...) and the published derived seeds for master_seed=42
 // (notebooks/batch_execution_demo.ipynb, cell 7). `tests/test_oracle_kat.py`
-// checks both.
+// checks both. The loop's other modes (Metropolis-Hastings acceptance,
+// monte_carlo.rs:168-224; the Act term, energy.rs:329-471) have no frozen
+// trajectory in the reference; the Act term is pinned against the scenarios
+// of the reference's own unit tests (energy.rs:955-1300) and the MH decision
+// against its formula (`tests/test_oracle_modes.py`).
 //
 // Every function cites the reference file:line it restates. The third-party
 // arithmetic the reference pulls from crates that are not vendored in the
@@ -24,7 +28,8 @@
 //     7-round compression, 1024-byte chunks, binary merkle tree.
 //   * serde_json: compact JSON with fields in declaration order, used for the
 //     convention and model hashes (crates/cpm-core/src/config.rs:423-556).
-//   * libm exp: the reference calls f64::exp (glibc on Linux); so do we.
+//   * libm exp and pow: the reference calls f64::exp / f64::powf (glibc on
+//     Linux); so do we.
 //
 // Build: see oracle/Makefile (gcc -O2 -ffp-contract=off; Rust never fuses
 // multiply-add, so neither may we).
