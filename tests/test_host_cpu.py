@@ -263,3 +263,34 @@ def test_tiled_site_colours_partition_the_tile_into_non_adjacent_sets():
                         gl = {(g0 + i) % L for i in c}
                         for x in gl:
                             assert (x + 1) % L not in gl or L == 1, (L, g0, tc, c)
+
+
+def test_samples_are_views_into_their_results_arrays():
+    """Sample fields (convert.rs:54-95) read from the arrays a result was
+    read into: per-sample rows, the variable-length lists by their offsets,
+    the dense upper-triangular contact matrix built from the sparse pairs."""
+    import numpy as np
+
+    from cpm._cpm import Sample
+
+    ns, n = 2, 3
+    a = {
+        "ids": np.array([[1, 2, 3], [1, 2, 3]], np.uint32),
+        "volume": np.array([[5, 6, 7], [8, 9, 10]], np.uint32),
+        "interface": np.zeros((ns, n), np.uint32), "radius_of_gyration_sq": np.zeros((ns, n)),
+        "kappa_sq": np.zeros((ns, n)), "centroid": np.zeros((ns, n, 2)), "eigenvalues": np.zeros((ns, n, 2)),
+        "contact_a": np.array([0, 1, 0], np.uint32), "contact_b": np.array([2, 3, 1], np.uint32),
+        "contact_count": np.array([4, 5, 6], np.uint32),
+    }
+    lists = ([0, 2, 3], [0, 1, 1], [0, 0, 2], [3], [7, 1], [True, False], [100, 200], [1.5, 2.5])
+    s0, s1 = Sample(a, 0, None, lists), Sample(a, 1, None, lists)
+    assert s0.mcs == 100 and s1.conservative_energy == 2.5
+    assert list(s1.volume) == [8, 9, 10]
+    assert s0.fragmented_cells == [3] and s1.fragmented_cells == []
+    assert s0.medium_component_volumes == [] and s1.medium_component_volumes == [7, 1]
+    assert s1.medium_component_touches_boundary == [True, False]
+    pa, pb, pc = s0.contact_pairs
+    assert list(pa) == [0, 1] and list(pb) == [2, 3] and list(pc) == [4, 5]
+    m = s0.contact
+    assert m.shape == (4, 4) and m[0, 2] == 4 and m[1, 3] == 5 and m.sum() == 9
+    assert s1.contact[0, 1] == 6 and s0.lattice is None
