@@ -533,6 +533,17 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def max_over_ranks(value, dist):
+    """The largest `value` over the ranks of the process group (the job's
+    time is its slowest rank's); the tensor lives where the backend works."""
+    import torch
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 # ------------------------------------------------------------- GPU arm ----
 def cpu_baseline(args):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -587,9 +598,7 @@ def run_gpu(args, rank, world, dist):
     s1 = eng.stats()
     total_ms = sum(ms)
     if dist:
-        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+        total_ms = max_over_ranks(total_ms, dist)
     attempts = (s1["attempts"] - s0["attempts"])
     assert attempts == args.steps * args.mcs_per_step * n_sites, (attempts, s1, s0)
     ok, _, _ = eng.recount_check()
