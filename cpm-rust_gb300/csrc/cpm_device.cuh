@@ -313,11 +313,11 @@ __device__ __forceinline__ bool decide_move(const SimDesc& s, const SigT* sig, c
 }
 
 // ------------------------------------------------------ modes of the loop ----
-// Acceptance by Metropolis-Hastings and the Act term, on the padded
-// global-memory lattice (the global sweep and the parity harness; the
-// shared-memory sweeps never run these modes). Both decide in FP64 with the
-// reference's operation order; pow and exp are CUDA's, within an ulp of the
-// host library's.
+// Acceptance by Metropolis-Hastings and the Act term, on a whole padded
+// lattice (the global sweep, the shared-memory resident sweep and the
+// parity harness; the tiled sweep never runs these modes). Both decide in
+// FP64 with the reference's operation order; pow and exp are CUDA's, within
+// an ulp of the host library's. The acquisition MCS lives in HBM.
 
 // Interior padded index a (possibly halo) padded index stands for under a
 // periodic boundary (energy.rs:363-376 canonical_flat); itself otherwise.
@@ -337,14 +337,15 @@ __device__ __forceinline__ int64_t act_canonical(const SimDesc& s, int64_t f) {
 
 // Geometric mean of the activity max(0, max_act - (mcs - birth)) over
 // `site` and its copy neighbours owned by `relevant` (energy.rs:377-412).
-__device__ __forceinline__ double act_geometric_mean(const SimDesc& s, const uint32_t* sig, int64_t site,
+template <class SigT>
+__device__ __forceinline__ double act_geometric_mean(const SimDesc& s, const SigT* sig, int64_t site,
                                                      uint32_t relevant, uint32_t max_act, uint64_t mcs) {
     const int64_t is = act_canonical(s, site);
     double product = 1.0;
     uint32_t count = 0;
     for (int k = -1; k < s.n_copy; ++k) {
         const int64_t c = k < 0 ? is : act_canonical(s, is + s.copy_off[k]);
-        if (sig[c] != relevant) continue;
+        if ((uint32_t)sig[c] != relevant) continue;
         const uint64_t b = s.birth[c];
         const uint64_t elapsed = mcs > b ? mcs - b : 0ull;
         product = __dmul_rn(product, (double)((uint64_t)max_act > elapsed ? (uint64_t)max_act - elapsed : 0ull));
@@ -355,10 +356,11 @@ __device__ __forceinline__ double act_geometric_mean(const SimDesc& s, const uin
 
 // energy.rs:441-451: -(lambda_act / max_act) (GM_src - GM_tgt) of the
 // gaining cell's type; 0 when the medium gains.
-__device__ __forceinline__ double act_delta(const SimDesc& s, const uint32_t* sig, int64_t t, int64_t src, uint32_t L,
-                                            uint32_t G, uint64_t mcs) {
+template <class SigT>
+__device__ __forceinline__ double act_delta(const SimDesc& s, const SigT* sig, const uint16_t* adh_of, int64_t t,
+                                            int64_t src, uint32_t L, uint32_t G, uint64_t mcs) {
     if (G == 0) return 0.0;
-    const int ty = s.adh_of[G] - 1;
+    const int ty = adh_of[G] - 1;
     const double lambda = s.lambda_act[ty];
     const uint32_t mx = s.max_act[ty];
     const double gs = act_geometric_mean(s, sig, src, G, mx, mcs);
@@ -369,13 +371,13 @@ __device__ __forceinline__ double act_delta(const SimDesc& s, const uint32_t* si
 // monte_carlo.rs:147-196 for a total delta-H `dh`: Metropolis, or
 // Metropolis-Hastings with the copy-neighbour counts n_A (losing) and n_B
 // (gaining) of the target (rejected outright when n_A = 0).
-template <class Draw>
-__device__ __forceinline__ bool accept_modes(const SimDesc& s, const uint32_t* sig, int64_t t, uint32_t L, uint32_t G,
+template <class SigT, class Draw>
+__device__ __forceinline__ bool accept_modes(const SimDesc& s, const SigT* sig, int64_t t, uint32_t L, uint32_t G,
                                              double dh, const Draw& draw) {
     if (s.acceptance == 0) return metropolis(dh, dh > 0.0 ? draw.u() : 0.0);
     int na = 0, nb = 0;
     for (int k = 0; k < s.n_copy; ++k) {
-        const uint32_t c = sig[t + s.copy_off[k]];
+        const uint32_t c = (uint32_t)sig[t + s.copy_off[k]];
         na += c == L;
         nb += c == G;
     }
@@ -386,14 +388,15 @@ __device__ __forceinline__ bool accept_modes(const SimDesc& s, const uint32_t* s
 
 // The decision of one attempt under the configured modes; `dh_total`
 // receives the delta-H the decision used (conservative + Act).
-template <int NE, class Draw>
-__device__ __forceinline__ bool decide_modes(const SimDesc& s, const uint32_t* sig, int64_t t, int64_t src, uint32_t L,
-                                             uint32_t G, uint64_t mcs, const Draw& draw, int& dl, int& dg,
-                                             double& dh_total) {
-    const DeltaOut o = delta_h<NE, uint32_t>(s, sig, s.adh_of, s.volume, s.interface, t, L, G);
+template <int NE, class SigT, class Draw>
+__device__ __forceinline__ bool decide_modes(const SimDesc& s, const SigT* sig, const uint16_t* adh_of,
+                                             const uint32_t* volume, const uint32_t* interface, int64_t t,
+                                             int64_t src, uint32_t L, uint32_t G, uint64_t mcs, const Draw& draw,
+                                             int& dl, int& dg, double& dh_total) {
+    const DeltaOut o = delta_h<NE, SigT>(s, sig, adh_of, volume, interface, t, L, G);
     dl = o.dl;
     dg = o.dg;
-    dh_total = s.act ? __dadd_rn(o.dh, act_delta(s, sig, t, src, L, G, mcs)) : o.dh;
+    dh_total = s.act ? __dadd_rn(o.dh, act_delta(s, sig, adh_of, t, src, L, G, mcs)) : o.dh;
     return accept_modes(s, sig, t, L, G, dh_total, draw);
 }
 

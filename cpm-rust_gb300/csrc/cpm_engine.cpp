@@ -197,14 +197,14 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
     }
     CUDA_TRY(dev_alloc((void**)&arena_, std::max<size_t>(cv.off, 256)));
     CUDA_TRY(dev_alloc((void**)&d_descs_, std::max<size_t>(N, 1) * sizeof(SimDesc)));
-    CUDA_TRY(dev_alloc((void**)&d_next_, sizeof(int) * 16));
+    CUDA_TRY(dev_alloc((void**)&d_next_, sizeof(int) * 64));
     uint32_t* done_dev = nullptr;
     if (track_done_) {
         CUDA_TRY(cudaHostAlloc((void**)&done_host_, std::max<size_t>(N, 1) * 4, cudaHostAllocMapped));
         std::memset(done_host_, 0, std::max<size_t>(N, 1) * 4);
         CUDA_TRY(cudaHostGetDevicePointer((void**)&done_dev, done_host_, 0));
     }
-    device_bytes_ = std::max<size_t>(cv.off, 256) + std::max<size_t>(N, 1) * sizeof(SimDesc) + sizeof(int) * 16;
+    device_bytes_ = std::max<size_t>(cv.off, 256) + std::max<size_t>(N, 1) * sizeof(SimDesc) + sizeof(int) * 64;
     (void)t3;
     // ---- host staging, then one upload per buffer
     std::vector<char> stage(in_bytes, 0);
@@ -397,8 +397,9 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
 DeviceSims::Path DeviceSims::path(size_t i) const {
     const SimLayout& L = layouts_[i];
     if (force_global_) return GLOBAL;
-    // Metropolis-Hastings acceptance and the Act term run on the global sweep only
-    if (descs_[i].acceptance || descs_[i].act) return GLOBAL;
+    // Metropolis-Hastings acceptance and the Act term run on the resident
+    // sweep when the lattice fits, else on the global sweep (not tiled)
+    const bool modes = descs_[i].acceptance || descs_[i].act;
     int dims[3] = {(int)L.g.dims[0], (int)L.g.dims[1], (int)L.g.dims[2]}, nt[3] = {1, 1, 1}, max_box = 0;
     const bool tiled_ok = cpmgpu::tiled_plan(L.g.D, dims, L.g.periodic, nt, &max_box) &&
                           cpmgpu::tiled_smem_bytes(max_box, L.n_cells, 0, L.g.D, 0) <= cpmgpu::resident_smem_limit();
@@ -411,10 +412,10 @@ DeviceSims::Path DeviceSims::path(size_t i) const {
         // colour into the tiled sweep (many SMs instead of one; a different,
         // equally exact chain, hence opt-in).
         const int per_color = (nt[0] * nt[1] * nt[2]) >> L.g.D;
-        if (prefer_tiled_ && tiled_ok && per_color >= 8) return TILED;
+        if (prefer_tiled_ && tiled_ok && per_color >= 8 && !modes) return TILED;
         return RESIDENT;
     }
-    return tiled_ok ? TILED : GLOBAL;
+    return tiled_ok && !modes ? TILED : GLOBAL;
 }
 
 // One simulation on the tiled sweep: the run window is replayed from the
@@ -519,7 +520,9 @@ std::string DeviceSims::run(const std::vector<RunPlan>& plans, int grid_override
         }
         const Path pa = path(p.sim);
         if (pa == TILED) { tiled.push_back(p); continue; }
-        const int kind = pa == RESIDENT ? 1 + cpmgpu::resident_variant(L.g.n_padded, L.n_cells) : 0;
+        // 0: global sweep; resident: 1 + variant, + 2 with Metropolis-Hastings or Act
+        const int modes = descs_[p.sim].acceptance || descs_[p.sim].act ? 1 : 0;
+        const int kind = pa == RESIDENT ? 1 + cpmgpu::resident_variant(L.g.n_padded, L.n_cells) + 2 * modes : 0;
         groups[std::make_tuple(kind, L.g.D, L.NE)].push_back(p);
     }
     for (const RunPlan& p : tiled) {
@@ -527,6 +530,7 @@ std::string DeviceSims::run(const std::vector<RunPlan>& plans, int grid_override
         if (!err.empty()) return err;
     }
     if (groups.empty()) return "";
+    if (groups.size() > 64) return "too many kinds of simulation in one run (more than 64 kernel groups)";
     size_t total = 0;
     for (auto& kv : groups) total += kv.second.size();
     if (total > plans_cap_) {
@@ -546,7 +550,7 @@ std::string DeviceSims::run(const std::vector<RunPlan>& plans, int grid_override
         flat.insert(flat.end(), kv.second.begin(), kv.second.end());
     }
     CUDA_TRY(cudaMemcpyAsync(d_plans_, flat.data(), flat.size() * sizeof(RunPlan), cudaMemcpyHostToDevice, stream_));
-    CUDA_TRY(cudaMemsetAsync(d_next_, 0, sizeof(int) * 16, stream_));
+    CUDA_TRY(cudaMemsetAsync(d_next_, 0, sizeof(int) * 64, stream_));
     int dev = 0, sms = 1;
     CUDA_TRY(cudaGetDevice(&dev));
     CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -577,11 +581,11 @@ std::string DeviceSims::run(const std::vector<RunPlan>& plans, int grid_override
             smem = std::max(smem, cpmgpu::resident_smem_bytes(L.g.n_padded, L.n_cells));
         }
         if (res) {
-            const int variant = res - 1;
+            const int variant = (res - 1) & 1, modes = (res - 1) >> 1;
             int per_sm = 1;
-            CUDA_TRY(cpmgpu::resident_occupancy(D, NE, variant, smem, &per_sm));
+            CUDA_TRY(cpmgpu::resident_occupancy(D, NE, variant, modes, smem, &per_sm));
             int grid = grid_override > 0 ? grid_override : std::min<int>((int)r.second, sms * std::max(1, per_sm));
-            CUDA_TRY(cpmgpu::launch_resident(D, NE, variant, d_descs_, d_plans_ + r.first, (int)r.second, d_next_ + gi, t3, smem,
+            CUDA_TRY(cpmgpu::launch_resident(D, NE, variant, modes, d_descs_, d_plans_ + r.first, (int)r.second, d_next_ + gi, t3, smem,
                                              std::max(1, grid), gst));
         } else {
             int grid = grid_override > 0 ? grid_override : std::min<int>((int)r.second, sms * 4);

@@ -20,7 +20,7 @@ cudaError_t launch_recount(int D, int NE, const SimDesc* d_sim, int64_t n_sites,
 cudaError_t launch_energy(int D, int NE, const SimDesc* d_sim, double* d_out, cudaStream_t st);
 cudaError_t launch_table3d(uint64_t* d_words, const uint32_t* d_face, const uint32_t* d_full, uint32_t origin_mask,
                            cudaStream_t st);
-// Shared-memory-resident sweep (cpm_resident.cu): one CTA per simulation;
+// Shared-memory-resident sweep (cpm_resident_impl.cuh): one CTA per simulation;
 // variant 1 = 256 threads (two per SM) for simulations needing at most half
 // an SM's shared memory, variant 0 = 512 threads.
 int resident_variant(int64_t n_padded, int n_cells);
@@ -30,9 +30,20 @@ cudaError_t prepare_tiled_kernels();
 size_t resident_smem_bytes(int64_t n_padded, int n_cells);
 size_t resident_smem_limit();
 int resident_block(int variant);
-cudaError_t launch_resident(int D, int NE, int variant, SimDesc* d_sims, const RunPlan* d_plans, int n_plans,
-                            int* d_next, const uint64_t* d_t3, size_t smem, int grid, cudaStream_t st);
-cudaError_t resident_occupancy(int D, int NE, int variant, size_t smem, int* blocks_per_sm);
+// `modes`: the simulations use Metropolis-Hastings acceptance or the Act
+// term (kernels of cpm_resident_modes.cu); a launch serves one kind.
+cudaError_t launch_resident(int D, int NE, int variant, int modes, SimDesc* d_sims, const RunPlan* d_plans,
+                            int n_plans, int* d_next, const uint64_t* d_t3, size_t smem, int grid, cudaStream_t st);
+cudaError_t resident_occupancy(int D, int NE, int variant, int modes, size_t smem, int* blocks_per_sm);
+// The variants behind them.
+cudaError_t prepare_resident_kernels_plain();
+cudaError_t prepare_resident_kernels_modes();
+cudaError_t launch_resident_plain(int D, int NE, int variant, SimDesc* d_sims, const RunPlan* d_plans, int n_plans,
+                                  int* d_next, const uint64_t* d_t3, size_t smem, int grid, cudaStream_t st);
+cudaError_t launch_resident_modes(int D, int NE, int variant, SimDesc* d_sims, const RunPlan* d_plans, int n_plans,
+                                  int* d_next, const uint64_t* d_t3, size_t smem, int grid, cudaStream_t st);
+cudaError_t resident_occupancy_plain(int D, int NE, int variant, size_t smem, int* blocks_per_sm);
+cudaError_t resident_occupancy_modes(int D, int NE, int variant, size_t smem, int* blocks_per_sm);
 // Tiled cooperative sweep for large lattices (cpm_tiled.cu).
 bool tiled_plan(int D, const int* dims, int periodic, int* nt, int* max_box);
 size_t tiled_smem_bytes(int max_box, int n_cells, int cl_cap, int D, int reg_smem);

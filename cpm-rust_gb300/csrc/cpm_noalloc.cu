@@ -255,7 +255,7 @@ extern "C" int cpm_run_mcs_noalloc(cpm_device_sim* sim, uint64_t n_mcs, void* st
     const bool resident = sim->n_cells < 65535 &&
                           cpmgpu::resident_smem_bytes(g.n_padded, (int)sim->n_cells) <= cpmgpu::resident_smem_limit();
     if (resident)
-        e = cpmgpu::launch_resident(2, NE, cpmgpu::resident_variant(g.n_padded, (int)sim->n_cells), d_desc, d_plan, 1,
+        e = cpmgpu::launch_resident(2, NE, cpmgpu::resident_variant(g.n_padded, (int)sim->n_cells), 0, d_desc, d_plan, 1,
                                     d_next, nullptr,
                                     cpmgpu::resident_smem_bytes(g.n_padded, (int)sim->n_cells), 1, st);
     else

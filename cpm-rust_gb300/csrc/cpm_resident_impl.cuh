@@ -1,0 +1,683 @@
+// Shared-memory-resident sweep: one CTA owns one whole simulation.
+//
+// The halo-padded sigma lattice (16-bit ids), the per-cell volume and
+// interface and the candidate lists of a colour pass all live in shared
+// memory for the whole run plan; only the unwrapped position sums (touched
+// by accepted moves alone) and the run-window outputs go to global memory.
+//
+// A colour pass (sites pairwise >= 2 apart, so no attempt reads a site
+// another attempt of the pass writes) is resolved exactly as if its
+// candidates were applied one by one in a fixed priority order
+// (deterministic hash of the site's class index), each seeing the exact
+// current volume and interface of its two cells:
+//   1. build  — early-out and simple-point test (functions of sigma only);
+//   2. speculate — every candidate evaluates the FP64 Delta-H and the
+//      Metropolis test on the current V/I;
+//   3. finalise — a shared-memory fixpoint marks candidate m final when
+//      every lower-priority candidate on either of its cells is final and
+//      rejected (so m's evaluation used exactly the state it would see);
+//      final accepts are then pairwise cell-disjoint and commit in
+//      parallel; candidates on cells that changed are re-evaluated and the
+//      fixpoint repeats.
+// Rejections are the common outcome (most copies cost energy), so one
+// round usually finalises long chains of them; the number of rounds is the
+// depth of chained accepts, not the number of candidates per cell.
+//
+// Reference semantics per attempt: monte_carlo.rs:52-145; run window:
+// output.rs:434-468.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <mutex>
+
+#include "cpm_common.h"
+#include "cpm_device.cuh"
+#include "cpm_kernels.h"
+
+namespace cpmgpu {
+
+// Two block sizes: 512 threads (one CTA per SM) for simulations whose
+// shared state needs more than half an SM, 256 threads with half the
+// candidate capacity for smaller ones, so that two share an SM and hide
+// each other's barrier latency. Which one a simulation uses depends only on
+// its own size (resident_variant).
+template <int BS>
+struct ResCfg {
+    static constexpr int CMAX = BS == 512 ? 2048 : 1024;   // candidate slots of one chunk
+    static constexpr int CHUNK = BS == 512 ? 8192 : 4096;  // sites per chunk (halved while a chunk overflows CMAX)
+};
+
+// flag bits of a candidate
+enum : uint32_t {
+    F_K = 7u,           // copy direction (bits 0..2)
+    F_ACC = 1u << 3,    // current evaluation accepts
+    F_PEND = 1u << 4,   // not yet finalised
+    F_FIN = 1u << 5,    // final in this round's fixpoint
+    F_GUARD = 1u << 6,  // volume guard rejects
+    F_DONE = 1u << 7,   // committed this round (clears dirty marks)
+};
+
+struct ResLayout {
+    uint32_t sig, vol, itf, b0, b1, adh, dirty, c_site, c_key, c_cells, c_flags, c_dl, total;
+};
+
+__host__ __device__ inline uint32_t res_take(uint32_t& off, uint64_t bytes) {
+    const uint32_t o = off;
+    off = (uint32_t)((off + bytes + 15) & ~(uint64_t)15);
+    return o;
+}
+
+__host__ __device__ inline ResLayout res_layout(int64_t n_padded, int n_cells, int CMAX) {
+    ResLayout L;
+    uint32_t off = 0;
+    const uint64_t n1 = (uint64_t)n_cells + 1;
+    L.sig = res_take(off, (uint64_t)n_padded * 2);
+    L.vol = res_take(off, n1 * 4);
+    L.itf = res_take(off, n1 * 4);
+    L.b0 = res_take(off, n1 * 4);
+    L.b1 = res_take(off, n1 * 4);
+    L.adh = res_take(off, n1 * 2);
+    L.dirty = res_take(off, n1);
+    L.c_site = res_take(off, CMAX * 4);
+    L.c_key = res_take(off, CMAX * 4);
+    L.c_cells = res_take(off, CMAX * 4);
+    L.c_flags = res_take(off, CMAX * 4);
+    L.c_dl = res_take(off, CMAX * 2);
+    L.total = off;
+    return L;
+}
+
+struct PassInfoR {
+    int cnt[3], base[3], step[3], n;
+};
+
+__device__ __forceinline__ void make_pass_r(const SimDesc& s, int color, PassInfoR& p) {
+    int c = color;
+    p.n = 1;
+    for (int d = s.D - 1; d >= 0; --d) {
+        const int cd = c % s.ncol[d];
+        c /= s.ncol[d];
+        if (cd == 2) { p.base[d] = s.dims[d] - 1; p.step[d] = 0; p.cnt[d] = 1; }
+        else { p.base[d] = cd; p.step[d] = 2; p.cnt[d] = s.lim[d] > cd ? (s.lim[d] - cd + 1) / 2 : 0; }
+        p.n *= p.cnt[d];
+    }
+    for (int d = s.D; d < 3; ++d) { p.cnt[d] = 1; p.base[d] = 0; p.step[d] = 0; }
+}
+
+template <int D>
+__device__ __forceinline__ int site_r(const SimDesc& s, const PassInfoR& p, int idx, int* x) {
+    int f = 0;
+#pragma unroll
+    for (int d = D - 1; d >= 0; --d) {
+        const int i = idx % p.cnt[d];
+        idx /= p.cnt[d];
+        x[d] = p.base[d] + p.step[d] * i;
+        f += (x[d] + 1) * (int)s.strides[d];
+    }
+    return f;
+}
+
+struct CountersR {
+    unsigned long long attempts, nonnull, topo, guard, evaluated, accepted, rounds, iters, c_build, c_resolve;
+};
+
+template <int BLOCK>
+__device__ double block_sum_r(double v, double* scratch) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();
+    if (lane == 0) scratch[warp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < BLOCK / 32; ++w) t += scratch[w];
+        scratch[0] = t;
+    }
+    __syncthreads();
+    const double t = scratch[0];
+    __syncthreads();
+    return t;
+}
+
+// Global energy of the resident state (each unordered pair of different
+// neighbouring cells contributes J once; volume and interface terms).
+template <int D, int NE, int RB>
+__device__ double res_energy(const SimDesc& s, const uint16_t* sig, const uint32_t* vol, const uint32_t* itf,
+                             const uint16_t* adh, double* scratch) {
+    const int nt1 = s.n_types + 1;
+    double ea = 0.0;
+    for (int q = threadIdx.x; q < (int)s.n_sites; q += RB) {
+        int x[3];
+        int r = q, f = 0;
+#pragma unroll
+        for (int d = D - 1; d >= 0; --d) {
+            x[d] = r % s.dims[d];
+            r /= s.dims[d];
+            f += (x[d] + 1) * (int)s.strides[d];
+        }
+        const uint32_t c = sig[f];
+        const int ci = adh[c];
+#pragma unroll
+        for (int k = 0; k < NE; ++k) {
+            bool count = (s.energy_pos_mask >> k) & 1u;
+            if (!count && !s.periodic) {
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    const int y = x[d] + s.energy_vec[k][d];
+                    if (y < 0 || y >= s.dims[d]) count = true;
+                }
+            }
+            if (!count) continue;
+            const uint32_t n = sig[f + (int)s.energy_off[k]];
+            if (n != c) ea += s.J[ci * nt1 + adh[n]];
+        }
+    }
+    double ev = 0.0, ei = 0.0;
+    for (int id = 1 + threadIdx.x; id <= s.n_cells; id += RB) {
+        const int ty = adh[id] - 1;
+        ev += quad_term(s.lambda_v[ty], s.target_v[ty], (double)vol[id]);
+        ei += quad_term(s.lambda_i[ty], s.target_i[ty], (double)itf[id]);
+    }
+    ev = block_sum_r<RB>(ev, scratch);
+    ei = block_sum_r<RB>(ei, scratch);
+    ea = block_sum_r<RB>(ea, scratch);
+    return (ev + ei) + ea;
+}
+
+// MODES: the simulations use Metropolis-Hastings acceptance or the Act term
+// (decide_modes; compiled as separate kernels, so that the Metropolis
+// kernels keep their registers).
+template <int D, int NE, int RB, bool MODES>
+struct Resident {
+    static constexpr int CMAX = ResCfg<RB>::CMAX;
+    static constexpr int CHUNK = ResCfg<RB>::CHUNK;
+    const SimDesc& s;
+    uint16_t* sig;
+    uint32_t *vol, *itf, *b0, *b1;
+    uint16_t* adh;
+    uint8_t* dirty;
+    uint32_t *c_site, *c_key, *c_cells, *c_flags;
+    int16_t* c_dl;  // dl in the low byte, dg in the high byte
+    const uint64_t* t3;
+    int* s_n;
+    int* s_flag;
+
+    // Evaluate candidate c on the current state (guard, Delta-H, Metropolis).
+    __device__ void evaluate(int c, uint64_t mcs) {
+        const int t = (int)c_site[c];
+        const uint32_t cells = c_cells[c];
+        const uint32_t L = cells & 0xFFFFu, G = cells >> 16;
+        uint32_t fl = c_flags[c] & ~(F_ACC | F_GUARD);
+        if (L != 0 && vol[L] <= s.min_cell_volume) {
+            fl |= F_GUARD;
+        } else {
+            int dl = 0, dg = 0;
+            bool acc;
+            if constexpr (MODES) {
+                double dh = 0.0;
+                acc = decide_modes<NE>(s, sig, adh, vol, itf, t, t + s.copy_off[fl & F_K], L, G, mcs,
+                                       PhiloxDraw{s.seed, mcs, (uint32_t)t}, dl, dg, dh);
+            } else {
+                acc = decide_move<NE, uint16_t>(s, sig, adh, vol, itf, t, L, G, PhiloxDraw{s.seed, mcs, (uint32_t)t}, dl, dg);
+            }
+            if (acc) fl |= F_ACC;
+            c_dl[c] = (int16_t)((dl & 0xFF) | ((dg & 0xFF) << 8));
+        }
+        c_flags[c] = fl;
+    }
+
+    __device__ void commit(int c, uint64_t mcs) {
+        const int t = (int)c_site[c];
+        const uint32_t cells = c_cells[c];
+        const uint32_t L = cells & 0xFFFFu, G = cells >> 16;
+        const int16_t dd = c_dl[c];
+        const int dl = (int)(int8_t)(dd & 0xFF), dg = (int)(int8_t)((dd >> 8) & 0xFF);
+        int x[3];
+        int f = t;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const int q = f / (int)s.strides[d];
+            f -= q * (int)s.strides[d];
+            x[d] = q - 1;
+        }
+        commit_move<D, uint16_t>(s, sig, vol, itf, s.sum_pos, s.sum_outer, x, L, G, dl, dg);
+        if constexpr (MODES) {
+            if (s.act) s.birth[t] = (uint32_t)mcs;  // energy.rs:453-458
+        }
+        if (L) dirty[L] = 1;
+        if (G) dirty[G] = 1;
+    }
+
+    // Resolve the candidates [0, n) of one chunk in priority order.
+    __device__ void resolve(int n, uint64_t mcs, CountersR& ct) {
+        const int tid = threadIdx.x;
+        for (int c = tid; c < n; c += RB) evaluate(c, mcs);
+        __syncthreads();
+        for (;;) {
+            // ---- finality. A pending candidate is final unless an accepting
+            // candidate lies in its lower closure (lower-key candidates
+            // sharing a cell, transitively): then every candidate before it
+            // in the sequential order leaves its cells as they are. Per cell,
+            // T = the lowest key of an accepting or tainted candidate on it;
+            // a candidate with a key above T on either cell is tainted and
+            // lowers T on both; iterate until T is stable. Rejects add
+            // nothing, so the iterations count cross-cell hops of accepts.
+            for (int c = tid; c < n; c += RB) {
+                if (!(c_flags[c] & F_PEND)) continue;
+                const uint32_t cells = c_cells[c];
+                if (cells & 0xFFFFu) b0[cells & 0xFFFFu] = 0xFFFFFFFFu;
+                if (cells >> 16) b0[cells >> 16] = 0xFFFFFFFFu;
+            }
+            __syncthreads();
+            for (int c = tid; c < n; c += RB) {
+                const uint32_t fl = c_flags[c];
+                if (!(fl & F_PEND) || !(fl & F_ACC) || (fl & F_GUARD)) continue;
+                const uint32_t cells = c_cells[c], key = c_key[c];
+                if (cells & 0xFFFFu) atomicMin(&b0[cells & 0xFFFFu], key);
+                if (cells >> 16) atomicMin(&b0[cells >> 16], key);
+            }
+            for (;;) {
+                __syncthreads();
+                int changed = 0;
+                for (int c = tid; c < n; c += RB) {
+                    if (!(c_flags[c] & F_PEND)) continue;
+                    const uint32_t cells = c_cells[c], key = c_key[c];
+                    const uint32_t L = cells & 0xFFFFu, G = cells >> 16;
+                    const bool tainted = (L && key > b0[L]) || (G && key > b0[G]);
+                    if (!tainted) continue;
+                    if (L && atomicMin(&b0[L], key) > key) changed = 1;
+                    if (G && atomicMin(&b0[G], key) > key) changed = 1;
+                }
+                ct.iters++;
+                if (!__syncthreads_or(changed)) break;
+            }
+            // ---- apply the final candidates
+            int left = 0;
+            for (int c = tid; c < n; c += RB) {
+                uint32_t fl = c_flags[c];
+                if (!(fl & F_PEND)) continue;
+                const uint32_t cells = c_cells[c], key = c_key[c];
+                const uint32_t L = cells & 0xFFFFu, G = cells >> 16;
+                if ((L && key > b0[L]) || (G && key > b0[G])) { left = 1; continue; }
+                fl &= ~F_PEND;
+                if (fl & F_GUARD) {
+                    ct.guard++;
+                } else {
+                    ct.evaluated++;
+                    if (fl & F_ACC) {
+                        commit(c, mcs);
+                        fl |= F_DONE;
+                        ct.accepted++;
+                    }
+                }
+                c_flags[c] = fl;
+            }
+            ct.rounds++;
+            const int more = __syncthreads_or(left);
+            if (!more) break;
+            // ---- re-evaluate candidates whose cells changed, then clear the marks
+            for (int c = tid; c < n; c += RB) {
+                const uint32_t fl = c_flags[c];
+                if (!(fl & F_PEND)) continue;
+                const uint32_t cells = c_cells[c];
+                if (dirty[cells & 0xFFFFu] || dirty[cells >> 16]) evaluate(c, mcs);
+            }
+            __syncthreads();
+            for (int c = tid; c < n; c += RB) {
+                uint32_t fl = c_flags[c];
+                if (!(fl & F_DONE)) continue;
+                const uint32_t cells = c_cells[c];
+                dirty[cells & 0xFFFFu] = 0;
+                dirty[cells >> 16] = 0;
+                c_flags[c] = fl & ~F_DONE;
+            }
+            __syncthreads();
+        }
+        // clear the marks of the last round's commits
+        for (int c = tid; c < n; c += RB) {
+            const uint32_t fl = c_flags[c];
+            if (!(fl & F_DONE)) continue;
+            const uint32_t cells = c_cells[c];
+            dirty[cells & 0xFFFFu] = 0;
+            dirty[cells >> 16] = 0;
+        }
+        __syncthreads();
+    }
+
+    // One colour pass: chunks of the class in index order.
+    __device__ void pass(const PassInfoR& p, uint64_t mcs, uint32_t pass_key, CountersR& ct) {
+        const int tid = threadIdx.x;
+        const int lane = tid & 31;
+        int start = 0;
+        while (start < p.n) {
+            int len = min(CHUNK, p.n - start);
+            for (;;) {
+                const long long t0 = clock64();
+                if (tid == 0) *s_n = 0;
+                __syncthreads();
+                unsigned long long nonnull = 0, topo = 0;
+                for (int j0 = 0; j0 < len; j0 += RB) {
+                    const int j = j0 + tid;
+                    bool cand = false;
+                    int t = 0, k = 0;
+                    uint32_t L = 0, G = 0;
+                    if (j < len) {
+                        int x[3];
+                        t = site_r<D>(s, p, start + j, x);
+                        const uint4 r = site_draw(s.seed, mcs, (uint32_t)t);
+                        k = (int)(((unsigned long long)r.x * (unsigned)s.n_copy) >> 32);
+                        L = sig[t];
+                        G = sig[t + (int)s.copy_off[k]];
+                        if (L != G) {
+                            ++nonnull;
+                            if (preserves_topology<D, uint16_t>(s, sig, t, L, s.table2d, t3)) cand = true;
+                            else ++topo;
+                        }
+                    }
+                    const unsigned m = __ballot_sync(0xffffffffu, cand);
+                    int base = 0;
+                    if (lane == 0 && m) base = atomicAdd(s_n, __popc(m));
+                    base = __shfl_sync(0xffffffffu, base, 0);
+                    if (cand) {
+                        const int pos = base + __popc(m & ((1u << lane) - 1));
+                        if (pos < CMAX) {
+                            c_site[pos] = (uint32_t)t;
+                            c_cells[pos] = L | (G << 16);
+                            c_key[pos] = (mix32((uint32_t)j * 0x9E3779B9u ^ pass_key) & 0xFFFFC000u) | (uint32_t)j;
+                            c_flags[pos] = (uint32_t)k | F_PEND;
+                        }
+                    }
+                }
+                __syncthreads();
+                const int n = *s_n;
+                __syncthreads();
+                if (n > CMAX) { len >>= 1; continue; }  // retry this chunk with fewer sites
+                ct.attempts += 0;  // attempts are counted per MCS (every site once)
+                ct.nonnull += nonnull;
+                ct.topo += topo;
+                const long long t1 = clock64();
+                ct.c_build += t1 - t0;
+                if (n > 0) resolve(n, mcs, ct);
+                ct.c_resolve += clock64() - t1;
+                break;
+            }
+            start += len;
+        }
+    }
+};
+
+template <int D, int NE, int RB, bool MODES>
+__global__ void __launch_bounds__(RB, 512 / RB) resident_kernel(SimDesc* sims, const RunPlan* plans, int n_plans,
+                                                                int* next_plan, const uint64_t* t3) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    __shared__ SimDesc sd;
+    __shared__ int s_plan, s_n, s_flag;
+    __shared__ int perm[27];
+    __shared__ PassInfoR pinfo;
+    __shared__ double scratch[RB / 32];
+    __shared__ unsigned long long sstat[10];
+    const int tid = threadIdx.x;
+    for (;;) {
+        if (tid == 0) s_plan = atomicAdd(next_plan, 1);
+        __syncthreads();
+        const int pl = s_plan;
+        __syncthreads();
+        if (pl >= n_plans) return;
+        const RunPlan plan = plans[pl];
+        if (tid == 0) sd = sims[plan.sim];
+        if (tid < 10) sstat[tid] = 0;
+        __syncthreads();
+        const ResLayout lay = res_layout(sd.n_padded, sd.n_cells, ResCfg<RB>::CMAX);
+        Resident<D, NE, RB, MODES> R{sd,
+                          (uint16_t*)(sm + lay.sig),
+                          (uint32_t*)(sm + lay.vol),
+                          (uint32_t*)(sm + lay.itf),
+                          (uint32_t*)(sm + lay.b0),
+                          (uint32_t*)(sm + lay.b1),
+                          (uint16_t*)(sm + lay.adh),
+                          (uint8_t*)(sm + lay.dirty),
+                          (uint32_t*)(sm + lay.c_site),
+                          (uint32_t*)(sm + lay.c_key),
+                          (uint32_t*)(sm + lay.c_cells),
+                          (uint32_t*)(sm + lay.c_flags),
+                          (int16_t*)(sm + lay.c_dl),
+                          t3,
+                          &s_n,
+                          &s_flag};
+        // ---- stage the state into shared memory
+        for (int f = tid; f < (int)sd.n_padded; f += RB) R.sig[f] = (uint16_t)sd.sigma[f];
+        for (int id = tid; id <= sd.n_cells; id += RB) {
+            R.vol[id] = sd.volume[id];
+            R.itf[id] = sd.interface[id];
+            R.adh[id] = sd.adh_of[id];
+            R.dirty[id] = 0;
+        }
+        __syncthreads();
+        CountersR ct = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+        uint64_t mcs = sd.mcs;
+        auto one_mcs = [&](uint64_t m) {
+            if (tid == 0) {
+                const int nc = sd.n_colors;
+                for (int c = 0; c < nc; ++c) perm[c] = c;
+                for (int c = nc - 1; c > 0; --c) {
+                    const uint4 r = aux_draw(sd.seed, m, TAG_ORDER, (uint32_t)c, 0u);
+                    const int j = (int)(((unsigned long long)r.x * (unsigned)(c + 1)) >> 32);
+                    const int tmp = perm[c]; perm[c] = perm[j]; perm[j] = tmp;
+                }
+            }
+            __syncthreads();
+            for (int pi = 0; pi < sd.n_colors; ++pi) {
+                if (tid == 0) make_pass_r(sd, perm[pi], pinfo);
+                __syncthreads();
+                const PassInfoR p = pinfo;
+                const uint32_t pass_key = aux_draw(sd.seed, m, TAG_PASS, (uint32_t)pi, 0u).x;
+                R.pass(p, m, pass_key, ct);
+                __syncthreads();
+            }
+            ct.attempts += (tid == 0) ? (unsigned long long)sd.n_sites : 0ull;
+        };
+        // ---- run plan (output.rs:441-468)
+        uint64_t burned = 0;
+        int e_idx = 0;
+        while (burned < plan.burn_in) {
+            const uint64_t chunk = plan.interval < plan.burn_in - burned ? plan.interval : plan.burn_in - burned;
+            for (uint64_t m = 0; m < chunk; ++m, ++mcs) one_mcs(mcs);
+            burned += chunk;
+            if (burned >= plan.energy_sample_start) {
+                const double e = res_energy<D, NE, RB>(sd, R.sig, R.vol, R.itf, R.adh, scratch);
+                if (tid == 0 && sd.energy_out) sd.energy_out[e_idx] = e;
+                ++e_idx;
+            }
+        }
+        for (int smp = 0; smp < plan.n_samples; ++smp) {
+            for (uint64_t m = 0; m < plan.interval; ++m, ++mcs) one_mcs(mcs);
+            const double e = res_energy<D, NE, RB>(sd, R.sig, R.vol, R.itf, R.adh, scratch);
+            if (tid == 0 && sd.energy_out) sd.energy_out[e_idx + smp] = e;
+            if (plan.write_samples) {
+                const int n1 = sd.n_cells + 1;
+                for (int id = tid; id < n1; id += RB) {
+                    sd.sample_volume[(int64_t)smp * n1 + id] = R.vol[id];
+                    sd.sample_interface[(int64_t)smp * n1 + id] = R.itf[id];
+                    for (int d = 0; d < D; ++d)
+                        sd.sample_sum_pos[((int64_t)smp * n1 + id) * D + d] = sd.sum_pos[(int64_t)id * D + d];
+                    for (int d = 0; d < D * D; ++d)
+                        sd.sample_sum_outer[((int64_t)smp * n1 + id) * D * D + d] = sd.sum_outer[(int64_t)id * D * D + d];
+                }
+            }
+            if (plan.write_lattice && sd.sample_lattice) {
+                for (int q = tid; q < (int)sd.n_sites; q += RB) {
+                    int r = q, f = 0;
+#pragma unroll
+                    for (int d = D - 1; d >= 0; --d) {
+                        f += (r % sd.dims[d] + 1) * (int)sd.strides[d];
+                        r /= sd.dims[d];
+                    }
+                    sd.sample_lattice[(int64_t)smp * sd.n_sites + q] = R.sig[f];
+                }
+            }
+            __syncthreads();
+        }
+        // ---- write the state back
+        for (int f = tid; f < (int)sd.n_padded; f += RB) sd.sigma[f] = R.sig[f];
+        for (int id = tid; id <= sd.n_cells; id += RB) {
+            sd.volume[id] = R.vol[id];
+            sd.interface[id] = R.itf[id];
+        }
+        atomicAdd(&sstat[CPM_STAT_ATTEMPTS], ct.attempts);
+        atomicAdd(&sstat[CPM_STAT_NONNULL], ct.nonnull);
+        atomicAdd(&sstat[CPM_STAT_TOPO_REJECT], ct.topo);
+        atomicAdd(&sstat[CPM_STAT_GUARD_REJECT], ct.guard);
+        atomicAdd(&sstat[CPM_STAT_EVALUATED], ct.evaluated);
+        atomicAdd(&sstat[CPM_STAT_ACCEPTED], ct.accepted);
+        atomicAdd(&sstat[9], ct.iters);
+        __syncthreads();
+        if (tid < 6) atomicAdd(&sd.stats[tid], sstat[tid]);
+        if (tid == 0) {
+            atomicAdd(&sd.stats[CPM_STAT_ROUNDS], ct.rounds);
+            atomicAdd(&sd.stats[CPM_STAT_PASSES], (unsigned long long)(mcs - sd.mcs) * sd.n_colors);
+            atomicAdd(&sd.stats[9], sstat[9]);
+            atomicAdd(&sd.stats[CPM_STAT_CYC_RES_BUILD], ct.c_build);
+            atomicAdd(&sd.stats[CPM_STAT_CYC_RES_RESOLVE], ct.c_resolve);
+            sims[plan.sim].mcs = mcs;
+        }
+        __syncthreads();
+        if (tid == 0 && sd.done_flag) {
+            // every write of this plan (state, samples, counters) before the flag
+            __threadfence_system();
+            *(volatile uint32_t*)sd.done_flag = 1u;
+        }
+        __syncthreads();
+    }
+}
+
+static int res_index(int D, int NE) {
+    if (D == 2 && NE == 4) return 0;
+    if (D == 2 && NE == 8) return 1;
+    if (D == 3 && NE == 6) return 2;
+    if (D == 3 && NE == 18) return 3;
+    if (D == 3 && NE == 26) return 4;
+    return -1;
+}
+
+// The kernel variants of the including unit: Metropolis in cpm_resident.cu;
+// Metropolis-Hastings / Act in cpm_resident_modes.cu, which includes this
+// file with CPM_RESIDENT_MODES_UNIT defined (two units build in parallel).
+// The host entry points shared by both are compiled in cpm_resident.cu only.
+#ifndef CPM_RESIDENT_MODES_UNIT
+#define RES_MODES false
+#define RES_VARIANT(name) name##_plain
+#else
+#define RES_MODES true
+#define RES_VARIANT(name) name##_modes
+#endif
+
+// The kernels' shared-memory limit is raised once per device, before any
+// launch: changing a function attribute while kernels run can wait for
+// them, which would serialise launches on different streams.
+cudaError_t RES_VARIANT(prepare_resident_kernels)() {
+    static std::mutex mu;
+    static bool done[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    if (dev >= 0 && dev < 64 && done[dev]) return cudaSuccess;
+    const int smem = (int)resident_smem_limit();
+#define RES_ATTR(D_, NE_)                                                                                    \
+    if ((e = cudaFuncSetAttribute(resident_kernel<D_, NE_, 256, RES_MODES>,                                  \
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)        \
+        return e;                                                                                              \
+    if ((e = cudaFuncSetAttribute(resident_kernel<D_, NE_, 512, RES_MODES>,                                  \
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)        \
+        return e;
+    RES_ATTR(2, 4)
+    RES_ATTR(2, 8)
+    RES_ATTR(3, 6)
+    RES_ATTR(3, 18)
+    RES_ATTR(3, 26)
+#undef RES_ATTR
+    if (dev >= 0 && dev < 64) done[dev] = true;
+    return cudaSuccess;
+}
+
+cudaError_t RES_VARIANT(launch_resident)(int Dd, int NEd, int variant, SimDesc* d_sims, const RunPlan* d_plans,
+                                         int n_plans, int* d_next, const uint64_t* d_t3, size_t smem, int grid,
+                                         cudaStream_t st) {
+    cudaError_t e = RES_VARIANT(prepare_resident_kernels)();
+    if (e != cudaSuccess) return e;
+#define RES_CASE(I, D_, NE_)                                                                                      \
+    case I: {                                                                                                     \
+        if (variant)                                                                                              \
+            resident_kernel<D_, NE_, 256, RES_MODES><<<grid, 256, smem, st>>>(d_sims, d_plans, n_plans, d_next, d_t3); \
+        else                                                                                                      \
+            resident_kernel<D_, NE_, 512, RES_MODES><<<grid, 512, smem, st>>>(d_sims, d_plans, n_plans, d_next, d_t3); \
+        break;                                                                                                    \
+    }
+    switch (res_index(Dd, NEd)) {
+        RES_CASE(0, 2, 4)
+        RES_CASE(1, 2, 8)
+        RES_CASE(2, 3, 6)
+        RES_CASE(3, 3, 18)
+        RES_CASE(4, 3, 26)
+        default: return cudaErrorInvalidValue;
+    }
+#undef RES_CASE
+    return cudaGetLastError();
+}
+
+cudaError_t RES_VARIANT(resident_occupancy)(int Dd, int NEd, int variant, size_t smem, int* blocks_per_sm) {
+    *blocks_per_sm = 1;
+    cudaError_t e = RES_VARIANT(prepare_resident_kernels)();
+    if (e != cudaSuccess) return e;
+#define OCC_CASE(I, D_, NE_)                                                                                      \
+    case I:                                                                                                       \
+        return variant ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(                                          \
+                             blocks_per_sm, resident_kernel<D_, NE_, 256, RES_MODES>, 256, smem)                  \
+                       : cudaOccupancyMaxActiveBlocksPerMultiprocessor(                                          \
+                             blocks_per_sm, resident_kernel<D_, NE_, 512, RES_MODES>, 512, smem);
+    switch (res_index(Dd, NEd)) {
+        OCC_CASE(0, 2, 4)
+        OCC_CASE(1, 2, 8)
+        OCC_CASE(2, 3, 6)
+        OCC_CASE(3, 3, 18)
+        OCC_CASE(4, 3, 26)
+        default: return cudaErrorInvalidValue;
+    }
+#undef OCC_CASE
+}
+
+#ifndef CPM_RESIDENT_MODES_UNIT
+size_t resident_smem_limit() { return 227 * 1024 - 4096; }
+
+// 1: the 256-thread variant (two CTAs per SM), when its shared state fits
+// half an SM; 0: the 512-thread variant.
+int resident_variant(int64_t n_padded, int n_cells) {
+    return res_layout(n_padded, n_cells, ResCfg<256>::CMAX).total <= resident_smem_limit() / 2 - 1024 ? 1 : 0;
+}
+size_t resident_smem_bytes(int64_t n_padded, int n_cells) {
+    return resident_variant(n_padded, n_cells) ? res_layout(n_padded, n_cells, ResCfg<256>::CMAX).total
+                                               : res_layout(n_padded, n_cells, ResCfg<512>::CMAX).total;
+}
+int resident_block(int variant) { return variant ? 256 : 512; }
+
+cudaError_t prepare_resident_kernels() {
+    cudaError_t e = prepare_resident_kernels_plain();
+    return e == cudaSuccess ? prepare_resident_kernels_modes() : e;
+}
+
+cudaError_t launch_resident(int Dd, int NEd, int variant, int modes, SimDesc* d_sims, const RunPlan* d_plans,
+                            int n_plans, int* d_next, const uint64_t* d_t3, size_t smem, int grid, cudaStream_t st) {
+    return modes ? launch_resident_modes(Dd, NEd, variant, d_sims, d_plans, n_plans, d_next, d_t3, smem, grid, st)
+                 : launch_resident_plain(Dd, NEd, variant, d_sims, d_plans, n_plans, d_next, d_t3, smem, grid, st);
+}
+
+cudaError_t resident_occupancy(int Dd, int NEd, int variant, int modes, size_t smem, int* blocks_per_sm) {
+    return modes ? resident_occupancy_modes(Dd, NEd, variant, smem, blocks_per_sm)
+                 : resident_occupancy_plain(Dd, NEd, variant, smem, blocks_per_sm);
+}
+#endif
+
+#undef RES_MODES
+#undef RES_VARIANT
+
+}  // namespace cpmgpu
