@@ -523,6 +523,10 @@ struct Sim {
     // (energy.rs:329-471), off unless set.
     int acceptance = 0;
     bool act = false;
+    // The connectivity check of an attempt; off only in the reference's
+    // exact-Boltzmann harness (`attempt(cpm, false)`, monte_carlo.rs:37-42,
+    // tests/exact_boltzmann.rs), where the chain must be free to reshape.
+    bool check_topology = true;
     std::vector<double> lambda_act;  // per type
     std::vector<uint32_t> max_act;   // per type
     std::vector<uint32_t> birth;     // per padded site: MCS at which its owner acquired it
@@ -793,7 +797,7 @@ struct Sim {
         const int64_t sf = tf + copy_off[k];
         const uint32_t lo = lat.cells[tf], ga = lat.cells[sf];
         if (lo == ga) return false;
-        if (!preserves_topology(tf, lo)) return false;
+        if (check_topology && !preserves_topology(tf, lo)) return false;
         if (lo != 0 && volume[lo - 1] <= cfg.min_cell_volume) return false;
         const double dh = total_delta(tf, lo, ga);
         // Act steers the decision but never reaches the conservative energy
@@ -1214,6 +1218,20 @@ void orc_set_modes(void* h, int acceptance, const double* lambda_act, const uint
     }
 }
 void orc_set_local_halo(void* h, int on) { ((Sim*)h)->local_halo = on != 0; }
+void orc_set_check_topology(void* h, int on) { ((Sim*)h)->check_topology = on != 0; }
+// Thinned chain samples (tests/exact_boltzmann.rs, single_cell_/two_cell_
+// harness): `burn_in` attempts, then per sample `thin` attempts followed by a
+// copy of the interior lattice (n_sites words) into out[i * n_sites].
+void orc_sample_attempts(void* h, uint64_t burn_in, int64_t n_samples, uint64_t thin, uint32_t* out) {
+    Sim* s = (Sim*)h;
+    for (uint64_t a = 0; a < burn_in; ++a) s->attempt();
+    const int64_t ns = s->lat.n_sites();
+    for (int64_t i = 0; i < n_samples; ++i) {
+        for (uint64_t a = 0; a < thin; ++a) s->attempt();
+        int64_t j = 0;
+        s->lat.each_interior([&](const int64_t* c) { out[i * ns + j++] = s->lat.cells[s->lat.flat(c)]; });
+    }
+}
 int orc_init_explicit(void* h, const uint32_t* lattice, int64_t n_sites, const uint32_t* cell_type_of, int n_cells, char* err, int errlen) {
     Sim* s = (Sim*)h;
     if (!s->place_explicit(lattice, n_sites, cell_type_of, n_cells)) { if (err) std::snprintf(err, errlen, "%s", s->err.c_str()); return -1; }

@@ -111,6 +111,8 @@ def lib():
             L.orc_act_delta.argtypes = [P, ctypes.c_int64, ctypes.c_int64]
             L.orc_act_delta.restype = ctypes.c_double
             L.orc_set_local_halo.argtypes = [P, ctypes.c_int]
+            L.orc_set_check_topology.argtypes = [P, ctypes.c_int]
+            L.orc_sample_attempts.argtypes = [P, ctypes.c_uint64, ctypes.c_int64, ctypes.c_uint64, P]
             L.orc_init_explicit.argtypes = [P, P, ctypes.c_int64, P, ctypes.c_int, ctypes.c_char_p, ctypes.c_int]
             L.orc_init_default.argtypes = [P, ctypes.c_char_p, ctypes.c_int]
             L.orc_run_mcs.argtypes = [P, ctypes.c_uint64]
@@ -240,6 +242,18 @@ class OracleSim:
 
     def set_local_halo(self, on: bool):
         lib().orc_set_local_halo(self.h, int(on))
+
+    def set_check_topology(self, on: bool):
+        """Connectivity check of each attempt; off only for the exact-Boltzmann
+        harness (tests/exact_boltzmann.rs calls attempt(cpm, false))."""
+        lib().orc_set_check_topology(self.h, int(on))
+
+    def sample_attempts(self, burn_in: int, n_samples: int, thin: int) -> np.ndarray:
+        """`burn_in` single attempts, then `n_samples` interior lattices, each
+        after `thin` more attempts; shape (n_samples, *grid)."""
+        out = np.zeros((int(n_samples), *self.spec.grid), np.uint32)
+        lib().orc_sample_attempts(self.h, int(burn_in), int(n_samples), int(thin), _ptr(out))
+        return out
 
     def init_explicit(self, lattice, cell_type_of):
         lat = np.ascontiguousarray(np.asarray(lattice, dtype=np.uint32).ravel())

@@ -1,6 +1,7 @@
 """The loop's other modes on the device: Metropolis-Hastings acceptance
 (monte_carlo.rs:168-196) and the Act term (energy.rs:329-471), run by the
-global-memory sweep.
+resident sweep when the lattice fits in shared memory and by the
+global-memory sweep otherwise.
 
 * Per move: for states the oracle reached (its acquisition MCS included) the
   device decides every proposed move as the oracle does, with the same
@@ -105,10 +106,16 @@ def test_commit_sets_acquisition_mcs(name, cuda_required):
     assert np.array_equal(eng.read_birth(), sim.birth())
 
 
+@pytest.mark.parametrize("sweep", ["auto", "global"])
 @pytest.mark.parametrize("name", ["mh_2d", "act_2d", "act_3d"])
-def test_runs_keep_exact_state(name, cuda_required):
+def test_runs_keep_exact_state(name, sweep, cuda_required, monkeypatch):
+    """Both sweeps that run these modes (resident for lattices that fit in
+    shared memory, the global-memory sweep for larger ones) keep exact V/I
+    and set acquisition MCS no later than the current MCS."""
     from cpm import _cpm
 
+    if sweep == "global":
+        monkeypatch.setenv("CPM_GPU_FORCE_GLOBAL", "1")
     model = MODELS[name]()
     eng = _cpm.Engine(model.builder(warn=False))
     eng.run_mcs(30 if model.D == 2 else 6)
