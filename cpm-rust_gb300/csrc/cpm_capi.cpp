@@ -84,7 +84,8 @@ extern "C" int cpm_builder_new(const uint64_t* grid, size_t grid_len, const char
                                const char* copy_neighborhood, const char* energy_neighborhood,
                                const char* connectivity_neighborhood, const char* acceptance, const char* proposal,
                                const char* const* keys, const int32_t* values, size_t n_keys, cpm_builder** out) {
-    if (!out || !boundary || !copy_neighborhood || !connectivity_neighborhood || (grid_len && !grid))
+    if (!out || !boundary || !copy_neighborhood || !connectivity_neighborhood || (grid_len && !grid) ||
+        (n_keys && (!keys || !values)))
         return fail(CPM_E_ARG, "null argument");
     auto b = std::make_unique<cpm_builder>();
     int e;
@@ -107,6 +108,7 @@ extern "C" int cpm_builder_new(const uint64_t* grid, size_t grid_len, const char
         else return fail(CPM_E_CONFIG, "unknown proposal mode " + dbg(proposal) + "; expected \"uniform\" or \"edge_list\"");
     }
     for (size_t i = 0; i < n_keys; ++i) {
+        if (!keys[i]) return fail(CPM_E_ARG, "null argument");
         const bool v = values[i] != 0;
         if (!std::strcmp(keys[i], "volume")) b->cfg.active.volume = v;
         else if (!std::strcmp(keys[i], "interface")) b->cfg.active.interface = v;
@@ -158,6 +160,9 @@ extern "C" int cpm_builder_add_cells(cpm_builder* b, const char* cell_type, uint
 
 extern "C" int cpm_builder_set_adhesion(cpm_builder* b, const double* values, const size_t* row_lengths, size_t n_rows) {
     if (!b || (n_rows && (!row_lengths))) return fail(CPM_E_ARG, "null argument");
+    size_t total = 0;
+    for (size_t r = 0; r < n_rows; ++r) total += row_lengths[r];
+    if (total && !values) return fail(CPM_E_ARG, "null argument");
     b->cfg.adhesion.assign(n_rows, {});
     size_t k = 0;
     for (size_t r = 0; r < n_rows; ++r) {
@@ -173,6 +178,7 @@ extern "C" int cpm_builder_initialize(cpm_builder* b, const uint32_t* lattice, s
     if (!b) return fail(CPM_E_ARG, "null argument");
     if (lattice) {
         if (!has_cto) return fail(CPM_E_CONFIG, "cell_type_of is required when lattice is supplied");
+        if (cto_len && !cell_type_of) return fail(CPM_E_ARG, "null argument");
         b->cfg.init_explicit = true;
         b->cfg.init_lattice.assign(lattice, lattice + lattice_len);
         b->cfg.init_type_of.assign(cell_type_of, cell_type_of + cto_len);
@@ -247,6 +253,7 @@ extern "C" int cpm_builder_run_batch(const cpm_builder* b, const double* thetas,
     int e = resolve(b, burn, readout, interval, c);
     if (e) return e;
     const size_t expected = theta_len(c.types.size());
+    if (n && expected && !thetas) return fail(CPM_E_ARG, "null argument");
     std::vector<std::vector<double>> th(n);
     size_t k = 0;
     for (size_t i = 0; i < n; ++i) {

@@ -6,7 +6,8 @@
 * derived seeds and the model hash reproduce the reference's known answers;
 * configuration errors surface as ValueError with the reference's messages
   (tests/python/test_errors.py:8-51) and theta has the canonical layout
-  (tests/python/test_batch.py:26-37).
+  (tests/python/test_batch.py:26-37);
+* the C ABI answers null buffers with CPM_E_ARG.
 """
 
 import ctypes
@@ -294,3 +295,49 @@ def test_samples_are_views_into_their_results_arrays():
     m = s0.contact
     assert m.shape == (4, 4) and m[0, 2] == 4 and m[1, 3] == 5 and m.sum() == 9
     assert s1.contact[0, 1] == 6 and s0.lattice is None
+
+
+def test_c_abi_rejects_null_pointers_with_an_argument_error():
+    """Host-only entry points return CPM_E_ARG ("null argument") for null
+    buffers whose sizes say they hold data, instead of reading them."""
+    from cpm import _cpm
+
+    lib = ctypes.CDLL(_cpm.LIB_PATH)
+    lib.cpm_last_error.restype = ctypes.c_char_p
+    E_ARG = 7  # CPM_E_ARG
+    P = ctypes.c_void_p
+    out = P()
+    grid = (ctypes.c_uint64 * 2)(10, 10)
+    new = lib.cpm_builder_new
+    new.argtypes = [P, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_uint64, ctypes.c_char_p, ctypes.c_char_p,
+                    ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, P, P, ctypes.c_size_t, P]
+    args = [ctypes.cast(grid, P), 2, b"periodic", 1, b"von_neumann", None, b"von_neumann", None, None]
+    # active-term keys announced but not passed
+    assert new(*args, None, None, 1, ctypes.byref(out)) == E_ARG
+    assert lib.cpm_last_error() == b"null argument"
+    assert new(*args, None, None, 0, ctypes.byref(out)) == 0
+    b = out
+    try:
+        lib.cpm_builder_set_adhesion.argtypes = [P, P, P, ctypes.c_size_t]
+        lens = (ctypes.c_size_t * 2)(2, 2)
+        assert lib.cpm_builder_set_adhesion(b, None, ctypes.cast(lens, P), 2) == E_ARG
+        assert lib.cpm_builder_set_adhesion(b, None, None, 2) == E_ARG
+        lib.cpm_builder_initialize.argtypes = [P, P, ctypes.c_size_t, P, ctypes.c_size_t, ctypes.c_int32,
+                                               ctypes.c_int32]
+        lat = (ctypes.c_uint32 * 100)()
+        assert lib.cpm_builder_initialize(b, ctypes.cast(lat, P), 100, None, 1, 1, 0) == E_ARG
+        lib.cpm_builder_register_cell_type.argtypes = [P, ctypes.c_char_p, ctypes.c_uint32, ctypes.c_uint32,
+                                                       ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                                       ctypes.c_uint32]
+        assert lib.cpm_builder_register_cell_type(b, b"a", 20, 20, 1.0, 1.0, 0.0, 0) == 0
+        adh = (ctypes.c_double * 4)(0, 1, 1, 0)
+        assert lib.cpm_builder_set_adhesion(b, ctypes.cast(adh, P), ctypes.cast(lens, P), 2) == 0
+        lib.cpm_builder_run_batch.argtypes = [P, P, P, ctypes.c_size_t, ctypes.c_uint64, ctypes.c_uint64,
+                                              ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int32, P, P]
+        tl = (ctypes.c_size_t * 1)(5)
+        res = (P * 1)()
+        assert lib.cpm_builder_run_batch(b, None, ctypes.cast(tl, P), 1, 1, 1, 1, 0, 0, None,
+                                         ctypes.cast(res, P)) == E_ARG
+    finally:
+        lib.cpm_builder_free.argtypes = [P]
+        lib.cpm_builder_free(b)
