@@ -304,6 +304,25 @@ def test_oracle_energy_matches_independent_count(case):
     assert pieces > 0  # the chain did visit disconnected shapes
 
 
+def test_hand_built_two_cell_energies():
+    """exact_boltzmann.rs:889-925: two diagonal singletons in opposite
+    corners, two face-adjacent singletons, a 2x2 block beside a 2x1 block;
+    the oracle's energy after placement equals the independent H."""
+    spec, p = _spec("two", "metropolis_hastings")
+    counter = Counter(4, 4, 2)
+    a = np.zeros((4, 4), np.uint32)
+    a[0, 0], a[3, 3] = 1, 2
+    b = np.zeros((4, 4), np.uint32)
+    b[1, 1], b[1, 2] = 1, 2
+    c = np.zeros((4, 4), np.uint32)
+    c[0:2, 0:2], c[0:2, 2] = 1, 2
+    for lat in (a, b, c):
+        sim = O.OracleSim(spec, 1)
+        sim.init_explicit(lat, [0, 1])
+        want = float(energy(counter, counter.keys_of(lat[None]), **p)[0])
+        assert abs(sim.energy - want) < 1e-9 and abs(sim.global_energy() - want) < 1e-9, (lat, sim.energy, want)
+
+
 def _disconnected(lat):
     """Some cell of the configuration has more than one von Neumann
     component."""
