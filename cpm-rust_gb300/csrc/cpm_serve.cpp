@@ -178,12 +178,29 @@ std::string Server::admit(Req& r) {
     const bool snapshots = r.ro.include_lattice || r.ro.topology;
     std::string e = r.dev->create({r.c}, {r.init}, {r.ns}, {r.ns + r.nt}, snapshots, r.stream);
     if (!e.empty()) return e;
-    r.times.device_bytes = r.dev->device_bytes();
-    if (r.ro.topology && r.ns > 0) r.times.device_bytes += topology_bytes(r.dev->layout(0).g.n_sites, r.dev->layout(0).n_cells);
+    size_t bytes = r.dev->device_bytes();
+    if (r.ro.topology && r.ns > 0) bytes += topology_bytes(r.dev->layout(0).g.n_sites, r.dev->layout(0).n_cells);
     e = r.dev->run({r.full});
     if (!e.empty()) return e;
+    // The accounting moves from the estimate to the arena's actual size
+    // before the hand-over is enqueued: from then on the pool may finish the
+    // request (and a caller take it) at any moment.
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        r.times.device_bytes = bytes;
+        st_.bytes_in_use += bytes;
+        st_.bytes_in_use -= r.est_bytes;
+        st_.peak_bytes = std::max(st_.peak_bytes, st_.bytes_in_use);
+        st_.launched++;
+    }
     ce = cudaLaunchHostFunc(r.stream, &Server::device_done, &r);
-    if (ce != cudaSuccess) return std::string("CUDA error: ") + cudaGetErrorString(ce);
+    if (ce != cudaSuccess) {
+        std::lock_guard<std::mutex> lk(mu_);
+        st_.bytes_in_use += r.est_bytes;
+        st_.bytes_in_use -= bytes;
+        st_.launched--;
+        return std::string("CUDA error: ") + cudaGetErrorString(ce);
+    }
     return "";
 }
 
@@ -267,29 +284,25 @@ void Server::scheduler_loop() {
         }
         for (Req* r : admitted) {
             const std::string e = admit(*r);
-            if (!e.empty()) {
-                // nothing of it runs any more: free it here
-                if (r->stream) cudaStreamSynchronize(r->stream);
-                release(*r);
-            }
+            // running: the device callback hands it to the pool, which may
+            // already have finished it and a caller taken (freed) it, so it
+            // is not touched here any more
+            if (e.empty()) continue;
+            // nothing of it runs any more (no hand-over was enqueued): free it here
+            if (r->stream) cudaStreamSynchronize(r->stream);
+            release(*r);
             std::lock_guard<std::mutex> lk(mu_);
             st_.bytes_in_use -= r->est_bytes;
-            if (!e.empty()) {
-                r->state = REQ_FAILED;
-                r->err = e;
-                r->times.finished = now();
-                st_.failed++;
-                active_--;
-                if (active_ == 0 && busy_since_ >= 0) {
-                    st_.busy_seconds += now() - busy_since_;
-                    busy_since_ = -1;
-                }
-                cv_done_.notify_all();
-            } else {
-                st_.bytes_in_use += r->times.device_bytes;
-                st_.peak_bytes = std::max(st_.peak_bytes, st_.bytes_in_use);
-                st_.launched++;
+            r->state = REQ_FAILED;
+            r->err = e;
+            r->times.finished = now();
+            st_.failed++;
+            active_--;
+            if (active_ == 0 && busy_since_ >= 0) {
+                st_.busy_seconds += now() - busy_since_;
+                busy_since_ = -1;
             }
+            cv_done_.notify_all();
         }
     }
 }
