@@ -41,6 +41,7 @@ size_t estimate_bytes(const Config& c, const Initial& init, int ns, int ne, bool
     size_t b = (size_t)g.n_padded * 4;
     b += n1 * (2 + 4 + 4 + 8 * D + 8 * D * D + 8);
     b += CPM_STAT_COUNT * 8 + t1 * t1 * 12 + nt * 24 + t1 * t1 * t1 * 12 + nt * tab * 32;
+    if (c.active.act) b += nt * 12 + (size_t)g.n_padded * 4;  // Act parameters and acquisition MCS
     b += (size_t)std::max(1, ne) * 8;
     b += (size_t)ns * n1 * (8 + 8 * D + 8 * D * D);
     if (snapshots) b += (size_t)ns * (size_t)g.n_sites * 4;
