@@ -1219,6 +1219,22 @@ void orc_set_modes(void* h, int acceptance, const double* lambda_act, const uint
 }
 void orc_set_local_halo(void* h, int on) { ((Sim*)h)->local_halo = on != 0; }
 void orc_set_check_topology(void* h, int on) { ((Sim*)h)->check_topology = on != 0; }
+// checker.rs:151-265: `n` single attempts with the brute-force check after
+// every accepted one. Returns the index of the first attempt after which the
+// check failed (its mismatch bits in *bad), or -1; *accepted counts accepts.
+int64_t orc_attempts_checked(void* h, uint64_t n, uint64_t* accepted, int* bad) {
+    Sim* s = (Sim*)h;
+    uint64_t acc = 0;
+    *bad = 0;
+    for (uint64_t a = 0; a < n; ++a) {
+        if (!s->attempt()) continue;
+        ++acc;
+        const int b = s->check(nullptr);
+        if (b) { *bad = b; *accepted = acc; return (int64_t)a; }
+    }
+    *accepted = acc;
+    return -1;
+}
 // Thinned chain samples (tests/exact_boltzmann.rs, single_cell_/two_cell_
 // harness): `burn_in` attempts, then per sample `thin` attempts followed by a
 // copy of the interior lattice (n_sites words) into out[i * n_sites].

@@ -112,6 +112,8 @@ def lib():
             L.orc_act_delta.restype = ctypes.c_double
             L.orc_set_local_halo.argtypes = [P, ctypes.c_int]
             L.orc_set_check_topology.argtypes = [P, ctypes.c_int]
+            L.orc_attempts_checked.argtypes = [P, ctypes.c_uint64, P, P]
+            L.orc_attempts_checked.restype = ctypes.c_int64
             L.orc_sample_attempts.argtypes = [P, ctypes.c_uint64, ctypes.c_int64, ctypes.c_uint64, P]
             L.orc_init_explicit.argtypes = [P, P, ctypes.c_int64, P, ctypes.c_int, ctypes.c_char_p, ctypes.c_int]
             L.orc_init_default.argtypes = [P, ctypes.c_char_p, ctypes.c_int]
@@ -247,6 +249,14 @@ class OracleSim:
         """Connectivity check of each attempt; off only for the exact-Boltzmann
         harness (tests/exact_boltzmann.rs calls attempt(cpm, false))."""
         lib().orc_set_check_topology(self.h, int(on))
+
+    def attempts_checked(self, n: int):
+        """`n` single attempts with the brute-force check after every accepted
+        one: (index of the first failing attempt or -1, mismatch bits,
+        accepted moves)."""
+        acc, bad = ctypes.c_uint64(0), ctypes.c_int(0)
+        first = lib().orc_attempts_checked(self.h, int(n), ctypes.byref(acc), ctypes.byref(bad))
+        return first, bad.value, acc.value
 
     def sample_attempts(self, burn_in: int, n_samples: int, thin: int) -> np.ndarray:
         """`burn_in` single attempts, then `n_samples` interior lattices, each

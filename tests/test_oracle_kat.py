@@ -10,7 +10,10 @@ the GB300 engine because these pass:
   crates/cpm-core/src/config.rs:423-556);
 * the simple-point tables against the slow reference checker
   (crates/cpm-core/src/simple_point.rs:514-628);
-* the brute-force recount after a run (crates/cpm-core/src/checker.rs:36-136).
+* the brute-force recount after a run (crates/cpm-core/src/checker.rs:36-136),
+  and after every accepted move in the checker's own scenarios: hand-placed
+  and scatter-and-grow 2D, 30^3, and with the Act term active
+  (crates/cpm-core/src/checker.rs:151-265).
 """
 
 import json
@@ -189,3 +192,67 @@ def test_local_halo_matches_full_refresh_after_default_init():
     b.run_mcs(50)
     assert np.array_equal(a.padded(), b.padded())
     assert bits(a.energy) == bits(b.energy)
+
+
+# checker.rs:326-432: 30x30 periodic, two types (V* 9, I* 20), five cells each
+CHECKER_TYPES = [(9, 20, 1.0, 0.2), (9, 20, 1.5, 0.3)]
+CHECKER_J = [[0.0, 3.0, 3.0], [3.0, 1.0, 5.0], [3.0, 5.0, 1.0]]
+
+
+def _checker_spec(act=None):
+    return O.ModelSpec((30, 30), True, CHECKER_TYPES, CHECKER_J, cell_counts=[5, 5], act=act)
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_checker_after_every_accept_hand_placed(seed):
+    """checker.rs:151-173: ten 3x3 blocks (origins (2|8|14|20|26, 2|15),
+    alternating types), 100,000 attempts, the brute-force check after every
+    accepted move."""
+    spec = _checker_spec()
+    spec.cell_counts = [0, 0]
+    sim = O.OracleSim(spec, seed)
+    lat = np.zeros((30, 30), np.uint32)
+    origins = [(2, 2), (8, 2), (14, 2), (20, 2), (26, 2), (2, 15), (8, 15), (14, 15), (20, 15), (26, 15)]
+    for i, (ox, oy) in enumerate(origins):
+        lat[ox:ox + 3, oy:oy + 3] = i + 1
+    sim.init_explicit(lat, [i % 2 for i in range(10)])
+    assert sim.check()[0] == 0
+    first, bad, acc = sim.attempts_checked(100_000)
+    assert first == -1, (first, bad)
+    assert acc > 100
+
+
+@pytest.mark.parametrize("seed", [10, 20, 30])
+def test_checker_after_every_accept_scatter_and_grow(seed):
+    """checker.rs:179-202: default placement, then 50,000 attempts checked
+    after every accept."""
+    sim = O.OracleSim(_checker_spec(), seed)
+    sim.init_default()
+    assert sim.check()[0] == 0
+    first, bad, acc = sim.attempts_checked(50_000)
+    assert first == -1, (first, bad)
+    assert acc > 100
+
+
+def test_checker_after_every_accept_3d():
+    """checker.rs:210-230: 30^3 periodic, five cells (V* 27, I* 90), 20,000
+    attempts checked after every accept."""
+    spec = O.ModelSpec((30, 30, 30), True, [(27, 90, 1.0, 0.2)], [[0.0, 3.0], [3.0, 1.0]], cell_counts=[5])
+    sim = O.OracleSim(spec, 1)
+    sim.set_local_halo(True)
+    sim.init_default()
+    assert sim.check()[0] == 0
+    first, bad, acc = sim.attempts_checked(20_000)
+    assert first == -1, (first, bad)
+    assert acc > 10
+
+
+@pytest.mark.parametrize("seed", [100, 200, 300])
+def test_checker_after_every_accept_with_act(seed):
+    """checker.rs:243-265: the Act term active (lambda_act 2 / 3, max_act
+    10 / 15) never reaches the conservative energy the checker recomputes."""
+    sim = O.OracleSim(_checker_spec(act=[(2.0, 10), (3.0, 15)]), seed)
+    sim.init_default()
+    first, bad, acc = sim.attempts_checked(50_000)
+    assert first == -1, (first, bad)
+    assert acc > 100
