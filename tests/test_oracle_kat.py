@@ -13,7 +13,9 @@ the GB300 engine because these pass:
 * the brute-force recount after a run (crates/cpm-core/src/checker.rs:36-136),
   and after every accepted move in the checker's own scenarios: hand-placed
   and scatter-and-grow 2D, 30^3, and with the Act term active
-  (crates/cpm-core/src/checker.rs:151-265).
+  (crates/cpm-core/src/checker.rs:151-265);
+* the connectivity unit cases (crates/cpm-core/src/connectivity.rs:72-123) and
+  the loop's properties (crates/cpm-core/src/monte_carlo.rs:485-528).
 """
 
 import json
@@ -256,3 +258,73 @@ def test_checker_after_every_accept_with_act(seed):
     first, bad, acc = sim.attempts_checked(50_000)
     assert first == -1, (first, bad)
     assert acc > 100
+
+
+def _connectivity_case(D, cells):
+    """A 5^D fixed lattice with cell 1 on `cells`; returns the oracle and a
+    function from a coordinate to its padded flat index."""
+    spec = O.ModelSpec((5,) * D, False, [(9, 20, 1.0, 0.2)], [[0.0, 3.0], [3.0, 1.0]], cell_counts=[0])
+    sim = O.OracleSim(spec, 1)
+    lat = np.zeros((5,) * D, np.uint32)
+    for c in cells:
+        lat[c] = 1
+    if cells:
+        sim.init_explicit(lat, [0])
+    st = sim.strides()
+    return sim, lambda c: int(sum((c[d] + 1) * st[d] for d in range(D)))
+
+
+def _topology_ok(sim, target_flat, k):
+    r = sim.evaluate_moves(np.array([target_flat], np.int64), np.array([k], np.int32), np.array([0.5]))
+    assert r["null_move"][0] == 0
+    return bool(r["topology_ok"][0])
+
+
+def test_connectivity_cases_of_the_reference():
+    """connectivity.rs:72-123, through the oracle's attempt evaluation:
+    copying medium into (2,2) of a cell made of (2,2), (2,1), (3,2) would pinch
+    it apart (rejected); a two-site cell (2,2), (2,1) may lose (2,2); the
+    medium losing a site is exempt, in 2D and (enclosed lumen) in 3D. The
+    copy direction k indexes the von Neumann stencil [+e0, -e0, +e1, -e1, ...]."""
+    sim, f = _connectivity_case(2, [(2, 2), (2, 1), (3, 2)])
+    assert not _topology_ok(sim, f((2, 2)), 1)  # source (1,2): medium
+    sim, f = _connectivity_case(2, [(2, 2), (2, 1)])
+    assert _topology_ok(sim, f((2, 2)), 1)
+    sim, f = _connectivity_case(2, [(2, 1)])
+    assert _topology_ok(sim, f((2, 2)), 3)  # medium at (2,2) takes cell 1 from (2,1)
+    ring = [(x, y, z) for x in (1, 2, 3) for y in (1, 2, 3) for z in (1, 2, 3) if (x, y, z) != (2, 2, 2)]
+    sim, f = _connectivity_case(3, ring)
+    assert _topology_ok(sim, f((2, 2, 2)), 0)  # the lumen site takes the ring's cell
+
+
+def _two_touching(seed):
+    """monte_carlo.rs:375-462: 30x30 periodic, two 3x3 cells side by side
+    (x 1..3 and 4..6, y 1..3), V* 15, I* 30."""
+    spec = O.ModelSpec((30, 30), True, [(15, 30, 1.0, 0.1), (15, 30, 1.0, 0.1)],
+                       [[0.0, 2.0, 2.0], [2.0, 1.0, 4.0], [2.0, 4.0, 1.0]], cell_counts=[0, 0])
+    sim = O.OracleSim(spec, seed)
+    lat = np.zeros((30, 30), np.uint32)
+    lat[1:4, 1:4], lat[4:7, 1:4] = 1, 2
+    sim.init_explicit(lat, [0, 1])
+    return sim
+
+
+def test_loop_properties_of_the_reference():
+    """monte_carlo.rs:485-528: run_mcs advances the MCS counter; the same
+    seed gives a bit-identical trajectory, different seeds diverge; no cell
+    goes below the minimum volume."""
+    a, b = _two_touching(42), _two_touching(42)
+    a.run_mcs(3)
+    assert a.mcs == 3
+    a.run_mcs(2)
+    b.run_mcs(5)
+    assert np.array_equal(a.lattice(), b.lattice())
+    assert np.array_equal(a.volume(), b.volume()) and np.array_equal(a.interface(), b.interface())
+    assert a.energy == b.energy
+    c, d = _two_touching(1), _two_touching(2)
+    c.run_mcs(10)
+    d.run_mcs(10)
+    assert not np.array_equal(c.volume(), d.volume())
+    e = _two_touching(7)
+    e.run_mcs(20)
+    assert e.volume().min() >= 1
