@@ -196,6 +196,23 @@ def test_wrong_length_theta_raises_a_clean_error():
         sim.run_batch([base, base[:-1]], burn_in_mcs=5, readout_mcs=5, sampling_interval_mcs=5, master_seed=1)
 
 
+@pytest.mark.parametrize("bad", [-1.0, float("nan"), float("inf"), 2.0 ** 33])
+def test_unrepresentable_max_act_in_theta_is_rejected(bad):
+    """theta.rs:93-117, 232-266: a Max_Act entry that does not round into
+    [0, u32::MAX] is rejected (not saturated), before any simulation runs."""
+    import cpm
+
+    sim = cpm.CPM(grid=(20, 20), boundary="periodic", seed=1)
+    sim.register_cell_type("a", 9, 20, 1.0, 0.2)
+    sim.add_cells("a", 2)
+    sim.set_adhesion([[0.0, 3.0], [3.0, 1.0]])
+    theta = list(sim.extract_theta())
+    theta[-1] = bad
+    with pytest.raises(ValueError, match=r"max_act\[a\] = .* does not round to a value representable as u32"):
+        sim.run_batch([sim.extract_theta(), theta], burn_in_mcs=5, readout_mcs=5, sampling_interval_mcs=5,
+                      master_seed=1)
+
+
 def test_cells_for_density_matches_reference_helper():
     import cpm
     from cpm.warnings import CPMLowResolutionWarning
