@@ -780,7 +780,7 @@ extern "C" int cpm_engine_write_state(cpm_engine* e, size_t i, const uint32_t* p
     if (sp) a.assign(sp, sp + n1 * D);
     if (so) b.assign(so, so + n1 * D * D);
     const std::string msg = e->sims.write_state(i, p, v, it, sp ? &a : nullptr, so ? &b : nullptr);
-    return msg.empty() ? ok() : fail(CPM_E_CUDA, msg);
+    return msg.empty() ? ok() : fail(msg.rfind("CUDA", 0) == 0 ? CPM_E_CUDA : CPM_E_ARG, msg);
 }
 
 extern "C" int cpm_engine_evaluate_moves(cpm_engine* e, size_t i, size_t n, const int64_t* target, const int32_t* k,

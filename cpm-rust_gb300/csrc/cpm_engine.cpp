@@ -887,6 +887,11 @@ std::string DeviceSims::write_state(size_t i, const std::vector<uint32_t>& padde
     const size_t n1 = layouts_[i].n_cells + 1;
     if (padded.size() != (size_t)layouts_[i].g.n_padded || vol.size() != n1 || itf.size() != n1)
         return "write_state: size mismatch";
+    // the sweeps index the per-cell arrays by the ids they read from sigma
+    for (size_t f = 0; f < padded.size(); ++f)
+        if (padded[f] > (uint32_t)layouts_[i].n_cells)
+            return "write_state: cell id " + std::to_string(padded[f]) + " at padded index " + std::to_string(f) +
+                   " exceeds the number of cells (" + std::to_string(layouts_[i].n_cells) + ")";
     CUDA_TRY(cudaMemcpy(descs_[i].sigma, padded.data(), padded.size() * 4, cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemcpy(descs_[i].volume, vol.data(), n1 * 4, cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemcpy(descs_[i].interface, itf.data(), n1 * 4, cudaMemcpyHostToDevice));

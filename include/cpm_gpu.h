@@ -260,7 +260,9 @@ int cpm_engine_take_sample(cpm_engine* e, size_t sim, int32_t include_lattice, c
 int cpm_engine_write_act_state(cpm_engine* e, size_t sim, const uint32_t* birth_padded, uint64_t mcs);
 int cpm_engine_read_birth(const cpm_engine* e, size_t sim, uint32_t* out /* n_padded */);
 /* Parity harness: overwrite the dynamic state, decide moves without
- * committing them, or apply moves in order with the sweep's commit. */
+ * committing them, or apply moves in order with the sweep's commit. Every
+ * padded entry written must be a cell id <= n_cells (CPM_E_ARG otherwise);
+ * targets must be interior sites and copy directions < 2 * dim. */
 int cpm_engine_write_state(cpm_engine* e, size_t sim, const uint32_t* padded, const uint32_t* volume,
                            const uint32_t* interface, const int64_t* sum_position, const int64_t* sum_position_outer);
 int cpm_engine_evaluate_moves(cpm_engine* e, size_t sim, size_t n, const int64_t* target_flat, const int32_t* k,
