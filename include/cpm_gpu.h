@@ -323,7 +323,8 @@ typedef struct {
     uint64_t seed;
     uint64_t mcs;                 /* MCS already performed */
     /* device pointers, caller-owned; per-cell arrays are indexed by id (n_cells + 1) */
-    uint32_t* sigma;              /* halo-padded lattice ((dims+2) per axis), halo consistent */
+    uint32_t* sigma;              /* halo-padded lattice ((dims+2) per axis), halo consistent,
+                                     every entry a cell id <= n_cells (not checked: device memory) */
     const uint16_t* type_plus_one;/* cell type + 1 per id, entry 0 = 0 (medium) */
     uint32_t* volume;
     uint32_t* interface;
