@@ -267,11 +267,13 @@ extern "C" int cpm_builder_run_batch(const cpm_builder* b, const double* thetas,
     ro.include_lattice = include_lattice != 0;
     ro.topology = true;
     std::vector<Result> rs;
-    const std::string msg = run_batch(c, th, master_seed, ro, rs);
+    BatchStage stage = BATCH_OK;
+    const std::string msg = run_batch(c, th, master_seed, ro, rs, &stage);
     if (!msg.empty()) {
-        int code = code_for(msg);
-        if (msg.find("must") != std::string::npos || msg.find("adhesion") != std::string::npos) code = CPM_E_CONFIG;
-        if (msg.rfind("max_act[", 0) == 0) code = CPM_E_THETA;
+        const int code = stage == BATCH_THETA    ? CPM_E_THETA
+                         : stage == BATCH_CONFIG ? CPM_E_CONFIG
+                         : stage == BATCH_INIT   ? CPM_E_INIT
+                                                 : code_for(msg);
         return fail(code, msg);
     }
     bool any = false;

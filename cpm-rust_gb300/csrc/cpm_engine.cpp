@@ -1241,32 +1241,46 @@ std::string run_one(const Config& c, const ReadoutOptions& ro, Result& out) {
 }
 
 std::string run_batch(const Config& base, const std::vector<std::vector<double>>& thetas, uint64_t master_seed,
-                      const ReadoutOptions& ro, std::vector<Result>& out) {
+                      const ReadoutOptions& ro, std::vector<Result>& out, BatchStage* stage) {
+    BatchStage dummy;
+    if (!stage) stage = &dummy;
+    *stage = BATCH_OK;
     const size_t expected = theta_len(base.types.size());
     for (size_t i = 0; i < thetas.size(); ++i)
-        if (thetas[i].size() != expected)
+        if (thetas[i].size() != expected) {
+            *stage = BATCH_THETA;
             return "theta at index " + std::to_string(i) + " has length " + std::to_string(thetas[i].size()) +
                    ", expected " + std::to_string(expected);
+        }
     std::vector<Config> cfgs(thetas.size(), base);
     std::vector<Initial> inits(thetas.size());
     std::vector<std::string> errs(thetas.size());
+    std::vector<BatchStage> stages(thetas.size(), BATCH_OK);
     std::atomic<size_t> next{0};
     auto worker = [&]() {
         for (;;) {
             const size_t i = next.fetch_add(1);
             if (i >= thetas.size()) return;
             std::string e = theta_inject(cfgs[i], thetas[i].data());
-            if (e.empty()) { cfgs[i].seed = derive_seed_u64(master_seed, i); e = validate(cfgs[i]); }
-            if (e.empty()) e = initialize(cfgs[i], inits[i]);
+            BatchStage at = BATCH_THETA;
+            if (e.empty()) { cfgs[i].seed = derive_seed_u64(master_seed, i); e = validate(cfgs[i]); at = BATCH_CONFIG; }
+            if (e.empty()) { e = initialize(cfgs[i], inits[i]); at = BATCH_INIT; }
             errs[i] = e;
+            if (!e.empty()) stages[i] = at;
         }
     };
     const unsigned nthreads = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), (unsigned)std::max<size_t>(thetas.size(), 1)));
     std::vector<std::thread> th;
     for (unsigned t = 0; t < nthreads; ++t) th.emplace_back(worker);
     for (auto& t : th) t.join();
-    for (auto& e : errs) if (!e.empty()) return e;
-    return run_many(cfgs, inits, ro, out);
+    for (size_t i = 0; i < errs.size(); ++i)
+        if (!errs[i].empty()) {
+            *stage = stages[i];
+            return errs[i];
+        }
+    std::string e = run_many(cfgs, inits, ro, out);
+    if (!e.empty()) *stage = BATCH_RUN;
+    return e;
 }
 
 }  // namespace cpmhost

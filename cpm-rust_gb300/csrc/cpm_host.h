@@ -163,9 +163,13 @@ std::string run_many(const std::vector<Config>& configs, const std::vector<Initi
 
 // The drop-in `run` (builder.rs:432-474 + output.rs:434-529).
 std::string run_one(const Config& c, const ReadoutOptions& ro, Result& out);
-// The drop-in `run_batch` (batch.rs:110-153).
+// The drop-in `run_batch` (batch.rs:110-153). On failure `stage` names the
+// step that failed: BATCH_THETA (length or injection), BATCH_CONFIG
+// (validation of an injected configuration), BATCH_INIT (placement) or
+// BATCH_RUN (the device run).
+enum BatchStage { BATCH_OK = 0, BATCH_THETA, BATCH_CONFIG, BATCH_INIT, BATCH_RUN };
 std::string run_batch(const Config& base, const std::vector<std::vector<double>>& thetas, uint64_t master_seed,
-                      const ReadoutOptions& ro, std::vector<Result>& out);
+                      const ReadoutOptions& ro, std::vector<Result>& out, BatchStage* stage = nullptr);
 
 std::string last_cuda_error();
 // Sets the message cpm_last_error() reports on this thread.

@@ -213,6 +213,25 @@ def test_unrepresentable_max_act_in_theta_is_rejected(bad):
                       master_seed=1)
 
 
+@pytest.mark.parametrize("index, value, message", [
+    (0, -1.0, "lambda_volume must be finite and non-negative, got -1"),
+    (2, float("nan"), r"adhesion\[0\]\[0\] = NaN is not finite"),
+])
+def test_theta_that_fails_validation_is_a_value_error(index, value, message):
+    """batch.rs:126-135: an injected theta goes through the same validation as
+    a configuration (CPM::new), before any simulation runs."""
+    import cpm
+
+    sim = cpm.CPM(grid=(20, 20), boundary="periodic", seed=1)
+    sim.register_cell_type("a", 9, 20, 1.0, 0.2)
+    sim.add_cells("a", 2)
+    sim.set_adhesion([[0.0, 3.0], [3.0, 1.0]])
+    theta = list(sim.extract_theta())
+    theta[index] = value
+    with pytest.raises(ValueError, match=message):
+        sim.run_batch([theta], burn_in_mcs=5, readout_mcs=5, sampling_interval_mcs=5, master_seed=1)
+
+
 def test_cells_for_density_matches_reference_helper():
     import cpm
     from cpm.warnings import CPMLowResolutionWarning
