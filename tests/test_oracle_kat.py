@@ -15,7 +15,10 @@ the GB300 engine because these pass:
   and scatter-and-grow 2D, 30^3, and with the Act term active
   (crates/cpm-core/src/checker.rs:151-265);
 * the connectivity unit cases (crates/cpm-core/src/connectivity.rs:72-123) and
-  the loop's properties (crates/cpm-core/src/monte_carlo.rs:485-528).
+  the loop's properties (crates/cpm-core/src/monte_carlo.rs:485-528);
+* the calibrated target interfaces (crates/cpm-core/tests/calibration.rs),
+  reproduced to the printed decimals: a second frozen trajectory, 60x60
+  fixed, 40,000 MCS.
 """
 
 import json
@@ -328,3 +331,50 @@ def test_loop_properties_of_the_reference():
     e = _two_touching(7)
     e.run_mcs(20)
     assert e.volume().min() >= 1
+
+
+def _calibration_relaxation(target_volume, j_medium):
+    """tests/calibration.rs:26-92: one cell on a 60x60 fixed lattice, seeded as
+    a compact blob (rows, then columns, from (30 - side/2, 30 - side/2) with
+    side = ceil(sqrt(V*)) + 1), lambda_V 5, no interface term, J(cell,
+    medium) given; 20,000 MCS of burn-in, then the interface every 10 MCS
+    for 2,000 samples. Returns their mean."""
+    grid = 60
+    spec = O.ModelSpec((grid, grid), False, [(target_volume, 0, 5.0, 0.0)], [[0.0, j_medium], [j_medium, 0.0]],
+                       cell_counts=[0])
+    sim = O.OracleSim(spec, 1)
+    side = int(np.ceil(np.sqrt(target_volume))) + 1
+    origin = grid // 2 - side // 2
+    lat = np.zeros((grid, grid), np.uint32)
+    placed = 0
+    for r in range(origin, origin + side):
+        for c in range(origin, origin + side):
+            if placed < target_volume:
+                lat[r, c] = 1
+                placed += 1
+    sim.init_explicit(lat, [0])
+    sim.run_mcs(20_000)
+    values = []
+    for _ in range(2_000):
+        sim.run_mcs(10)
+        values.append(float(sim.interface()[0]))
+    return float(np.mean(values))
+
+
+def test_calibrated_target_interfaces():
+    """tests/calibration.rs:118-131: the relaxed interface of the two
+    calibrated cell types lands within 5 calibration standard deviations of
+    the published values (epithelial V* 50, J 5: 74.753 +/- 0.973; stem V*
+    40, J 6: 66.097 +/- 0.430; config.rs:588-595). The oracle reproduces both
+    published means to all three printed decimals: the same seed gives the
+    reference's own 40,000-MCS trajectory, so this is a second frozen
+    trajectory, in the fixed boundary the first one does not cover."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    O.lib()
+    cases = [(50, 5.0, 74.753, 0.973), (40, 6.0, 66.097, 0.430)]
+    with ThreadPoolExecutor(2) as ex:
+        means = list(ex.map(lambda c: _calibration_relaxation(c[0], c[1]), cases))
+    for (v, j, want, std), got in zip(cases, means):
+        assert abs(got - want) < 5.0 * std, (v, j, got, want)
+        assert abs(got - want) < 5e-4, (v, j, got, want)
