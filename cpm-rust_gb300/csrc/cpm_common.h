@@ -103,7 +103,10 @@ struct SimDesc {
     const float* dj32;
     const float* J32;
     int32_t tab_n;
-    int32_t pad1;
+    // Test switch (the reference's `attempt(cpm, false)` of its exact-Boltzmann
+    // harness): nonzero skips the connectivity check; honoured by the
+    // global-memory sweep only, and the engine routes such simulations there.
+    int32_t no_connectivity;
     // ---- state ----
     int32_t n_cells;
     int32_t pad0;

@@ -119,6 +119,9 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
     // Selects the tiled sweep wherever it applies (tests use it on lattices
     // small enough for the resident sweep).
     force_tiled_ = std::getenv("CPM_GPU_FORCE_TILED") != nullptr;
+    // Skips the connectivity check of every attempt, on the global-memory
+    // sweep (the exact-Boltzmann test; never set in production).
+    no_connectivity_ = std::getenv("CPM_GPU_TEST_NO_CONNECTIVITY") != nullptr;
     prefer_tiled_ = std::getenv("CPM_GPU_PREFER_TILED") != nullptr;
     const size_t N = configs.size();
     layouts_.resize(N);
@@ -295,6 +298,7 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
         }
         s.n_sites = L.g.n_sites;
         s.n_padded = L.g.n_padded;
+        s.no_connectivity = no_connectivity_ ? 1 : 0;
         s.n_colors = 1;
         s.max_class = 1;
         for (int d = 0; d < 3; ++d) {
@@ -396,7 +400,7 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
 
 DeviceSims::Path DeviceSims::path(size_t i) const {
     const SimLayout& L = layouts_[i];
-    if (force_global_) return GLOBAL;
+    if (force_global_ || no_connectivity_) return GLOBAL;
     // Metropolis-Hastings acceptance and the Act term run on the resident
     // sweep when the lattice fits, else on the global sweep (not tiled)
     const bool modes = descs_[i].acceptance || descs_[i].act;

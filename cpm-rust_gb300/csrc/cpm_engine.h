@@ -119,6 +119,7 @@ class DeviceSims {
     cudaStream_t stream_ = 0;
     bool force_global_ = false;
     bool force_tiled_ = false;
+    bool no_connectivity_ = false;
     bool prefer_tiled_ = false;
     void* d_bar_ = nullptr;
     uint32_t* d_reg_ = nullptr;  // tiled sweep: per-CTA cell registries

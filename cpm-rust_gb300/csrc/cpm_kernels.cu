@@ -176,7 +176,10 @@ __device__ void color_pass(const SimDesc& s, const PassInfo& p, uint64_t mcs, ui
             ct.attempts++;
             if (L == G) continue;  // early-out (monte_carlo.rs:60-64)
             ct.nonnull++;
-            if (!preserves_topology<D, uint32_t>(s, sig, t, L, s.table2d, t3)) { ct.topo_reject++; continue; }
+            if (!s.no_connectivity && !preserves_topology<D, uint32_t>(s, sig, t, L, s.table2d, t3)) {
+                ct.topo_reject++;
+                continue;
+            }
             pend |= 1ull << i;
             kb0 |= (unsigned long long)(k & 1) << i;
             kb1 |= (unsigned long long)((k >> 1) & 1) << i;
