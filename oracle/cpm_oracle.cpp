@@ -1,20 +1,26 @@
 // CPU restatement of the DebajyotiS/cpm-rust `cpm-core` hot path.
 //
 // TEST INFRASTRUCTURE ONLY. This file is the correctness oracle for the
-// GB300 engine: it is imported by `tests/`, by `__graft_entry__.smoke()` as a
-// checker, and by `bench.py` for the timed CPU baseline (and the
-// `--impl reference` arm). The product path never links or calls it.
+// GB300 engine: it is imported by `tests/`, by `__graft_entry__.smoke()` to
+// compare one small device run against, and by `bench.py` for the timed CPU
+// baseline (and the `--impl reference` arm). The product path never links or
+// calls it.
 //
 // Parity status: pinned. The restatement reproduces the reference's frozen
 // 2D trajectory bit for bit (crates/cpm-core/tests/dimension_consistency.rs:
 // 113-131: V=[7,9], I=[28,32], energy bits 4638468362461406824, model_hash
 // 60ec713d...) and the published derived seeds for master_seed=42
-// (notebooks/batch_execution_demo.ipynb, cell 7). `tests/test_oracle_kat.py`
-// checks both. The loop's other modes (Metropolis-Hastings acceptance,
-// monte_carlo.rs:168-224; the Act term, energy.rs:329-471) have no frozen
-// trajectory in the reference; the Act term is pinned against the scenarios
-// of the reference's own unit tests (energy.rs:955-1300) and the MH decision
-// against its formula (`tests/test_oracle_modes.py`).
+// (notebooks/batch_execution_demo.ipynb, cell 7), and the calibrated target
+// interfaces 74.753 / 66.097 to all printed decimals (tests/calibration.rs,
+// config.rs:588-595: one cell on a 60x60 fixed lattice, 40,000 MCS, a second
+// frozen trajectory). `tests/test_oracle_kat.py` checks them. The loop's
+// other modes (Metropolis-Hastings acceptance, monte_carlo.rs:168-224; the
+// Act term, energy.rs:329-471) have no frozen trajectory in the reference;
+// the Act term is pinned against the scenarios of the reference's own unit
+// tests (energy.rs:955-1300), the MH decision against its formula
+// (`tests/test_oracle_modes.py`), and the MH chain against the exact
+// Boltzmann distribution of the reference's harness
+// (tests/exact_boltzmann.rs; `tests/test_oracle_boltzmann.py`).
 //
 // Every function cites the reference file:line it restates. The third-party
 // arithmetic the reference pulls from crates that are not vendored in the

@@ -1,13 +1,15 @@
 """ctypes wrapper over the CPU oracle (``oracle/cpm_oracle.cpp``).
 
-TEST INFRASTRUCTURE ONLY: the oracle is the checker the GB300 engine is
-compared against. Only ``tests/``, ``__graft_entry__.smoke()`` and
+TEST INFRASTRUCTURE ONLY: the oracle is what the GB300 engine is compared
+against. Only ``tests/``, ``__graft_entry__.smoke()`` and
 ``bench.py`` (its CPU-baseline leg and ``--impl reference`` arm) may load it;
 the ``cpm`` package never does.
 
 The oracle restates DebajyotiS/cpm-rust ``cpm-core`` (see the C++ file header
 for the per-function citations) and is pinned by the reference's frozen
-trajectory and derived-seed vectors (``tests/test_oracle_kat.py``).
+trajectory, its calibrated target interfaces (a second trajectory, fixed
+boundary) and derived-seed vectors (``tests/test_oracle_kat.py``), and by
+the exact-Boltzmann harness (``tests/test_oracle_boltzmann.py``).
 """
 
 from __future__ import annotations
