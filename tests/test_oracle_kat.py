@@ -1,7 +1,7 @@
 """Pins the CPU oracle against the reference's own known answers.
 
-Runs on the CPU (no GPU marker). The oracle is only trusted as the checker for
-the GB300 engine because these pass:
+Runs on the CPU (no GPU marker). The oracle is only trusted as the reference
+the GB300 engine is compared against because these pass:
 
 * the frozen 2D trajectory (crates/cpm-core/tests/dimension_consistency.rs:113-131),
   with both the reference's whole-halo refresh and the local refresh;
@@ -200,12 +200,12 @@ def test_local_halo_matches_full_refresh_after_default_init():
 
 
 # checker.rs:326-432: 30x30 periodic, two types (V* 9, I* 20), five cells each
-CHECKER_TYPES = [(9, 20, 1.0, 0.2), (9, 20, 1.5, 0.3)]
-CHECKER_J = [[0.0, 3.0, 3.0], [3.0, 1.0, 5.0], [3.0, 5.0, 1.0]]
+RECOUNT_TYPES = [(9, 20, 1.0, 0.2), (9, 20, 1.5, 0.3)]
+RECOUNT_J = [[0.0, 3.0, 3.0], [3.0, 1.0, 5.0], [3.0, 5.0, 1.0]]
 
 
 def _checker_spec(act=None):
-    return O.ModelSpec((30, 30), True, CHECKER_TYPES, CHECKER_J, cell_counts=[5, 5], act=act)
+    return O.ModelSpec((30, 30), True, RECOUNT_TYPES, RECOUNT_J, cell_counts=[5, 5], act=act)
 
 
 @pytest.mark.parametrize("seed", [1, 2, 3])
@@ -255,7 +255,8 @@ def test_checker_after_every_accept_3d():
 @pytest.mark.parametrize("seed", [100, 200, 300])
 def test_checker_after_every_accept_with_act(seed):
     """checker.rs:243-265: the Act term active (lambda_act 2 / 3, max_act
-    10 / 15) never reaches the conservative energy the checker recomputes."""
+    10 / 15) never reaches the conservative energy the brute-force recount
+    recomputes."""
     sim = O.OracleSim(_checker_spec(act=[(2.0, 10), (3.0, 15)]), seed)
     sim.init_default()
     first, bad, acc = sim.attempts_checked(50_000)
