@@ -344,11 +344,14 @@ struct FastChecker {
         return touching == 1;
     }
 };
+// Built once per process on first use; function-local statics initialise
+// thread-safely, so simulations on several host threads may race to it.
 static FastChecker& checker(int D) {
-    static FastChecker c2, c3;
-    static bool done2 = false, done3 = false;
-    if (D == 2) { if (!done2) { c2.init(2); done2 = true; } return c2; }
-    if (!done3) { c3.init(3); done3 = true; }
+    if (D == 2) {
+        static FastChecker c2 = [] { FastChecker c; c.init(2); return c; }();
+        return c2;
+    }
+    static FastChecker c3 = [] { FastChecker c; c.init(3); return c; }();
     return c3;
 }
 
