@@ -134,6 +134,10 @@ struct Placer {
     Geometry g;
     std::vector<uint32_t> lat;  // padded; only interior entries are meaningful
     std::vector<int64_t> copy_off;
+    // canon[f]: f for an interior site; for a halo site its periodic image
+    // (periodic) or -1 (fixed: not a site). One lookup replaces the per-axis
+    // divisions of `interior` / `wrapped` on the growth path.
+    std::vector<int32_t> canon;
     explicit Placer(const Config& cfg) : c(cfg) {
         g.init(cfg);
         lat.assign((size_t)g.n_padded, 0);
@@ -142,34 +146,29 @@ struct Placer {
             for (int a = 0; a < cfg.D; ++a) d += o[a] * g.strides[a];
             copy_off.push_back(d);
         }
-    }
-    bool interior(int64_t f) const {
-        for (int d = 0; d < g.D; ++d) {
-            const int64_t q = f / g.strides[d];
-            f %= g.strides[d];
-            if (q == 0 || q == g.pdims[d] - 1) return false;
+        canon.resize((size_t)g.n_padded);
+        int64_t pc[3] = {0, 0, 0};
+        for (int64_t f = 0; f < g.n_padded; ++f) {
+            bool halo = false;
+            int64_t ic[3] = {0, 0, 0};
+            for (int d = 0; d < g.D; ++d) {
+                if (pc[d] == 0 || pc[d] == g.pdims[d] - 1) halo = true;
+                ic[d] = pc[d] == 0 ? g.dims[d] - 1 : (pc[d] == g.pdims[d] - 1 ? 0 : pc[d] - 1);
+            }
+            canon[f] = !halo ? (int32_t)f : (g.periodic ? (int32_t)g.flat(ic) : -1);
+            for (int d = g.D - 1; d >= 0; --d) { if (++pc[d] < g.pdims[d]) break; pc[d] = 0; }
         }
-        return true;
-    }
-    int64_t wrapped(int64_t f) const {
-        int64_t ic[3] = {0, 0, 0};
-        for (int d = 0; d < g.D; ++d) {
-            const int64_t q = f / g.strides[d];
-            f %= g.strides[d];
-            ic[d] = q == 0 ? g.dims[d] - 1 : (q == g.pdims[d] - 1 ? 0 : q - 1);
-        }
-        return g.flat(ic);
     }
     // initialization.rs:173-187 / 303-318
     int64_t canonical(int64_t f, int64_t off) const {
         const int64_t nb = f + off;
-        if (interior(nb) || !g.periodic) return nb;
-        return wrapped(nb);
+        return g.periodic ? canon[nb] : nb;
     }
     bool growable(int64_t f, int64_t off, int64_t& out) const {
-        const int64_t raw = f + off;
-        if (interior(raw) || g.periodic) { out = canonical(f, off); return true; }
-        return false;
+        const int32_t c2 = canon[f + off];
+        if (c2 < 0) return false;
+        out = c2;
+        return true;
     }
     double distance(const int64_t* a, const int64_t* b) const {
         double s = 0.0;
