@@ -625,14 +625,14 @@ class CPM:
         """Host-only placement (no device work): (lattice, cell_type_of, used_default)."""
         n_sites = int(np.prod(self._grid))
         lat = np.zeros(n_sites, dtype=np.uint32)
-        n = ctypes.c_size_t(0)
+        # every cell holds at least one site, so n_sites bounds the cell count:
+        # one placement fills both buffers
+        cto = np.zeros(max(n_sites, 1), dtype=np.uint32)
+        n = ctypes.c_size_t(cto.size)
         used = ctypes.c_int32(0)
-        _check(_lib.cpm_builder_initial_state(self._h, _ptr(lat), n_sites, None, ctypes.byref(n), ctypes.byref(used)))
-        cap = ctypes.c_size_t(n.value)
-        cto = np.zeros(max(n.value, 1), dtype=np.uint32)
-        _check(_lib.cpm_builder_initial_state(self._h, _ptr(lat), n_sites, _ptr(cto), ctypes.byref(cap),
+        _check(_lib.cpm_builder_initial_state(self._h, _ptr(lat), n_sites, _ptr(cto), ctypes.byref(n),
                                               ctypes.byref(used)))
-        return lat.reshape(self._grid), cto[: n.value], bool(used.value)
+        return lat.reshape(self._grid), cto[: n.value].copy(), bool(used.value)
 
     def hashes(self, burn_in_mcs, readout_mcs, sampling_interval_mcs, lattice, cell_type_of):
         """(convention_hash, model_hash) for the given windows and lattice."""
