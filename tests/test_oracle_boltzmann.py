@@ -381,3 +381,19 @@ def test_plain_metropolis_fails_the_exact_check():
     chi2, df, _, _ = chi_squared(h, g, energy(counter, counter.keys_of(lats), **p))
     print(f"plain Metropolis: chi2 {chi2:.1f} df {df}")
     assert chi2 > 8.0 * df, (chi2, df)
+
+
+def test_two_cell_chain_survives_very_stiff_parameters():
+    """exact_boltzmann.rs:764-794: at four times the two-cell coefficients the
+    chain is trapped (too few bins for chi-squared), but 500,000 attempts keep
+    both cells at volume >= 1 and a finite energy."""
+    spec, p = _spec("two@4.0", "metropolis_hastings")
+    sim = O.OracleSim(spec, 2)
+    lat = _start("two")
+    sim.init_explicit(lat, [0, 1])
+    sim.set_check_topology(False)
+    last = sim.sample_attempts(500_000, 1, 0)
+    assert sim.volume().min() >= 1
+    counter = Counter(4, 4, 2)
+    h = energy(counter, counter.keys_of(last), **p)
+    assert np.all(np.isfinite(h)) and np.isfinite(sim.energy)
