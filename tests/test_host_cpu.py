@@ -377,3 +377,25 @@ def test_c_abi_rejects_null_pointers_with_an_argument_error():
     finally:
         lib.cpm_builder_free.argtypes = [P]
         lib.cpm_builder_free(b)
+
+
+def test_c99_client_compiles_links_and_runs(tmp_path):
+    """include/cpm_gpu.h is a C99 header and the library serves a plain C
+    caller: builder calls, the reference's duplicate-type error text, theta
+    length and the published derived seed for (42, 0)."""
+    import shutil
+    import subprocess
+
+    from cpm import _cpm
+
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    root = _cpm.__file__.replace("cpm-rust_gb300/python/cpm/_cpm.py", "")
+    libdir = root + "cpm-rust_gb300/lib"
+    exe = str(tmp_path / "c_abi_client")
+    subprocess.run([gcc, "-std=c99", "-Wall", "-Werror", "-I", root + "include", root + "tests/c_abi_client.c",
+                    "-L", libdir, "-lcpm_gpu", "-Wl,-rpath," + libdir, "-o", exe], check=True)
+    out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout
+    assert 'cell type "a" has already been added' in out
+    assert "seed=6806512004122731638" in out
