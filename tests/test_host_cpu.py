@@ -232,6 +232,23 @@ def test_theta_that_fails_validation_is_a_value_error(index, value, message):
         sim.run_batch([theta], burn_in_mcs=5, readout_mcs=5, sampling_interval_mcs=5, master_seed=1)
 
 
+def test_warning_classes_are_user_warnings():
+    """tests/python/test_warnings.py:8-22: both warning classes are
+    UserWarnings, raisable, catchable and silenced by a filter."""
+    import cpm
+    from cpm.warnings import CPMInitializationWarning, CPMLowResolutionWarning
+
+    assert cpm.CPMInitializationWarning is CPMInitializationWarning
+    for cls in (CPMInitializationWarning, CPMLowResolutionWarning):
+        assert issubclass(cls, UserWarning)
+        with pytest.warns(cls):
+            warnings.warn("x", cls, stacklevel=2)
+        with warnings.catch_warnings(record=True) as caught:
+            warnings.simplefilter("ignore", cls)
+            warnings.warn("x", cls, stacklevel=2)
+        assert not caught
+
+
 def test_cells_for_density_matches_reference_helper():
     import cpm
     from cpm.warnings import CPMLowResolutionWarning
@@ -243,7 +260,7 @@ def test_cells_for_density_matches_reference_helper():
     with warnings.catch_warnings():
         warnings.simplefilter("error", CPMLowResolutionWarning)
         cpm.cells_for_density(grid=(64, 64), target_volume=1000, phi=0.8)
-    # the survey's config sizes
+    # the cell counts of the 512x512 sorting and 128^3 organoid workloads
     assert cpm.cells_for_density((512, 512), 50, 0.2) == 1049
     assert cpm.cells_for_density((128, 128, 128), 1048, 0.8 / 3) == 534
 
