@@ -925,6 +925,43 @@ extern "C" int cpm_builder_hashes(const cpm_builder* b, uint64_t burn, uint64_t 
 
 extern "C" uint64_t cpm_derive_seed_u64(uint64_t master, uint64_t index) { return derive_seed_u64(master, index); }
 
+extern "C" int cpm_run_status(const double* energy_trace, size_t n_trace, size_t n_samples, const uint64_t* sample_mcs,
+                              uint32_t n_cells, const uint32_t* volumes, const uint32_t* first_fragmented,
+                              const uint32_t* last_contact_pairs, size_t n_pairs, uint32_t min_cell_volume,
+                              int32_t* kind, uint32_t* cell_id, uint64_t* at_mcs) {
+    if (!kind || !cell_id || !at_mcs || (n_trace && !energy_trace) || (n_samples && (!sample_mcs || !volumes)) ||
+        (n_pairs && !last_contact_pairs))
+        return fail(CPM_E_ARG, "null argument");
+    const bool topo = first_fragmented != nullptr;
+    std::vector<Sample> samples(n_samples);
+    for (size_t k = 0; k < n_samples; ++k) {
+        Sample& s = samples[k];
+        s.mcs = sample_mcs[k];
+        s.cells.resize(n_cells);
+        for (uint32_t i = 0; i < n_cells; ++i) {
+            s.cells[i] = CellSample();
+            s.cells[i].id = i + 1;
+            s.cells[i].volume = volumes[k * n_cells + i];
+        }
+        if (topo && first_fragmented[k]) s.fragmented.push_back(first_fragmented[k]);
+        if (k + 1 == n_samples)
+            for (size_t q = 0; q < n_pairs; ++q) {
+                s.contact_a.push_back(last_contact_pairs[2 * q]);
+                s.contact_b.push_back(last_contact_pairs[2 * q + 1]);
+                s.contact_n.push_back(1);
+            }
+    }
+    const Status st = run_status(min_cell_volume, std::vector<double>(energy_trace, energy_trace + n_trace), samples,
+                                 (int)n_cells, topo);
+    static const char* kinds[] = {"Ok", "NotEquilibrated", "Fragmented", "CellLost", "Degenerate"};
+    *kind = 0;
+    for (int q = 0; q < 5; ++q)
+        if (st.kind == kinds[q]) *kind = q;
+    *cell_id = st.has_cell ? st.cell_id : 0;
+    *at_mcs = st.has_cell ? st.at_mcs : 0;
+    return ok();
+}
+
 // ------------------------------------------------------------ serving ----
 struct cpm_server {
     Server s;

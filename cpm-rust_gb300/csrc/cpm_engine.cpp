@@ -974,8 +974,8 @@ static bool not_equilibrated(const std::vector<double>& y) {
 }
 
 // output.rs:456-522 (priority NotEquilibrated > Fragmented > CellLost > Degenerate)
-static Status status_of(const Config& c, const std::vector<double>& trace, const std::vector<Sample>& samples,
-                        int n_cells, bool have_topology) {
+Status run_status(uint32_t min_cell_volume, const std::vector<double>& trace, const std::vector<Sample>& samples,
+                  int n_cells, bool have_topology) {
     Status st;
     if (not_equilibrated(trace)) { st.kind = "NotEquilibrated"; return st; }
     if (have_topology)
@@ -991,7 +991,7 @@ static Status status_of(const Config& c, const std::vector<double>& trace, const
         for (int id = 1; id <= n_cells; ++id) {
             bool all = true;
             for (size_t k = start; k < samples.size(); ++k)
-                if (!(samples[k].cells[id - 1].volume <= c.min_cell_volume)) { all = false; break; }
+                if (!(samples[k].cells[id - 1].volume <= min_cell_volume)) { all = false; break; }
             if (all) {
                 st.kind = "CellLost"; st.has_cell = true; st.cell_id = (uint32_t)id; st.at_mcs = samples[start].mcs;
                 return st;
@@ -1024,6 +1024,11 @@ static Status status_of(const Config& c, const std::vector<double>& trace, const
         }
     }
     return st;
+}
+
+static Status status_of(const Config& c, const std::vector<double>& trace, const std::vector<Sample>& samples,
+                        int n_cells, bool have_topology) {
+    return run_status(c.min_cell_volume, trace, samples, n_cells, have_topology);
 }
 
 // Number of energy-trace points the burn-in loop records (output.rs:441-454).

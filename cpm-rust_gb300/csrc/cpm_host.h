@@ -149,6 +149,12 @@ struct Result {
     std::vector<double> energy_trace;  // burn-in energy trace (the status reads it)
 };
 
+// The run status (output.rs:456-522) from the burn-in energy trace and the
+// readout samples (per-cell volumes by id, fragmented ids, the last
+// sample's contact pairs); topology-based kinds only with `have_topology`.
+Status run_status(uint32_t min_cell_volume, const std::vector<double>& trace, const std::vector<Sample>& samples,
+                  int n_cells, bool have_topology);
+
 // Readout knobs: what each sample carries besides the per-cell summary.
 struct ReadoutOptions {
     bool include_lattice = false;  // Sample.lattice

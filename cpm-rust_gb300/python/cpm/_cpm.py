@@ -168,7 +168,7 @@ EXPORTED_SYMBOLS = (
     "cpm_engine_evaluate_moves", "cpm_engine_commit_moves", "cpm_engine_take_sample", "cpm_engine_write_act_state",
     "cpm_engine_read_birth", "cpm_engine_destroy",
     "cpm_run_many",
-    "cpm_builder_initial_state", "cpm_builder_hashes", "cpm_derive_seed_u64",
+    "cpm_builder_initial_state", "cpm_builder_hashes", "cpm_derive_seed_u64", "cpm_run_status",
     "cpm_run_mcs_noalloc",
     "cpm_serve_start", "cpm_serve_submit", "cpm_serve_poll", "cpm_serve_wait", "cpm_serve_cancel",
     "cpm_serve_stats_get", "cpm_serve_stop", "cpm_result_samples_sizes", "cpm_result_samples_read",
@@ -235,6 +235,7 @@ def _load():
     L.cpm_builder_hashes.argtypes = [_P, U64, U64, U64, _P, SZ, _P, SZ, ctypes.c_char_p, ctypes.c_char_p]
     L.cpm_derive_seed_u64.argtypes = [U64, U64]
     L.cpm_derive_seed_u64.restype = U64
+    L.cpm_run_status.argtypes = [_P, SZ, SZ, _P, ctypes.c_uint32, _P, _P, _P, SZ, ctypes.c_uint32, _P, _P, _P]
     L.cpm_result_samples_sizes.argtypes = [_P, _P]
     L.cpm_result_samples_read.argtypes = [_P, _P]
     L.cpm_results_samples_read.argtypes = [_P, SZ, _P]
@@ -664,6 +665,26 @@ class CPM:
 
 def derive_seed_u64(master_seed: int, index: int) -> int:
     return int(_lib.cpm_derive_seed_u64(_u64(master_seed, "master_seed"), _u64(index, "index")))
+
+
+STATUS_KINDS = ("Ok", "NotEquilibrated", "Fragmented", "CellLost", "Degenerate")
+
+
+def run_status(trace, sample_mcs, volumes, first_fragmented=None, last_pairs=(), min_cell_volume=1):
+    """The status rule ``run`` applies (output.rs:456-522) on given readouts;
+    see ``cpm_run_status``. Returns (kind, cell_id, at_mcs)."""
+    t = np.ascontiguousarray(trace, dtype=np.float64)
+    m = np.ascontiguousarray(sample_mcs, dtype=np.uint64)
+    v = np.ascontiguousarray(volumes, dtype=np.uint32)
+    if v.ndim != 2 or v.shape[0] != m.size:
+        raise ValueError("volumes: one row of cell volumes per sample")
+    f = None if first_fragmented is None else np.ascontiguousarray(first_fragmented, dtype=np.uint32)
+    p = np.ascontiguousarray(np.asarray(last_pairs, dtype=np.uint32).reshape(-1, 2))
+    kind, cid, at = ctypes.c_int32(0), ctypes.c_uint32(0), ctypes.c_uint64(0)
+    _check(_lib.cpm_run_status(_ptr(t), t.size, m.size, _ptr(m), v.shape[1], _ptr(v),
+                               _ptr(f) if f is not None else None, _ptr(p), len(p), int(min_cell_volume),
+                               ctypes.byref(kind), ctypes.byref(cid), ctypes.byref(at)))
+    return STATUS_KINDS[kind.value], cid.value, at.value
 
 
 def run_many(builders, burn_in_mcs, readout_mcs, sampling_interval_mcs, include_lattice=False, topology=True):

@@ -295,6 +295,20 @@ int cpm_builder_hashes(const cpm_builder* b, uint64_t burn_in_mcs, uint64_t read
                        char* convention_hash_out, char* model_hash_out);
 /* rng.rs:37-40: first 8 LE bytes of BLAKE3(master LE || index LE). */
 uint64_t cpm_derive_seed_u64(uint64_t master_seed, uint64_t simulation_index);
+/* The run status of output.rs:456-522 (SimulationStatus, with the priority
+ * NotEquilibrated > Fragmented > CellLost > Degenerate) over given readouts:
+ * the burn-in energy trace (not_equilibrated, output.rs:388-420), then per
+ * readout sample its MCS and every cell's volume (row k holds ids 1..n_cells),
+ * the first fragmented cell id of each sample (0: none; NULL: the run had no
+ * topology readouts, which skips Fragmented and Degenerate) and the last
+ * sample's contact pairs with a positive count (a, b interleaved; the medium
+ * is id 0). kind: 0 Ok, 1 NotEquilibrated, 2 Fragmented, 3 CellLost,
+ * 4 Degenerate; cell_id and at_mcs are set for Fragmented and CellLost, else 0.
+ * This is the rule cpm_builder_run applies to its own samples. */
+int cpm_run_status(const double* energy_trace, size_t n_trace, size_t n_samples, const uint64_t* sample_mcs,
+                   uint32_t n_cells, const uint32_t* volumes, const uint32_t* first_fragmented,
+                   const uint32_t* last_contact_pairs, size_t n_pairs, uint32_t min_cell_volume, int32_t* kind,
+                   uint32_t* cell_id, uint64_t* at_mcs);
 
 /* -------------------------------------------- allocation-free sweep ---
  * No counterpart in the reference. For callers that cannot call cudaMalloc
@@ -302,16 +316,24 @@ uint64_t cpm_derive_seed_u64(uint64_t master_seed, uint64_t simulation_index);
  * own pool, or a service that reserves every byte at start-up and treats a
  * later allocation as a failure — and that therefore hand over simulations
  * already resident on the device. cpm_run_mcs_noalloc advances such a
- * simulation by n_mcs MCS with the same sweep as cpm_engine_run_mcs and
- * allocates no device memory: its own scratch (descriptor, plan, work-queue
- * counter, per-cell conflict slots) is a static 1 MiB device array inside
- * the library, held by every GPU that loads it until the process exits.
+ * simulation by n_mcs MCS and allocates no device memory: its own scratch
+ * (descriptor, plan, work-queue counter, per-cell conflict slots) is a
+ * static 1 MiB device array inside the library, held by every GPU that
+ * loads it until the process exits.
+ * Which sweep runs: a lattice that fits one SM's shared memory (the
+ * engine's resident sweep, about 298^2 and below) runs exactly the sweep
+ * cpm_engine_run_mcs runs for it, so both give the same trajectory. A
+ * larger lattice runs the global-memory sweep on one CTA (the chain the
+ * engine runs under CPM_GPU_FORCE_GLOBAL), not the engine's tiled sweep:
+ * a different, equally exact chain, and much slower than the engine there.
  * Limits: 2D lattices only (3D needs the 8 MiB simple-point table), at most
- * 130,559 cells. The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress) with that device current, so make it before
- * any stream capture. Calls share the array: calls that overlap on the GPU
- * race, so serialise them. On return sim->mcs has advanced by n_mcs (the RNG
- * counter base of the next call). */
+ * 130,559 cells. The first call on a device does the set-up: it looks up
+ * the array's device address (cudaGetSymbolAddress) with that device
+ * current, so make that first call before any stream capture. The address
+ * is kept for the life of the process, so the library must not outlive a
+ * cudaDeviceReset of that device. Calls share the array: calls that overlap
+ * on the GPU race, so serialise them. On return sim->mcs has advanced by
+ * n_mcs (the RNG counter base of the next call). */
 typedef struct {
     int32_t dim;                  /* must be 2 */
     int32_t periodic;             /* 1 periodic, 0 fixed */

@@ -1371,6 +1371,66 @@ int orc_take_sample(void* h, orc_cell_sample* cells, double* energy, uint32_t* f
 
 int orc_not_equilibrated(const double* trace, int n) { return not_equilibrated(std::vector<double>(trace, trace + n)) ? 1 : 0; }
 
+// output.rs:456-522: the status of a run from its burn-in energy trace and
+// its readout samples, in the reference's order of checks. Samples are given
+// as arrays: per sample its MCS, every cell's volume (row k, ids 1..n),
+// the first fragmented id (0 none; null = no topology readouts) and, for the
+// last sample, the contact pairs with a positive count. kind: 0 Ok,
+// 1 NotEquilibrated, 2 Fragmented, 3 CellLost, 4 Degenerate.
+int orc_run_status(const double* trace, size_t n_trace, size_t n_samples, const uint64_t* sample_mcs,
+                   uint32_t n_cells, const uint32_t* volumes, const uint32_t* first_fragmented,
+                   const uint32_t* pairs, size_t n_pairs, uint32_t min_cell_volume, int32_t* kind,
+                   uint32_t* cell_id, uint64_t* at_mcs) {
+    *kind = 0; *cell_id = 0; *at_mcs = 0;
+    // output.rs:459-463: NotEquilibrated from the burn-in trace
+    if (not_equilibrated(std::vector<double>(trace, trace + n_trace))) { *kind = 1; return 0; }
+    // output.rs:470-485: the first sample with a fragmented cell, its first id
+    if (first_fragmented)
+        for (size_t k = 0; k < n_samples; ++k)
+            if (first_fragmented[k] != 0) {
+                *kind = 2; *cell_id = first_fragmented[k]; *at_mcs = sample_mcs[k];
+                return 0;
+            }
+    // output.rs:487-511: a cell at the volume floor over the trailing
+    // ceil(0.5 * samples) samples (at least one, at most all)
+    {
+        size_t window = (size_t)std::ceil((double)n_samples * 0.5);
+        window = std::min(std::max(window, (size_t)1), n_samples);
+        if (window > 0) {
+            const size_t first = n_samples - window;
+            for (uint32_t id = 1; id <= n_cells; ++id) {
+                bool floor_all = true;
+                for (size_t k = first; k < n_samples && floor_all; ++k)
+                    floor_all = volumes[k * n_cells + (id - 1)] <= min_cell_volume;
+                if (floor_all) { *kind = 3; *cell_id = id; *at_mcs = sample_mcs[first]; return 0; }
+            }
+        }
+    }
+    // output.rs:513-522, 531-559: the last sample's cell-adjacency graph
+    // (pairs without the medium) is one component holding every cell
+    if (first_fragmented && n_samples > 0 && n_cells >= 2) {
+        std::map<uint32_t, std::vector<uint32_t>> adj;
+        for (size_t q = 0; q < n_pairs; ++q) {
+            const uint32_t a = pairs[2 * q], b = pairs[2 * q + 1];
+            if (a == 0 || b == 0) continue;
+            adj[a].push_back(b);
+            adj[b].push_back(a);
+        }
+        if (!adj.empty()) {
+            std::vector<uint32_t> stack{adj.begin()->first};
+            std::map<uint32_t, bool> seen{{adj.begin()->first, true}};
+            while (!stack.empty()) {
+                const uint32_t u = stack.back();
+                stack.pop_back();
+                for (uint32_t w : adj[u])
+                    if (!seen.count(w)) { seen[w] = true; stack.push_back(w); }
+            }
+            if (seen.size() == n_cells) *kind = 4;
+        }
+    }
+    return 0;
+}
+
 void orc_shape_descriptors(int D, const int64_t* outer, uint32_t volume, const double* centroid, double* eig, double* rg2, double* kappa2) {
     shape_descriptors(D, outer, volume, centroid, eig, rg2, kappa2);
 }
@@ -1420,6 +1480,57 @@ int orc_run_many(int D, const int* grid, int periodic, int copy_kind, int energy
                     shape_descriptors(Dd, &s->sum_outer[(size_t)i * Dd * Dd], s->volume[i], o.centroid, o.eigenvalues, &o.rg2, &o.kappa2);
                 }
                 out_energy[r] = s->energy;
+                delete s;
+            }
+        });
+    for (auto& x : th) x.join();
+    return failed.load();
+}
+
+// Independent runs as orc_run_many, each stopped at `n_ckpt` increasing
+// cumulative MCS counts along one trajectory (monte_carlo.rs:327-357 run in
+// pieces; the chain is the same as one run_mcs call of the total). At each
+// checkpoint c of run r: the running energy and every cell's volume and
+// interface (rows of max_cells, run-major then checkpoint).
+int orc_run_many_checkpoints(int D, const int* grid, int periodic, int copy_kind, int energy_kind, int conn_kind,
+                             int n_types, const uint32_t* target_volume, const uint32_t* target_interface,
+                             const double* lambda_volume, const double* lambda_interface,
+                             const uint64_t* cell_counts, const double* adhesion,
+                             const uint32_t* explicit_lattice, const uint32_t* explicit_type_of,
+                             int explicit_n_cells, int n_runs, const uint64_t* seeds, int n_ckpt,
+                             const uint64_t* ckpt_mcs, int threads, int max_cells, uint32_t* out_volume,
+                             uint32_t* out_interface, double* out_energy, int* out_n_cells) {
+    std::atomic<int> next{0}, failed{0};
+    if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    std::vector<std::thread> th;
+    for (int t = 0; t < threads; ++t)
+        th.emplace_back([&] {
+            for (;;) {
+                const int r = next.fetch_add(1);
+                if (r >= n_runs) break;
+                char err[256];
+                Sim* s = (Sim*)orc_new(D, grid, periodic, copy_kind, energy_kind, conn_kind, n_types, target_volume,
+                                       target_interface, lambda_volume, lambda_interface, cell_counts, adhesion,
+                                       seeds[r], 1, err, sizeof err);
+                if (!s) { failed++; out_n_cells[r] = 0; continue; }
+                s->local_halo = true;
+                bool ok = explicit_lattice
+                              ? s->place_explicit(explicit_lattice, s->lat.n_sites(), explicit_type_of, explicit_n_cells)
+                              : s->scatter_and_grow();
+                if (!ok) { failed++; out_n_cells[r] = 0; delete s; continue; }
+                const int n = std::min(max_cells, s->n_cells());
+                out_n_cells[r] = n;
+                uint64_t done = 0;
+                for (int c = 0; c < n_ckpt; ++c) {
+                    s->run_mcs(ckpt_mcs[c] - done);
+                    done = ckpt_mcs[c];
+                    const size_t row = ((size_t)r * n_ckpt + c) * max_cells;
+                    for (int i = 0; i < n; ++i) {
+                        out_volume[row + i] = s->volume[i];
+                        out_interface[row + i] = s->interface[i];
+                    }
+                    out_energy[(size_t)r * n_ckpt + c] = s->energy;
+                }
                 delete s;
             }
         });

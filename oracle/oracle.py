@@ -157,6 +157,13 @@ def lib():
                 ctypes.c_int, P, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, ctypes.c_int,
                 ctypes.c_int, P, P, P, ctypes.c_int, P, P,
             ]
+            L.orc_run_status.argtypes = [P, ctypes.c_size_t, ctypes.c_size_t, P, ctypes.c_uint32, P, P, P,
+                                         ctypes.c_size_t, ctypes.c_uint32, P, P, P]
+            L.orc_run_many_checkpoints.argtypes = [
+                ctypes.c_int, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                ctypes.c_int, P, P, P, P, P, P, P, P, ctypes.c_int,
+                ctypes.c_int, P, ctypes.c_int, P, ctypes.c_int, ctypes.c_int, P, P, P, P,
+            ]
             _lib = L
         return _lib
 
@@ -426,6 +433,27 @@ def not_equilibrated(trace) -> bool:
     return bool(lib().orc_not_equilibrated(_ptr(t), t.size))
 
 
+STATUS_KINDS = ("Ok", "NotEquilibrated", "Fragmented", "CellLost", "Degenerate")
+
+
+def run_status(trace, sample_mcs, volumes, first_fragmented=None, last_pairs=(), min_cell_volume=1):
+    """output.rs:456-522 on given readouts: (kind, cell_id, at_mcs).
+    volumes: (samples, cells) by id; first_fragmented: per sample the first
+    fragmented id (0 none) or None (no topology readouts); last_pairs: the
+    last sample's contact pairs (a, b) with a positive count."""
+    t = np.ascontiguousarray(trace, dtype=np.float64)
+    m = np.ascontiguousarray(sample_mcs, dtype=np.uint64)
+    v = np.ascontiguousarray(volumes, dtype=np.uint32)
+    assert v.ndim == 2 and v.shape[0] == m.size, "volumes: one row of cell volumes per sample"
+    f = None if first_fragmented is None else np.ascontiguousarray(first_fragmented, dtype=np.uint32)
+    p = np.ascontiguousarray(np.asarray(last_pairs, dtype=np.uint32).reshape(-1, 2))
+    kind, cid, at = ctypes.c_int32(0), ctypes.c_uint32(0), ctypes.c_uint64(0)
+    lib().orc_run_status(_ptr(t), t.size, m.size, _ptr(m), v.shape[1], _ptr(v), _ptr(f) if f is not None else None,
+                         _ptr(p), len(p), int(min_cell_volume), ctypes.byref(kind), ctypes.byref(cid),
+                         ctypes.byref(at))
+    return STATUS_KINDS[kind.value], cid.value, at.value
+
+
 def run_many(spec: ModelSpec, seeds, burn_in: int, readout: int, threads: int = 0, local_halo: bool = True,
              explicit=None, max_cells=None):
     """Independent runs of ``spec`` (default init unless ``explicit`` =
@@ -451,3 +479,33 @@ def run_many(spec: ModelSpec, seeds, burn_in: int, readout: int, threads: int = 
                             threads, int(local_halo), max_cells, _ptr(out_cells), _ptr(out_energy), _ptr(out_n),
                             acc, _ptr(la) if la is not None else None, _ptr(ma) if ma is not None else None)
     return failed, out_cells.reshape(seeds.size, max_cells), out_energy, out_n
+
+
+def run_many_checkpoints(spec: ModelSpec, seeds, checkpoints, threads: int = 0, explicit=None):
+    """Independent runs of ``spec`` (default init unless ``explicit`` =
+    (lattice, cell_type_of)), each read at the cumulative MCS counts
+    ``checkpoints`` along one trajectory. Returns (failed, volume, interface,
+    energy, n_cells): volume and interface of shape (runs, checkpoints,
+    cells), energy (runs, checkpoints)."""
+    L = lib()
+    grid, tv, ti, lv, li, cc, adh = spec.arrays()
+    seeds = np.ascontiguousarray(np.asarray(seeds, dtype=np.uint64))
+    ck = np.ascontiguousarray(np.asarray(checkpoints, dtype=np.uint64))
+    assert np.all(np.diff(ck.astype(np.int64)) > 0)
+    max_cells = int(sum(spec.cell_counts)) if explicit is None else len(explicit[1])
+    vol = np.zeros((seeds.size, ck.size, max_cells), dtype=np.uint32)
+    itf = np.zeros_like(vol)
+    energy = np.zeros((seeds.size, ck.size), dtype=np.float64)
+    n = np.zeros(seeds.size, dtype=np.int32)
+    if explicit is not None:
+        el = np.ascontiguousarray(np.asarray(explicit[0], dtype=np.uint32).ravel())
+        et = np.ascontiguousarray(np.asarray(explicit[1], dtype=np.uint32))
+        elp, etp, en = _ptr(el), _ptr(et), et.size
+    else:
+        elp, etp, en = None, None, 0
+    failed = L.orc_run_many_checkpoints(spec.D, _ptr(grid), int(spec.periodic), NBH[spec.copy], NBH[spec.energy],
+                                        NBH[spec.connectivity], len(spec.types), _ptr(tv), _ptr(ti), _ptr(lv),
+                                        _ptr(li), _ptr(cc), _ptr(adh), elp, etp, en, seeds.size, _ptr(seeds),
+                                        ck.size, _ptr(ck), threads, max_cells, _ptr(vol), _ptr(itf), _ptr(energy),
+                                        _ptr(n))
+    return failed, vol, itf, energy, n
