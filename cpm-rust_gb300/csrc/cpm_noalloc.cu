@@ -22,6 +22,14 @@
 // device address is obtained once per device, with that device current,
 // through cudaGetSymbolAddress, on the first call of the entry point on that
 // device; that first call should therefore come before any stream capture.
+// The address is kept for the life of the process (a cudaDeviceReset of the
+// device would leave it stale).
+//
+// Which sweep runs: the engine's resident sweep when the lattice fits one
+// SM's shared memory (the same trajectory as cpm_engine_run_mcs), else the
+// global-memory sweep on one CTA, which the engine only runs when forced
+// (CPM_GPU_FORCE_GLOBAL); the engine's tiled sweep for such lattices needs
+// per-launch scratch sized by its grid, which this entry point does not hold.
 //
 // Every call shares the array and the array keeps the last call's contents:
 // the work-queue counter (and the fallback statistics) are cleared by each

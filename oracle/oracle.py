@@ -428,6 +428,18 @@ def table_3d() -> np.ndarray:
     return words
 
 
+def shape_descriptors(D: int, sum_outer, volume: int, centroid):
+    """output.rs:147-231 for one cell: (sorted eigenvalues (3), R_g^2, kappa^2)
+    of the gyration tensor sum_outer / V - c c^T."""
+    so = np.ascontiguousarray(np.asarray(sum_outer, dtype=np.int64).ravel())
+    c = np.zeros(3)
+    c[:D] = np.asarray(centroid, dtype=np.float64)[:D]
+    eig = np.zeros(3)
+    rg2, kap = ctypes.c_double(0.0), ctypes.c_double(0.0)
+    lib().orc_shape_descriptors(D, _ptr(so), int(volume), _ptr(c), _ptr(eig), ctypes.byref(rg2), ctypes.byref(kap))
+    return eig, rg2.value, kap.value
+
+
 def not_equilibrated(trace) -> bool:
     t = np.ascontiguousarray(trace, dtype=np.float64)
     return bool(lib().orc_not_equilibrated(_ptr(t), t.size))

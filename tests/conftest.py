@@ -7,7 +7,7 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 PKG = os.path.join(ROOT, "cpm-rust_gb300")
-for p in (ROOT, os.path.join(PKG, "python"), os.path.join(ROOT, "oracle")):
+for p in (ROOT, os.path.join(PKG, "python"), os.path.join(ROOT, "oracle"), os.path.join(ROOT, "tests", "golden")):
     if p not in sys.path:
         sys.path.insert(0, p)
 

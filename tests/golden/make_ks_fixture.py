@@ -20,7 +20,20 @@ And (`odd_oracle_summary.npz`, `--odd`) a lattice with odd periodic sides,
 31x29, one type (V*=50, I*=75, lambda_V=10, lambda_I=2, 5 cells) whose cells
 repel (J=[[0,3],[3,12]]), so the state is stationary by the sample with no
 slow aggregation (2000 burn-in + 2000 readout MCS, seeds 1..96).
-Usage: python tests/golden/make_ks_fixture.py [--fluct | --modes | --odd]
+And (`shapes_oracle_summary.npz`, `--shapes`) the headline shapes on
+lattices the tiled sweep cuts, read at several MCS along each trajectory
+(per seed: energy, mean and spread of the volumes, mean interface):
+  * sorting (the 512x512 differential-adhesion case's shape on 128x128
+    periodic): 4 types V*=50 I*=30 lambda_V=5 lambda_I=1, 66 cells per type
+    (phi=0.8), Moore energy, medium row of J 16 and type-type J uniform in
+    [2, 14] from default_rng(1), scatter-and-grow placement; seeds 1..128,
+    read at 100, 300, 1000, 3000 and 10000 MCS;
+  * organoid (the 128^3 case's shape on 40^3 periodic): 3 types V*=1048
+    I*=600 lambda_V=2 lambda_I=0.5, 16 cells per type (phi=0.8), 26-neighbour
+    energy, medium row 16 and type-type J uniform in [1, 12] from
+    default_rng(1), nested-layer placement (one 2x2x2 seed per cell, types
+    from the centre out); seeds 1..128, read at 25, 50, 100, 200 and 500 MCS.
+Usage: python tests/golden/make_ks_fixture.py [--fluct | --modes | --odd | --shapes]
 """
 
 import os
@@ -111,6 +124,74 @@ def odd_main():
     print("wrote", os.path.join(HERE, "odd_oracle_summary.npz"))
 
 
+SHAPE_SEEDS = 128
+SORTING_CKPT = (100, 300, 1000, 3000, 10000)
+ORGANOID_CKPT = (25, 50, 100, 200, 500)
+
+
+def sorting_shape_spec():
+    rng = np.random.default_rng(1)
+    J = np.zeros((5, 5))
+    J[0, 1:] = J[1:, 0] = 16.0
+    tt = rng.uniform(2, 14, size=(4, 4))
+    J[1:, 1:] = np.triu(tt) + np.triu(tt, 1).T
+    return O.ModelSpec((128, 128), True, [(50, 30, 5.0, 1.0)] * 4, J, cell_counts=[66] * 4)
+
+
+def organoid_shape_adhesion():
+    rng = np.random.default_rng(1)
+    J = np.zeros((4, 4))
+    J[0, 1:] = J[1:, 0] = 16.0
+    tt = rng.uniform(1, 12, size=(3, 3))
+    J[1:, 1:] = np.triu(tt) + np.triu(tt, 1).T
+    return J
+
+
+def organoid_shape_placement(side=40, per_type=(16, 16, 16)):
+    """One 2x2x2 seed per cell on a cubic grid, the seeds nearest the centre
+    first, types in order from the centre outwards."""
+    k = int(sum(per_type))
+    g = max(2, int((side ** 3 / max(k, 1)) ** (1.0 / 3.0)))
+    while True:
+        ax = np.arange(g // 2, side - 1, g)
+        pts = np.stack(np.meshgrid(ax, ax, ax, indexing="ij"), -1).reshape(-1, 3)
+        if len(pts) >= k or g == 2:
+            break
+        g -= 1
+    c = (side - 1) / 2.0
+    order = np.lexsort((np.arange(len(pts)), ((pts - c) ** 2).sum(1)))
+    pts = pts[order[:k]]
+    lat = np.zeros((side, side, side), dtype=np.uint32)
+    for i, (x, y, z) in enumerate(pts):
+        lat[x:x + 2, y:y + 2, z:z + 2] = i + 1
+    return lat.ravel(), np.repeat(np.arange(len(per_type)), per_type)
+
+
+def organoid_shape_spec():
+    return O.ModelSpec((40, 40, 40), True, [(1048, 600, 2.0, 0.5)] * 3, organoid_shape_adhesion(),
+                       cell_counts=[16] * 3, energy="twenty_six")
+
+
+def _summaries(vol, itf, energy):
+    v = vol.astype(np.float64)
+    i = itf.astype(np.float64)
+    return {"energy": energy, "mean_volume": v.mean(2), "volume_std": v.std(2), "mean_interface": i.mean(2)}
+
+
+def shapes_main():
+    seeds = np.arange(1, SHAPE_SEEDS + 1, dtype=np.uint64)
+    out = {"seeds": seeds, "sorting_ckpt": np.array(SORTING_CKPT), "organoid_ckpt": np.array(ORGANOID_CKPT)}
+    failed, vol, itf, energy, n = O.run_many_checkpoints(sorting_shape_spec(), seeds, SORTING_CKPT)
+    assert failed == 0 and np.all(n == 264)
+    out.update({f"sorting_{k}": v for k, v in _summaries(vol, itf, energy).items()})
+    failed, vol, itf, energy, n = O.run_many_checkpoints(organoid_shape_spec(), seeds, ORGANOID_CKPT,
+                                                         explicit=organoid_shape_placement())
+    assert failed == 0 and np.all(n == 48)
+    out.update({f"organoid_{k}": v for k, v in _summaries(vol, itf, energy).items()})
+    np.savez_compressed(os.path.join(HERE, "shapes_oracle_summary.npz"), **out)
+    print("wrote", os.path.join(HERE, "shapes_oracle_summary.npz"))
+
+
 def main():
     seeds = np.arange(1, N_SEEDS + 1, dtype=np.uint64)
     failed, cells, energy, n = O.run_many(c1_spec(), seeds, BURN_IN, READOUT, threads=0, local_halo=True)
@@ -134,8 +215,11 @@ if __name__ == "__main__":
         modes_main()
     elif "--odd" in sys.argv:
         odd_main()
+    elif "--shapes" in sys.argv:
+        shapes_main()
     else:
         main()
         fluct_main()
         modes_main()
         odd_main()
+        shapes_main()

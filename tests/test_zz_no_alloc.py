@@ -59,17 +59,18 @@ def _lib():
     return lib
 
 
-def test_noalloc_sweep_matches_engine_on_two_calls(cuda_required):
+def _check_two_calls(model, builder, cto, mcs, with_stats=True):
+    """Two calls of the no-allocation entry point against the engine on the
+    same simulation (the engine built from `builder`); `with_stats` False
+    passes no counters (the static scratch then holds them)."""
     import torch
 
     from cpm import _cpm
 
     torch.cuda.set_device(0)
-    model = sorting_model(side=48, seed=4)
-    eng = _cpm.Engine(model.builder())
+    eng = _cpm.Engine(builder)
     info = eng.info[0]
     n1 = int(info.n_cells) + 1
-    _, cto, _ = model.builder().initial_state()
 
     # caller-owned device buffers, initialised with the engine's starting state
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
@@ -85,7 +86,7 @@ def test_noalloc_sweep_matches_engine_on_two_calls(cuda_required):
     lam_i = dev(np.array([t[4] for t in model.types], np.float64))
     tv = dev(np.array([t[1] for t in model.types], np.int32))
     ti = dev(np.array([t[2] for t in model.types], np.int32))
-    stats = torch.zeros(32, dtype=torch.int64, device="cuda")  # CPM_STAT_COUNT counters
+    stats = torch.zeros(32, dtype=torch.int64, device="cuda") if with_stats else None  # CPM_STAT_COUNT counters
     torch.cuda.synchronize()
 
     ds = DeviceSim()
@@ -97,16 +98,16 @@ def test_noalloc_sweep_matches_engine_on_two_calls(cuda_required):
     for name, t in (("sigma", sigma), ("type_plus_one", tp1), ("volume", vol), ("interface", itf),
                     ("sum_position", sp), ("sum_position_outer", so), ("adhesion", adh), ("lambda_volume", lam_v),
                     ("lambda_interface", lam_i), ("target_volume", tv), ("target_interface", ti), ("stats", stats)):
-        setattr(ds, name, t.data_ptr())
+        setattr(ds, name, t.data_ptr() if t is not None else None)
 
     lib = _lib()
     stream = torch.cuda.current_stream().cuda_stream
     for call in range(2):
-        rc = lib.cpm_run_mcs_noalloc(ctypes.byref(ds), 10, ctypes.c_void_p(stream))
+        rc = lib.cpm_run_mcs_noalloc(ctypes.byref(ds), mcs, ctypes.c_void_p(stream))
         assert rc == 0, lib.cpm_last_error().decode()
         torch.cuda.synchronize()
-        assert ds.mcs == 10 * (call + 1)
-        eng.run_mcs(10)
+        assert ds.mcs == mcs * (call + 1)
+        eng.run_mcs(mcs)
         eng.synchronize()
         ev, ei, esp, eso = eng.cells()
         assert np.array_equal(sigma.cpu().numpy().view(np.uint32), eng.padded())
@@ -115,9 +116,54 @@ def test_noalloc_sweep_matches_engine_on_two_calls(cuda_required):
         assert np.array_equal(sp.cpu().numpy(), esp.ravel())
         assert np.array_equal(so.cpu().numpy(), eso.ravel())
         st = eng.stats()
-        got = stats.cpu().numpy()
-        assert got[0] == st["attempts"] == 10 * (call + 1) * int(info.n_sites)
-        assert got[5] == st["accepted"]
+        assert st["attempts"] == mcs * (call + 1) * int(info.n_sites)
+        if with_stats:
+            got = stats.cpu().numpy()
+            assert got[0] == st["attempts"]
+            assert got[5] == st["accepted"]
+    assert eng.recount_check()[0]
+
+
+def test_noalloc_sweep_matches_engine_on_two_calls(cuda_required):
+    model = sorting_model(side=48, seed=4)
+    _, cto, _ = model.builder().initial_state()
+    _check_two_calls(model, model.builder(), cto, 10)
+
+
+def test_noalloc_without_counters_matches_engine(cuda_required):
+    """No counters passed: the sweep keeps them in the static scratch, and
+    the state after two calls is still the engine's."""
+    model = sorting_model(side=40, seed=6)
+    _, cto, _ = model.builder().initial_state()
+    _check_two_calls(model, model.builder(), cto, 7, with_stats=False)
+
+
+def test_noalloc_above_the_resident_size_runs_the_global_sweep(cuda_required, monkeypatch):
+    """A 320x320 lattice does not fit one SM: the entry point runs the
+    one-CTA global-memory sweep, which is the engine's chain when the
+    engine is forced onto that sweep."""
+    monkeypatch.setenv("CPM_GPU_FORCE_GLOBAL", "1")
+    model = sorting_model(side=320, seed=8)
+    _, cto, _ = model.builder().initial_state()
+    _check_two_calls(model, model.builder(), cto, 2)
+
+
+def test_noalloc_many_cells_keep_their_slots_in_the_static_scratch(cuda_required, monkeypatch):
+    """28,900 cells (2x2 blocks filling a 340x340 lattice) exceed what the
+    global-memory sweep keeps in shared memory, so their conflict slots live
+    in the static scratch array; the state still equals the engine's on the
+    same sweep."""
+    from helpers import Model
+
+    monkeypatch.setenv("CPM_GPU_FORCE_GLOBAL", "1")
+    side = 340
+    r = np.arange(side) // 2
+    lat = (r[:, None] * (side // 2) + r[None, :] + 1).astype(np.uint32)
+    n = (side // 2) ** 2
+    cto = [k % 2 for k in range(n)]
+    model = Model((side, side), "periodic", [("a", 4, 8, 2.0, 0.5), ("b", 4, 8, 2.0, 0.5)],
+                  [[0, 10, 10], [10, 3, 6], [10, 6, 4]], [0, 0], seed=9)
+    _check_two_calls(model, model.builder(lattice=lat, cell_type_of=cto), cto, 2)
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch(cuda_required):
