@@ -220,23 +220,34 @@ struct GivenDraw {  // the parity harness: u given
     __device__ uint32_t z() const { return (uint32_t)__dmul_rn(u_, 4294967296.0); }
 };
 
-template <int NE, class SigT, class Draw>
-__device__ __forceinline__ bool decide_move(const SimDesc& s, const SigT* sig, const uint16_t* adh_of,
-                                            const uint32_t* volume, const uint32_t* interface, int64_t t, uint32_t L,
-                                            uint32_t G, const Draw& draw, int& dl, int& dg) {
+// The two halves of decide_move. The neighbour half depends on sigma only
+// (the target's energy neighbours, never written by another attempt of the
+// same colour pass), the cell half on the volumes and interfaces of the two
+// cells; a caller that has run the neighbour half once re-runs only the
+// cell half when those cells change. Together they are decide_move, with
+// the same float operations in the same order.
+struct NeighbourPart {
+    float adh, sabs;  // float adhesion sum over the neighbours, sum of |leaf|
+    int dl, dg;       // integer interface deltas
+    bool fast;        // float tables present (else the FP64 path decides)
+};
+
+template <int NE, class SigT, class Off>
+__device__ __forceinline__ NeighbourPart decide_neighbours(const SimDesc& s, const SigT* sig, const uint16_t* adh_of,
+                                                           const Off* energy_off, int64_t t, uint32_t L, uint32_t G) {
     const int nt1 = s.n_types + 1;
     const int li = adh_of[L], gi = adh_of[G];
-    const int tn = s.tab_n;
-    bool fast = s.dj32 != nullptr;
+    NeighbourPart o;
+    o.fast = s.dj32 != nullptr;
     float adh = 0.f, sabs = 0.f;
     int cl = 0, cg = 0;
-    if (fast) {
+    if (o.fast) {
         const float* Dt = s.dj32 + (li * nt1 + gi) * nt1;
         const float jgl = s.J32[gi * nt1 + li];
         const float jlg = -s.J32[li * nt1 + gi];
 #pragma unroll
         for (int k = 0; k < NE; ++k) {
-            const uint32_t nc = (uint32_t)sig[t + s.energy_off[k]];
+            const uint32_t nc = (uint32_t)sig[t + energy_off[k]];
             const bool isl = nc == L, isg = nc == G;
             cl += isl;
             cg += isg;
@@ -247,69 +258,101 @@ __device__ __forceinline__ bool decide_move(const SimDesc& s, const SigT* sig, c
     } else {
 #pragma unroll
         for (int k = 0; k < NE; ++k) {
-            const uint32_t nc = (uint32_t)sig[t + s.energy_off[k]];
+            const uint32_t nc = (uint32_t)sig[t + energy_off[k]];
             cl += nc == L;
             cg += nc == G;
         }
     }
-    dl = 2 * cl - NE;
-    dg = NE - 2 * cg;
-    if (fast) {
-        float vol = 0.f, itf = 0.f;
-        float sterm = 0.f;
-        // one term difference table[x1] - table[x0] as a leaf
-        auto leaf = [&](const float* hi, const float* lo, int64_t x1, int64_t x0) -> float {
-            const float a = hi[x1], b = hi[x0];
-            const float r = (a - b) + (lo[x1] - lo[x0]);
-            sabs += fabsf(r);
-            sterm += fabsf(a) + fabsf(b);
-            return r;
-        };
-        if (L) {
-            const int ty = li - 1;
-            const int64_t v = volume[L], i = interface[L];
-            if (v >= 1 && v < tn && i + dl >= 0 && i + dl < tn && i < tn) {
-                vol += leaf(s.vterm32 + ty * tn, s.vterm32lo + ty * tn, v - 1, v);
-                itf += leaf(s.iterm32 + ty * tn, s.iterm32lo + ty * tn, i + dl, i);
-            } else {
-                fast = false;
-            }
-        }
-        if (G) {
-            const int ty = gi - 1;
-            const int64_t v = volume[G], i = interface[G];
-            if (v + 1 < tn && i + dg >= 0 && i + dg < tn && i < tn) {
-                vol += leaf(s.vterm32 + ty * tn, s.vterm32lo + ty * tn, v + 1, v);
-                itf += leaf(s.iterm32 + ty * tn, s.iterm32lo + ty * tn, i + dg, i);
-            } else {
-                fast = false;
-            }
-        }
-        if (fast && sabs <= 1e30f && sterm <= 1e30f) {
-            const float dh = (vol + itf) + adh;
-            const float eps = 4e-6f * sabs + 1e-12f * sterm + 1e-30f;
-            const float hi = dh + eps, lo = dh - eps;
-            if (hi <= 0.f) return true;
-            const uint32_t z = draw.z();
-            if (lo > 64.f) {
-                if (z != 0u) return false;  // u >= 2^-32 > exp(-64)
-            } else if (hi <= 64.f) {
-                const float ulo = __uint2float_rd(z) * 2.3283064365386963e-10f;
-                const float uhi = __fadd_ru(__uint2float_ru(z), 1.0f) * 2.3283064365386963e-10f;
-                // u < exp(-hi) <= exp(-dh64) accepts whatever the sign of dh64
-                const float elo = expf(-hi) * (1.0f - 3e-5f);
-                if (uhi < elo) return true;
-                if (lo > 0.f) {
-                    const float ehi = expf(-lo) * (1.0f + 3e-5f);
-                    if (ulo > ehi) return false;
-                }
-            }
+    o.adh = adh;
+    o.sabs = sabs;
+    o.dl = 2 * cl - NE;
+    o.dg = NE - 2 * cg;
+    return o;
+}
+
+// The cell half: 1 = accept, 0 = reject, -1 = the float bracket cannot
+// decide (the caller then runs the FP64 computation in the reference's
+// order). `li` / `gi` are the adhesion indices (type + 1) of L and G.
+template <class Draw>
+__device__ __forceinline__ int decide_cells(const SimDesc& s, const NeighbourPart& nb, int li, int gi,
+                                            const uint32_t* volume, const uint32_t* interface, uint32_t L,
+                                            uint32_t G, const Draw& draw) {
+    if (!nb.fast) return -1;
+    const int tn = s.tab_n;
+    const int dl = nb.dl, dg = nb.dg;
+    float sabs = nb.sabs;
+    float vol = 0.f, itf = 0.f;
+    float sterm = 0.f;
+    // one term difference table[x1] - table[x0] as a leaf
+    auto leaf = [&](const float* hi, const float* lo, int64_t x1, int64_t x0) -> float {
+        const float a = hi[x1], b = hi[x0];
+        const float r = (a - b) + (lo[x1] - lo[x0]);
+        sabs += fabsf(r);
+        sterm += fabsf(a) + fabsf(b);
+        return r;
+    };
+    if (L) {
+        const int ty = li - 1;
+        const int64_t v = volume[L], i = interface[L];
+        if (v >= 1 && v < tn && i + dl >= 0 && i + dl < tn && i < tn) {
+            vol += leaf(s.vterm32 + ty * tn, s.vterm32lo + ty * tn, v - 1, v);
+            itf += leaf(s.iterm32 + ty * tn, s.iterm32lo + ty * tn, i + dl, i);
+        } else {
+            return -1;
         }
     }
-    // exact: the reference's FP64 operation order
+    if (G) {
+        const int ty = gi - 1;
+        const int64_t v = volume[G], i = interface[G];
+        if (v + 1 < tn && i + dg >= 0 && i + dg < tn && i < tn) {
+            vol += leaf(s.vterm32 + ty * tn, s.vterm32lo + ty * tn, v + 1, v);
+            itf += leaf(s.iterm32 + ty * tn, s.iterm32lo + ty * tn, i + dg, i);
+        } else {
+            return -1;
+        }
+    }
+    if (!(sabs <= 1e30f && sterm <= 1e30f)) return -1;
+    const float dh = (vol + itf) + nb.adh;
+    const float eps = 4e-6f * sabs + 1e-12f * sterm + 1e-30f;
+    const float hi = dh + eps, lo = dh - eps;
+    if (hi <= 0.f) return 1;
+    const uint32_t z = draw.z();
+    if (lo > 64.f) {
+        if (z != 0u) return 0;  // u >= 2^-32 > exp(-64)
+    } else if (hi <= 64.f) {
+        const float ulo = __uint2float_rd(z) * 2.3283064365386963e-10f;
+        const float uhi = __fadd_ru(__uint2float_ru(z), 1.0f) * 2.3283064365386963e-10f;
+        // u < exp(-hi) <= exp(-dh64) accepts whatever the sign of dh64
+        const float elo = expf(-hi) * (1.0f - 3e-5f);
+        if (uhi < elo) return 1;
+        if (lo > 0.f) {
+            const float ehi = expf(-lo) * (1.0f + 3e-5f);
+            if (ulo > ehi) return 0;
+        }
+    }
+    return -1;
+}
+
+// The exact decision: the reference's FP64 operation order (counted).
+template <int NE, class SigT, class Draw>
+__device__ __noinline__ bool decide_exact(const SimDesc& s, const SigT* sig, const uint16_t* adh_of,
+                                          const uint32_t* volume, const uint32_t* interface, int64_t t, uint32_t L,
+                                          uint32_t G, const Draw& draw) {
     if (s.stats) atomicAdd(&s.stats[CPM_STAT_EXACT_DECISIONS], 1ull);
     const DeltaOut o = delta_h<NE, SigT>(s, sig, adh_of, volume, interface, t, L, G);
     return metropolis(o.dh, o.dh > 0.0 ? draw.u() : 0.0);
+}
+
+template <int NE, class SigT, class Draw>
+__device__ __forceinline__ bool decide_move(const SimDesc& s, const SigT* sig, const uint16_t* adh_of,
+                                            const uint32_t* volume, const uint32_t* interface, int64_t t, uint32_t L,
+                                            uint32_t G, const Draw& draw, int& dl, int& dg) {
+    const NeighbourPart nb = decide_neighbours<NE, SigT, int64_t>(s, sig, adh_of, s.energy_off, t, L, G);
+    dl = nb.dl;
+    dg = nb.dg;
+    const int r = decide_cells(s, nb, adh_of[L], adh_of[G], volume, interface, L, G, draw);
+    if (r >= 0) return r != 0;
+    return decide_exact<NE, SigT, Draw>(s, sig, adh_of, volume, interface, t, L, G, draw);
 }
 
 // ------------------------------------------------------ modes of the loop ----

@@ -42,6 +42,7 @@ namespace cpmgpu {
 constexpr int TB = 256;          // threads per CTA
 constexpr int TCMAX = 1024;      // candidate slots per tile pass
 constexpr int TMAX_BOX = 48 * 48 * 48;  // largest shared box (sites)
+constexpr int TCHG = 1024;       // changed sites listed per sub-phase (beyond: the whole tile is written back)
 enum : uint32_t {
     T_ACC = 1u << 3, T_PEND = 1u << 4, T_FIN = 1u << 5, T_GUARD = 1u << 6, T_DONE = 1u << 7,
 };
@@ -109,9 +110,17 @@ static __device__ bool grid_sync(BarrierState* b, unsigned int n, unsigned int& 
     return s_ok != 0;
 }
 
+// Per-thread event counts (32-bit: a launch covers at most 2^18 MCS) and,
+// in shared memory, the cycle counters thread 0 (lane 0 in the warp
+// resolution) keeps for the profile (CPM_STAT_CYC_*).
+enum TileCyc { TC_PASS = 0, TC_STAGE, TC_SYNC, TC_BUILD, TC_EVAL, TC_FIX, TC_APPLY, TC_LOWER, TC_CLAIM, TC_BAR1,
+               TC_BAR2, TC_N };
 struct TileCounters {
-    unsigned long long nonnull, topo, guard, evaluated, accepted, rounds, deferred, wide;
-    unsigned long long c_build, c_eval, c_fix, c_apply, c_lower;
+    uint32_t nonnull, topo, guard, evaluated, accepted, rounds, deferred, wide;
+    unsigned long long* cyc;  // TC_N shared counters
+    __device__ __forceinline__ void tick(int which, long long d) {
+        if (threadIdx.x == 0) cyc[which] += (unsigned long long)d;
+    }
 };
 
 // The attempt's draw with its top word taken from the per-site table staged
@@ -123,6 +132,18 @@ struct TileDraw {
     __device__ uint32_t z() const { return zv; }
 };
 
+// preserves_topology on the box with 32-bit local offsets
+template <int D>
+__device__ __forceinline__ bool tile_simple(const uint16_t* sig, const int* toff, int t, uint32_t losing,
+                                            const uint32_t* t2, const uint64_t* t3) {
+    if (losing == 0) return true;  // medium is exempt (connectivity.rs:48-50)
+    constexpr int NF = D == 2 ? 8 : 26;
+    uint32_t p = 0;
+#pragma unroll
+    for (int i = 0; i < NF; ++i) p |= (uint32_t)((uint32_t)sig[t + toff[i]] == losing) << i;
+    return D == 2 ? table2d_bit(t2, p) : table3d_bit(t3, p);
+}
+
 template <int D, int NE>
 struct TileProc {
     const SimDesc& g;     // global descriptor
@@ -132,10 +153,31 @@ struct TileProc {
     uint32_t *vol, *itf, *b0, *b1;
     uint16_t* adh;
     uint8_t *dirty, *own, *mod;
+    // candidate arrays of the pass being resolved (a slice of the tile's
+    // candidate storage: see at())
     uint32_t *c_site, *c_key, *c_cells, *c_flags, *c_gf, *c_z;
     int16_t* c_dl;
+    // the neighbour half of each candidate's decision (decide_neighbours,
+    // computed while building the pass) and its global coordinates
+    float *c_adh, *c_sabs;
+    uint32_t* c_xy;   // axis 0 | axis 1 << 16
+    uint16_t* c_x2;   // axis 2 (3D)
+    // sites whose sigma a commit changed in this sub-phase (box indices)
+    uint32_t* chg;
+    int* s_nchg;
     const uint64_t* t3;
     int* s_n;
+    // the candidate storage's base pointers; at(off) points the candidate
+    // arrays at the slice starting at candidate `off`
+    uint32_t *b_site, *b_key, *b_cells, *b_flags, *b_gf, *b_z, *b_xy;
+    int16_t* b_dl;
+    float *b_adh, *b_sabs;
+    uint16_t* b_x2;
+    __device__ __forceinline__ void at(int off) {
+        c_site = b_site + off; c_key = b_key + off; c_cells = b_cells + off; c_flags = b_flags + off;
+        c_gf = b_gf + off; c_z = b_z + off; c_xy = b_xy + off; c_dl = b_dl + off; c_adh = b_adh + off;
+        c_sabs = b_sabs + off; c_x2 = b_x2 + off;
+    }
     // The box holds box-local cell slots, not cell ids: slot s >= 1 is
     // the cell clist[s - 1], slot 0 the medium; every per-cell array is
     // indexed by slot. Position sums of the first cl_cap slots are staged in
@@ -180,17 +222,27 @@ struct TileProc {
         return f;
     }
 
+    // The candidate's decision on the current volumes and interfaces: the
+    // cell half of decide_move over the neighbour half staged with the
+    // candidate (sigma around it cannot change within its pass).
     __device__ void evaluate(int c, uint64_t mcs) {
-        const int t = (int)c_site[c];
         const uint32_t cells = c_cells[c];
         const uint32_t L = cells & 0xFFFFu, G = cells >> 16;
         uint32_t fl = c_flags[c] & ~(T_ACC | T_GUARD);
         if (L != 0 && vol[L] <= l.min_cell_volume) {
             fl |= T_GUARD;
         } else {
-            int dl = 0, dg = 0;
-            if (decide_move<NE, uint16_t>(l, sig, adh, vol, itf, t, L, G, TileDraw{g.seed, mcs, c_gf[c], c_z[c]}, dl, dg)) fl |= T_ACC;
-            c_dl[c] = (int16_t)((dl & 0xFF) | ((dg & 0xFF) << 8));
+            const int16_t dd = c_dl[c];
+            NeighbourPart nb;
+            nb.adh = c_adh[c];
+            nb.sabs = c_sabs[c];
+            nb.dl = (int)(int8_t)(dd & 0xFF);
+            nb.dg = (int)(int8_t)((dd >> 8) & 0xFF);
+            nb.fast = l.dj32 != nullptr;
+            const TileDraw draw{g.seed, mcs, c_gf[c], c_z[c]};
+            int r = decide_cells(l, nb, adh[L], adh[G], vol, itf, L, G, draw);
+            if (r < 0) r = decide_exact<NE, uint16_t>(l, sig, adh, vol, itf, (int)c_site[c], L, G, draw) ? 1 : 0;
+            if (r) fl |= T_ACC;
         }
         c_flags[c] = fl;
     }
@@ -204,8 +256,15 @@ struct TileProc {
         const int16_t dd = c_dl[c];
         const int dl = (int)(int8_t)(dd & 0xFF), dg = (int)(int8_t)((dd >> 8) & 0xFF);
         int xg[3];
-        gflat_of_box(t, xg);
+        const uint32_t xy = c_xy[c];
+        xg[0] = (int)(xy & 0xFFFFu);
+        xg[1] = (int)(xy >> 16);
+        xg[2] = D > 2 ? (int)c_x2[c] : 0;
         sig[t] = (uint16_t)G;
+        {
+            const int k = atomicAdd(s_nchg, 1);
+            if (k < TCHG) chg[k] = (uint32_t)t;
+        }
         if (L) {
             vol[L] -= 1;
             itf[L] += (uint32_t)dl;
@@ -266,16 +325,13 @@ struct TileProc {
 
     // K = 1 handles n <= 32 candidates, K = 2 n <= 64 (candidate c = lane +
     // 32 q, bit c of the 64-bit masks).
+    //
+    // The build has already made every candidate's first decision.
     template <int K>
     __device__ void resolve_warp(int n, uint64_t mcs, TileCounters& ct) {
         const int lane = threadIdx.x & 31;
         long long t0 = clock64();
-#pragma unroll
-        for (int q = 0; q < K; ++q)
-            if (lane + 32 * q < n) evaluate(lane + 32 * q, mcs);
-        __syncwarp();
-        long long tm = clock64();
-        ct.c_eval += tm - t0;
+        long long tm = t0;
         uint32_t Lc[K], Gc[K], key[K], fl[K];
         Mask<K> lower[K];
         bool have[K];
@@ -323,7 +379,7 @@ struct TileProc {
         for (int q = 0; q < K; ++q) fl[q] = have[q] ? c_flags[lane + 32 * q] : 0u;
         Mask<K> pending = ballot_k<K>(have);
         long long t1 = clock64();
-        ct.c_lower += t1 - tm;
+        ct.tick(TC_LOWER, t1 - tm);
         while (pending) {
             t0 = clock64();
             bool mine[K], rej[K];
@@ -345,7 +401,7 @@ struct TileProc {
                 fin = f2;
             }
             t1 = clock64();
-            ct.c_fix += t1 - t0;
+            ct.tick(TC_FIX, t1 - t0);
             bool cm[K];
 #pragma unroll
             for (int q = 0; q < K; ++q) {
@@ -373,17 +429,16 @@ struct TileProc {
                 }
             }
             __syncwarp();
-            ct.c_apply += clock64() - t1;
+            ct.tick(TC_APPLY, clock64() - t1);
         }
     }
 
+    // The block-wide resolution (more than 64 candidates); the build has
+    // made the first decisions.
     __device__ void resolve(int n, uint64_t mcs, TileCounters& ct) {
         const int tid = threadIdx.x;
         long long t0 = clock64();
-        for (int c = tid; c < n; c += TB) evaluate(c, mcs);
-        __syncthreads();
-        long long t1 = clock64();
-        ct.c_eval += t1 - t0;
+        long long t1 = t0;
         for (;;) {
             t0 = clock64();
             // finality as in the resident sweep: final unless an accepting
@@ -417,7 +472,7 @@ struct TileProc {
                 if (!__syncthreads_or(changed)) break;
             }
             t1 = clock64();
-            ct.c_fix += t1 - t0;
+            ct.tick(TC_FIX, t1 - t0);
             int left = 0;
             for (int c = tid; c < n; c += TB) {
                 uint32_t fl = c_flags[c];
@@ -435,7 +490,7 @@ struct TileProc {
             }
             ct.rounds++;
             const int more = __syncthreads_or(left);
-            ct.c_apply += clock64() - t1;
+            ct.tick(TC_APPLY, clock64() - t1);
             if (!more) break;
             t1 = clock64();
             for (int c = tid; c < n; c += TB) {
@@ -453,7 +508,7 @@ struct TileProc {
                 c_flags[c] = fl & ~T_DONE;
             }
             __syncthreads();
-            ct.c_apply += clock64() - t1;
+            ct.tick(TC_APPLY, clock64() - t1);
         }
         for (int c = tid; c < n; c += TB) {
             if (!(c_flags[c] & T_DONE)) continue;
@@ -466,9 +521,8 @@ struct TileProc {
 };
 
 struct TileShared {
-    uint32_t sig, sid, skd, sgf, sz, vol, itf, b0, b1, adh, dirty, own, mod, clist, ssp, sso, rseen, rslot, c_site, c_key,
-        c_cells,
-        c_flags, c_gf, c_z, c_dl, total;
+    uint32_t sig, sid, skd, sgf, sz, vol, itf, b0, b1, adh, dirty, own, mod, clist, ssp, sso, rseen, rslot, chg, pass, c_site,
+        c_key, c_cells, c_flags, c_gf, c_z, c_dl, c_adh, c_sabs, c_xy, c_x2, total;
 };
 
 __host__ __device__ inline uint32_t tl_take(uint32_t& off, uint64_t b) {
@@ -500,16 +554,22 @@ __host__ __device__ inline TileShared tile_shared(int box_sites, int n_cells, in
     s.sso = tl_take(off, (uint64_t)cl_cap * D * D * 8);
     s.rseen = tl_take(off, reg_smem ? ((uint64_t)n_cells + 1) * 4 : 0);
     s.rslot = tl_take(off, reg_smem ? ((uint64_t)n_cells + 1) * 2 : 0);
+    s.chg = tl_take(off, TCHG * 4);
+    s.pass = tl_take(off, (27 * 12 + 27 + 28 + 27 * 6) * 4);  // per-pass geometry and counters
     s.c_site = tl_take(off, TCMAX * 4);
     s.c_key = tl_take(off, TCMAX * 4);
     s.c_cells = tl_take(off, TCMAX * 4);
     s.c_flags = tl_take(off, TCMAX * 4);
     s.c_gf = tl_take(off, TCMAX * 4);
     s.c_z = tl_take(off, TCMAX * 4);
+    s.c_adh = tl_take(off, TCMAX * 4);
+    s.c_sabs = tl_take(off, TCMAX * 4);
+    s.c_xy = tl_take(off, TCMAX * 4);
     s.c_dl = tl_take(off, TCMAX * 2);
+    s.c_x2 = tl_take(off, TCMAX * 2);
     // the staged cell ids, before they become slots: only used while a box
     // is staged, so they share the candidate arrays when they fit there
-    s.sid = (uint64_t)box_sites * 4 <= (uint64_t)(s.c_dl + TCMAX * 2 - s.c_site) ? s.c_site
+    s.sid = (uint64_t)box_sites * 4 <= (uint64_t)(s.c_x2 + TCMAX * 2 - s.c_site) ? s.c_site
                                                                                    : tl_take(off, (uint64_t)box_sites * 4);
     s.total = off;
     return s;
@@ -534,9 +594,12 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                                                    int reg_smem, uint32_t* seen_all, uint32_t* slot_all) {
     extern __shared__ __align__(16) unsigned char sm[];
     __shared__ SimDesc gsd, lsd;
-    __shared__ int s_n, s_tile, s_ncell, s_box_dims[3], s_gx0[3], s_tcnt[3];
+    __shared__ int s_n, s_tile, s_ncell, s_box_dims[3], s_gx0[3], s_g0[3], s_tcnt[3];
     __shared__ int perm[8], sperm[27];
-    __shared__ uint32_t s_pkey[27];
+    __shared__ uint32_t s_pkey[27], s_swap[27];
+    __shared__ int s_nchg;
+    // the box's stencils as 32-bit local index offsets
+    __shared__ int s_eoff[CPM_MAX_STENCIL], s_toff[CPM_MAX_STENCIL], s_coff[6];
     __shared__ int s_ncls[3];
     __shared__ unsigned long long sstat[8];
     const int tid = threadIdx.x;
@@ -584,6 +647,18 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
     // tile's box. In shared memory when it fits (reg_smem), else in HBM
     // (n_cells + 1 words each per CTA).
     const TileShared ts0 = tile_shared(max_box, g.n_cells, cl_cap, D, reg_smem != 0);
+    // per site-colour pass: class geometry (count, first, count before the
+    // wrap, first past the wrap per axis), site count and prefix, and the
+    // speculative build's candidate count, accept flag and event counts
+    int(*s_pg)[12] = (int(*)[12])(sm + ts0.pass);
+    int* s_pn = (int*)(sm + ts0.pass) + 27 * 12;
+    int* s_pfx = s_pn + 27;
+    int* s_pcnt = s_pfx + 28;
+    int* s_pacc = s_pcnt + 27;
+    int* s_pguard = s_pacc + 27;
+    int* s_pnonnull = s_pguard + 27;
+    int* s_ptopo = s_pnonnull + 27;
+    int* s_pdef = s_ptopo + 27;
     uint32_t* seen_g = seen_all + (size_t)blockIdx.x * (size_t)(g.n_cells + 1);
     uint32_t* slot_g = slot_all + (size_t)blockIdx.x * (size_t)(g.n_cells + 1);
     for (int id = tid; id <= g.n_cells; id += TB) {
@@ -603,9 +678,11 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
     auto reg_get = [&](uint32_t id) -> uint32_t {
         return reg_smem ? (uint32_t)((const uint16_t*)(sm + ts0.rslot))[id] : __ldcg(slot_g + id);
     };
-    TileCounters ct = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    __shared__ unsigned long long s_cyc[TC_N];
+    if (tid < TC_N) s_cyc[tid] = 0ull;
+    __syncthreads();
+    TileCounters ct = {0, 0, 0, 0, 0, 0, 0, 0, s_cyc};
     unsigned long long attempts = 0, tile_passes = 0;
-    unsigned long long cyc_pass = 0, cyc_stage = 0, cyc_sync = 0, cyc_claim = 0, cyc_bar1 = 0, cyc_bar2 = 0;
     const uint64_t mcs0 = g.mcs;
     bool alive = true;
     unsigned int bar_epoch = 0;
@@ -618,11 +695,16 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
             const uint32_t rr[3] = {r.x, r.y, r.z};
             for (int d = 0; d < D; ++d) tg.off[d] = g.periodic ? (int)(((unsigned long long)rr[d] * (unsigned)g.dims[d]) >> 32) : 0;
         }
+        // Fisher-Yates over the tile colours; the draws first, one per thread
+        if (tid > 0 && tid < tg.colors) {
+            const uint4 r = aux_draw(g.seed, mcs, TAG_TILE, 1u, (uint32_t)tid);
+            s_swap[tid] = (uint32_t)(((unsigned long long)r.x * (unsigned)(tid + 1)) >> 32);
+        }
+        __syncthreads();
         if (tid == 0) {
             for (int c = 0; c < tg.colors; ++c) perm[c] = c;
             for (int c = tg.colors - 1; c > 0; --c) {
-                const uint4 r = aux_draw(g.seed, mcs, TAG_TILE, 1u, (uint32_t)c);
-                const int j = (int)(((unsigned long long)r.x * (unsigned)(c + 1)) >> 32);
+                const int j = (int)s_swap[c];
                 const int t = perm[c]; perm[c] = perm[j]; perm[j] = t;
             }
         }
@@ -660,6 +742,7 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                         const int L = g.dims[d];
                         const int b0 = tile_begin(tc[d], L, tg.nt[d]), b1 = tile_begin(tc[d] + 1, L, tg.nt[d]);
                         s_gx0[d] = b0 + tg.off[d];
+                        s_g0[d] = (b0 + tg.off[d]) % L;  // both terms are in [0, L)
                         s_tcnt[d] = b1 - b0;
                         s_box_dims[d] = b1 - b0 + 2;
                         lsd.dims[d] = b1 - b0;
@@ -681,9 +764,10 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                         t += (int64_t)g.topo_vec[kk][d] * lsd.strides[d];
                         if (kk < 6) c += (int64_t)g.copy_vec[kk][d] * lsd.strides[d];
                     }
-                    if (kk < g.n_energy) lsd.energy_off[kk] = e;
+                    if (kk < g.n_energy) { lsd.energy_off[kk] = e; s_eoff[kk] = (int)e; }
                     lsd.topo_off[kk] = t;
-                    if (kk < g.n_copy) lsd.copy_off[kk] = c;
+                    s_toff[kk] = (int)t;
+                    if (kk < g.n_copy) { lsd.copy_off[kk] = c; s_coff[kk] = (int)c; }
                 }
                 __syncthreads();
             };
@@ -692,7 +776,13 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                               (uint16_t*)(sm + ts.adh), (uint8_t*)(sm + ts.dirty), (uint8_t*)(sm + ts.own),
                               (uint8_t*)(sm + ts.mod), (uint32_t*)(sm + ts.c_site), (uint32_t*)(sm + ts.c_key),
                               (uint32_t*)(sm + ts.c_cells), (uint32_t*)(sm + ts.c_flags), (uint32_t*)(sm + ts.c_gf),
-                              (uint32_t*)(sm + ts.c_z), (int16_t*)(sm + ts.c_dl), t3, &s_n,
+                              (uint32_t*)(sm + ts.c_z), (int16_t*)(sm + ts.c_dl), (float*)(sm + ts.c_adh),
+                              (float*)(sm + ts.c_sabs), (uint32_t*)(sm + ts.c_xy), (uint16_t*)(sm + ts.c_x2),
+                              (uint32_t*)(sm + ts.chg), &s_nchg, t3, &s_n,
+                              (uint32_t*)(sm + ts.c_site), (uint32_t*)(sm + ts.c_key), (uint32_t*)(sm + ts.c_cells),
+                              (uint32_t*)(sm + ts.c_flags), (uint32_t*)(sm + ts.c_gf), (uint32_t*)(sm + ts.c_z),
+                              (uint32_t*)(sm + ts.c_xy), (int16_t*)(sm + ts.c_dl), (float*)(sm + ts.c_adh),
+                              (float*)(sm + ts.c_sabs), (uint16_t*)(sm + ts.c_x2),
                               clist, (long long*)(sm + ts.ssp), (long long*)(sm + ts.sso), cl_cap};
             uint32_t* sid = (uint32_t*)(sm + ts.sid);
             uint8_t* skd = (uint8_t*)(sm + ts.skd);
@@ -759,18 +849,21 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                     }
                 }
                 // the tile's site-colour order and pass keys
-                if (tid == 0) {
-                    const int ncol = n_cls;
-                    for (int c = 0; c < ncol; ++c) sperm[c] = c;
-                    for (int c = ncol - 1; c > 0; --c) {
-                        const uint4 rr = aux_draw(g.seed, mcs, TAG_TILE, 2u + (uint32_t)k, (uint32_t)c);
-                        const int j = (int)(((unsigned long long)rr.x * (unsigned)(c + 1)) >> 32);
-                        const int t = sperm[c]; sperm[c] = sperm[j]; sperm[j] = t;
-                    }
+                // (Fisher-Yates draws one per thread, then the swaps)
+                if (tid > 0 && tid < n_cls) {
+                    const uint4 rr = aux_draw(g.seed, mcs, TAG_TILE, 2u + (uint32_t)k, (uint32_t)tid);
+                    s_swap[tid] = (uint32_t)(((unsigned long long)rr.x * (unsigned)(tid + 1)) >> 32);
                 }
                 if (tid < n_cls)
                     s_pkey[tid] = aux_draw(g.seed, mcs, TAG_PASS, (uint32_t)(tid * 64 + ci), (uint32_t)k).x;
                 __syncthreads();  // every listing (and its slot write) is visible to the block
+                if (tid == 0) {
+                    for (int c = 0; c < n_cls; ++c) sperm[c] = c;
+                    for (int c = n_cls - 1; c > 0; --c) {
+                        const int j = (int)s_swap[c];
+                        const int t = sperm[c]; sperm[c] = sperm[j]; sperm[j] = t;
+                    }
+                }
 #pragma unroll 4
                 for (int q = tid; q < box; q += TB) {
                     const uint32_t id = sid[q];
@@ -843,9 +936,9 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
             const long long t_c1 = clock64();
             if (!grid_sync(bar, arrivals, bar_epoch)) { alive = false; break; }
             const long long t_c2 = clock64();
-            cyc_sync += t_c2 - t_c0;
-            cyc_claim += t_c1 - t_c0;
-            cyc_bar1 += t_c2 - t_c1;
+            ct.tick(TC_SYNC, t_c2 - t_c0);
+            ct.tick(TC_CLAIM, t_c1 - t_c0);
+            ct.tick(TC_BAR1, t_c2 - t_c1);
             // ---- process the tiles
             for (int k = blockIdx.x; k < per_color; k += nblk) {
                 long long t_s0 = clock64();
@@ -854,119 +947,235 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                     stage_box(k, false, 512u);  // a stamp distinct from the claim pass over this box
                     __syncthreads();
                 }
+                if (tid == 0) s_nchg = 0;
                 read_claims(k);
                 const unsigned long long key = base_key | (unsigned long long)k;
                 (void)key;
                 int box = 1;
                 for (int d = 0; d < D; ++d) box *= s_box_dims[d];
                 long long t_p0 = clock64();
-                cyc_stage += t_p0 - t_s0;
-                // site-colour passes of this tile, in the order staged with the box
-                for (int pi = 0; pi < n_cls; ++pi) {
-                    int sc = sperm[pi];
-                    // The local sites whose global coordinate has colour sc_d on
-                    // every axis d: the parity, or (odd periodic axis) 2 for the
-                    // last coordinate L-1, whose neighbour across the wrap (0)
-                    // has its parity. Per axis they are first_a + 2i for
-                    // i < cnt_a, then (past the wrap) base_b + 2(i - cnt_a).
-                    int cnt[3], base[3], cnt_a[3], base_b[3];
+                ct.tick(TC_STAGE, t_p0 - t_s0);
+                // Site-colour passes of this tile, in the order staged with the
+                // box. Every pass is first built at once from the state the
+                // tile starts with (candidates, their neighbour halves and
+                // first decisions): sigma and the cells change only through
+                // commits, so while no pass has committed those builds are
+                // exactly what building each pass in turn would give. A pass
+                // without an accepting candidate needs no resolution (every
+                // candidate is a final reject); the first pass that commits
+                // ends the speculation, and each later pass is built again
+                // after the one before it.
+                //
+                // The local sites of pass pi have colour sc_d on every axis d:
+                // the parity, or (odd periodic axis) 2 for the last coordinate
+                // L-1, whose neighbour across the wrap (0) has its parity. Per
+                // axis they are first_a + 2i for i < cnt_a, then (past the
+                // wrap) base_b + 2(i - cnt_a).
+                if (tid < n_cls) {
+                    int sc = sperm[tid];
                     int n_class = 1;
+                    int* pg = s_pg[tid];
                     for (int d = 0; d < D; ++d) {
                         const int Ld = g.dims[d];
                         const int nc_d = ODD ? s_ncls[d] : 2;
                         const int want = ODD ? sc % nc_d : (sc >> d) & 1;
                         if (ODD) sc /= nc_d;
-                        const int g0 = ((s_gx0[d] % Ld) + Ld) % Ld;
+                        const int g0 = s_g0[d];
                         const int tc = s_tcnt[d];
+                        int cnt, base, cnt_a, base_b;
                         if (nc_d == 2) {
                             const int first = (want - (g0 & 1)) & 1;  // first local offset with that parity
-                            base[d] = first;
-                            cnt[d] = tc > first ? (tc - first + 1) / 2 : 0;
-                            cnt_a[d] = cnt[d];
-                            base_b[d] = 0;
+                            base = first;
+                            cnt = tc > first ? (tc - first + 1) / 2 : 0;
+                            cnt_a = cnt;
+                            base_b = 0;
                         } else {
                             const int w = Ld - g0;  // local offsets before the wrap: g0 + i <= L - 1
                             if (want == 2) {
-                                base[d] = w - 1;
-                                cnt[d] = cnt_a[d] = w - 1 < tc ? 1 : 0;
-                                base_b[d] = 0;
+                                base = w - 1;
+                                cnt = cnt_a = w - 1 < tc ? 1 : 0;
+                                base_b = 0;
                             } else {
                                 const int end_a = w - 1 < tc ? w - 1 : tc;  // g0 + i < L - 1
                                 const int first = (want - (g0 & 1)) & 1;
-                                base[d] = first;
-                                cnt_a[d] = end_a > first ? (end_a - first + 1) / 2 : 0;
-                                base_b[d] = w + want;  // past the wrap: g = i - w
-                                cnt[d] = cnt_a[d] + (tc > base_b[d] ? (tc - base_b[d] + 1) / 2 : 0);
+                                base = first;
+                                cnt_a = end_a > first ? (end_a - first + 1) / 2 : 0;
+                                base_b = w + want;  // past the wrap: g = i - w
+                                cnt = cnt_a + (tc > base_b ? (tc - base_b + 1) / 2 : 0);
                             }
                         }
-                        n_class *= cnt[d];
+                        pg[4 * d + 0] = cnt;
+                        pg[4 * d + 1] = base;
+                        pg[4 * d + 2] = cnt_a;
+                        pg[4 * d + 3] = base_b;
+                        n_class *= cnt;
                     }
-                    const uint32_t pass_key = s_pkey[pi];
+                    s_pn[tid] = n_class;
+                    s_pcnt[tid] = 0;
+                    s_pacc[tid] = 0;
+                    s_pguard[tid] = 0;
+                    s_pnonnull[tid] = 0;
+                    s_ptopo[tid] = 0;
+                    s_pdef[tid] = 0;
+                }
+                __syncthreads();
+                if (tid == 0) {
+                    int acc = 0;
+                    for (int q = 0; q < n_cls; ++q) { s_pfx[q] = acc; acc += s_pn[q]; }
+                    s_pfx[n_cls] = acc;
+                }
+                __syncthreads();
+                // One site j of pass pi: a candidate goes to slot atomicAdd(cnt)
+                // of the slice at candidate `off` (capacity `cap`; beyond it the
+                // pass overflows and is built again with the whole storage).
+                // `spec`: event counts go to the pass's shared counters (used
+                // only if the build is used), else to this thread's counters.
+                auto build_site = [&](int pi, int j, int off, int cap, int* cnt, bool spec) {
+                    const int* pg = s_pg[pi];
+                    int r = j, t = 0;
+                    int xg[3] = {0, 0, 0};
+                    for (int d = D - 1; d >= 0; --d) {
+                        const int c_d = pg[4 * d];
+                        const int i = r % c_d;
+                        r /= c_d;
+                        const int li = !ODD || i < pg[4 * d + 2] ? pg[4 * d + 1] + 2 * i
+                                                                : pg[4 * d + 3] + 2 * (i - pg[4 * d + 2]);
+                        t += (li + 1) * (int)lsd.strides[d];
+                        int x = s_g0[d] + li;  // global interior coordinate
+                        if (x >= g.dims[d]) x -= g.dims[d];
+                        xg[d] = x;
+                    }
+                    const int kd = skd[t];
+                    const uint32_t L = P.sig[t];
+                    const uint32_t G = P.sig[t + s_coff[kd]];
+                    if (L == G) return;
+                    if (spec) atomicAdd(&s_pnonnull[pi], 1); else ct.nonnull++;
+                    if (!P.own[L] || !P.own[G]) {
+                        if (spec) atomicAdd(&s_pdef[pi], 1); else ct.deferred++;
+                        return;
+                    }
+                    if (!tile_simple<D>(P.sig, s_toff, t, L, g.table2d, t3)) {
+                        if (spec) atomicAdd(&s_ptopo[pi], 1); else ct.topo++;
+                        return;
+                    }
+                    const int pos = atomicAdd(cnt, 1);
+                    if (pos >= cap) return;
+                    const int c = off + pos;
+                    const int gf = (int)sgf[t];
+                    // the neighbour half of the decision, fixed for the pass
+                    const NeighbourPart nb = decide_neighbours<NE, uint16_t, int>(lsd, P.sig, P.adh, s_eoff, t, L, G);
+                    P.b_site[c] = (uint32_t)t;
+                    P.b_cells[c] = L | (G << 16);
+                    P.b_key[c] = (mix32((uint32_t)j * 0x9E3779B9u ^ s_pkey[pi]) & 0xFFFFC000u) | (uint32_t)j;
+                    P.b_gf[c] = (uint32_t)gf;
+                    P.b_z[c] = sz[t];
+                    P.b_adh[c] = nb.adh;
+                    P.b_sabs[c] = nb.sabs;
+                    P.b_dl[c] = (int16_t)((nb.dl & 0xFF) | ((nb.dg & 0xFF) << 8));
+                    P.b_xy[c] = (uint32_t)xg[0] | ((uint32_t)xg[1] << 16);
+                    if (D > 2) P.b_x2[c] = (uint16_t)xg[2];
+                    // the first decision, on the volumes and interfaces before
+                    // any commit of the pass (TileProc::evaluate, made here)
+                    uint32_t fl = (uint32_t)kd | T_PEND;
+                    if (L != 0 && P.vol[L] <= lsd.min_cell_volume) {
+                        fl |= T_GUARD;
+                        atomicAdd(&s_pguard[pi], 1);
+                    } else {
+                        const TileDraw draw{g.seed, mcs, (uint32_t)gf, sz[t]};
+                        int rr = decide_cells(lsd, nb, P.adh[L], P.adh[G], P.vol, P.itf, L, G, draw);
+                        if (rr < 0) rr = decide_exact<NE, uint16_t>(lsd, P.sig, P.adh, P.vol, P.itf, t, L, G, draw) ? 1 : 0;
+                        if (rr) {
+                            fl |= T_ACC;
+                            s_pacc[pi] = 1;
+                        }
+                    }
+                    P.b_flags[c] = fl;
+                };
+                const int ncap = TCMAX / n_cls;  // candidates per pass while speculating
+                {
                     const long long tb0 = clock64();
-                    if (tid == 0) s_n = 0;
-                    __syncthreads();
-                    for (int j0 = 0; j0 < n_class; j0 += TB) {
+                    const int total = s_pfx[n_cls];
+                    for (int j0 = 0; j0 < total; j0 += TB) {
                         const int j = j0 + tid;
-                        bool cand = false;
-                        int t = 0, kd = 0, gf = 0;
-                        uint32_t L = 0, G = 0;
-                        if (j < n_class) {
-                            int r = j;
-                            t = 0;
-                            for (int d = D - 1; d >= 0; --d) {
-                                const int i = r % cnt[d];
-                                r /= cnt[d];
-                                const int li = !ODD || i < cnt_a[d] ? base[d] + 2 * i : base_b[d] + 2 * (i - cnt_a[d]);
-                                t += (li + 1) * (int)lsd.strides[d];
-                            }
-                            gf = (int)sgf[t];
-                            kd = skd[t];
-                            L = P.sig[t];
-                            G = P.sig[t + (int)lsd.copy_off[kd]];
-                            if (L != G) {
-                                ct.nonnull++;
-                                if (!P.own[L] || !P.own[G]) ct.deferred++;
-                                else if (preserves_topology<D, uint16_t>(lsd, P.sig, t, L, g.table2d, t3)) cand = true;
-                                else ct.topo++;
-                            }
-                        }
-                        const unsigned msk = __ballot_sync(0xffffffffu, cand);
-                        int basepos = 0;
-                        if ((tid & 31) == 0 && msk) basepos = atomicAdd(&s_n, __popc(msk));
-                        basepos = __shfl_sync(0xffffffffu, basepos, 0);
-                        if (cand) {
-                            const int pos = basepos + __popc(msk & ((1u << (tid & 31)) - 1));
-                            if (pos < TCMAX) {
-                                P.c_site[pos] = (uint32_t)t;
-                                P.c_cells[pos] = L | (G << 16);
-                                P.c_key[pos] = (mix32((uint32_t)j * 0x9E3779B9u ^ pass_key) & 0xFFFFC000u) | (uint32_t)j;
-                                P.c_flags[pos] = (uint32_t)kd | T_PEND;
-                                P.c_gf[pos] = (uint32_t)gf;
-                                P.c_z[pos] = sz[t];
-                            }
-                        }
+                        if (j >= total) break;
+                        int pi = 0;
+                        while (pi + 1 < n_cls && s_pfx[pi + 1] <= j) ++pi;
+                        build_site(pi, j - s_pfx[pi], pi * ncap, ncap, &s_pcnt[pi], true);
                     }
                     __syncthreads();
-                    const int n = min(s_n, TCMAX);
-                    __syncthreads();
-                    ct.c_build += clock64() - tb0;
-                    if (n > 64) {
-                        P.resolve(n, mcs, ct);
-                        ct.wide++;
-                    } else if (n > 0) {
-                        if (tid < 32) {
-                            if (n > 32) P.template resolve_warp<2>(n, mcs, ct);
-                            else P.template resolve_warp<1>(n, mcs, ct);
+                    ct.tick(TC_BUILD, clock64() - tb0);
+                }
+                bool spec = true;
+                for (int pi = 0; pi < n_cls; ++pi) {
+                    const int n_class = s_pn[pi];
+                    int n, off;
+                    bool acc;
+                    uint32_t guards;
+                    if (spec && s_pcnt[pi] <= ncap) {
+                        // the speculative build of this pass stands
+                        n = s_pcnt[pi];
+                        off = pi * ncap;
+                        acc = s_pacc[pi] != 0;
+                        guards = (uint32_t)s_pguard[pi];
+                        if (tid == 0) {
+                            ct.nonnull += (uint32_t)s_pnonnull[pi];
+                            ct.topo += (uint32_t)s_ptopo[pi];
+                            ct.deferred += (uint32_t)s_pdef[pi];
                         }
+                    } else {
+                        // built again on the state the earlier passes left
+                        spec = false;
+                        const long long tb0 = clock64();
+                        if (tid == 0) { s_n = 0; s_pacc[pi] = 0; s_pguard[pi] = 0; }
                         __syncthreads();
+                        for (int j = tid; j < n_class; j += TB) build_site(pi, j, 0, TCMAX, &s_n, false);
+                        __syncthreads();
+                        n = min(s_n, TCMAX);
+                        off = 0;
+                        acc = s_pacc[pi] != 0;
+                        guards = (uint32_t)s_pguard[pi];
+                        ct.tick(TC_BUILD, clock64() - tb0);
                     }
+                    P.at(off);
+                    if (!acc) {
+                        // no candidate accepts: all are final rejects
+                        if (tid == 0) {
+                            ct.guard += guards;
+                            ct.evaluated += (uint32_t)n - guards;
+                        }
+                    } else {
+                        spec = false;  // this pass commits
+                        if (n > 64) {
+                            P.resolve(n, mcs, ct);
+                            ct.wide++;
+                        } else {
+                            if (tid < 32) {
+                                if (n > 32) P.template resolve_warp<2>(n, mcs, ct);
+                                else P.template resolve_warp<1>(n, mcs, ct);
+                            }
+                        }
+                    }
+                    // every thread has read this pass's counters before the
+                    // next (re)build resets shared state
+                    __syncthreads();
                     attempts += tid == 0 ? (unsigned long long)n_class : 0ull;
                     tile_passes += tid == 0 ? 1ull : 0ull;
                 }
                 long long t_w0 = clock64();
-                cyc_pass += t_w0 - t_p0;
-                // write back the tile's sites (and periodic mirrors) and the owned cells
-                for (int q = tid; q < box; q += TB) {
+                ct.tick(TC_PASS, t_w0 - t_p0);
+                // write back the sites commits changed (and their periodic
+                // mirrors), or every tile site if the list overflowed, and
+                // the owned cells
+                const int nchg = s_nchg;
+                if (nchg <= TCHG) {
+                    for (int k2 = tid; k2 < nchg; k2 += TB) {
+                        const int q = (int)P.chg[k2];
+                        int xg[3];
+                        P.gflat_of_box(q, xg);
+                        const uint32_t sl = P.sig[q];
+                        write_site<D, uint32_t>(g, g.sigma, xg, sl ? clist[sl - 1] : 0u);
+                    }
+                } else for (int q = tid; q < box; q += TB) {
                     int r = q;
                     int li[3];
                     bool interior = true;
@@ -997,12 +1206,12 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                     }
                 }
                 __syncthreads();
-                cyc_stage += clock64() - t_w0;
+                ct.tick(TC_STAGE, clock64() - t_w0);
             }
             long long t_b0 = clock64();
             if (!grid_sync(bar, arrivals, bar_epoch)) { alive = false; break; }
-            cyc_sync += clock64() - t_b0;
-            cyc_bar2 += clock64() - t_b0;
+            ct.tick(TC_SYNC, clock64() - t_b0);
+            ct.tick(TC_BAR2, clock64() - t_b0);
         }
     }
     // statistics: every site was attempted once per completed MCS
@@ -1018,18 +1227,18 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
     if (tid == 0) {
         atomicAdd(&g.stats[CPM_STAT_ROUNDS], ct.rounds);
         atomicAdd(&g.stats[CPM_STAT_DEFERRED], sstat[6]);
-        atomicAdd(&g.stats[CPM_STAT_CYC_PASSES], cyc_pass);
-        atomicAdd(&g.stats[CPM_STAT_CYC_STAGE], cyc_stage);
-        atomicAdd(&g.stats[CPM_STAT_CYC_SYNC], cyc_sync);
-        atomicAdd(&g.stats[CPM_STAT_CYC_BUILD], ct.c_build);
-        atomicAdd(&g.stats[CPM_STAT_CYC_EVAL], ct.c_eval);
-        atomicAdd(&g.stats[CPM_STAT_CYC_FIX], ct.c_fix);
-        atomicAdd(&g.stats[CPM_STAT_CYC_APPLY], ct.c_apply);
+        atomicAdd(&g.stats[CPM_STAT_CYC_PASSES], s_cyc[TC_PASS]);
+        atomicAdd(&g.stats[CPM_STAT_CYC_STAGE], s_cyc[TC_STAGE]);
+        atomicAdd(&g.stats[CPM_STAT_CYC_SYNC], s_cyc[TC_SYNC]);
+        atomicAdd(&g.stats[CPM_STAT_CYC_BUILD], s_cyc[TC_BUILD]);
+        atomicAdd(&g.stats[CPM_STAT_CYC_EVAL], s_cyc[TC_EVAL]);
+        atomicAdd(&g.stats[CPM_STAT_CYC_FIX], s_cyc[TC_FIX]);
+        atomicAdd(&g.stats[CPM_STAT_CYC_APPLY], s_cyc[TC_APPLY]);
         atomicAdd(&g.stats[CPM_STAT_WIDE_PASSES], ct.wide);
-        atomicAdd(&g.stats[CPM_STAT_CYC_LOWER], ct.c_lower);
-        atomicAdd(&g.stats[CPM_STAT_CYC_CLAIM], cyc_claim);
-        atomicAdd(&g.stats[CPM_STAT_CYC_BAR_CLAIM], cyc_bar1);
-        atomicAdd(&g.stats[CPM_STAT_CYC_BAR_WRITE], cyc_bar2);
+        atomicAdd(&g.stats[CPM_STAT_CYC_LOWER], s_cyc[TC_LOWER]);
+        atomicAdd(&g.stats[CPM_STAT_CYC_CLAIM], s_cyc[TC_CLAIM]);
+        atomicAdd(&g.stats[CPM_STAT_CYC_BAR_CLAIM], s_cyc[TC_BAR1]);
+        atomicAdd(&g.stats[CPM_STAT_CYC_BAR_WRITE], s_cyc[TC_BAR2]);
         atomicAdd(&g.stats[CPM_STAT_PASSES], tile_passes);
         if (blockIdx.x == 0 && alive) simp->mcs = mcs0 + n_mcs;
         if (!alive) {
