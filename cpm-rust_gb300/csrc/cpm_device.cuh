@@ -73,6 +73,17 @@ __device__ __forceinline__ bool preserves_topology(const SimDesc& s, const SigT*
     return D == 2 ? table2d_bit(t2, p) : table3d_bit(t3, p);
 }
 
+// True when every copy neighbour of t holds `id` (= sigma[t]): the attempt
+// at t is null (monte_carlo.rs:60-64) for every copy direction, so a sweep
+// can skip its draw; draws are counters of (seed, MCS, site), so skipping
+// one changes no other.
+template <class SigT>
+__device__ __forceinline__ bool copy_uniform(const SimDesc& s, const SigT* sig, int64_t t, uint32_t id) {
+    bool u = true;
+    for (int k = 0; k < s.n_copy; ++k) u &= (uint32_t)sig[t + s.copy_off[k]] == id;
+    return u;
+}
+
 // ------------------------------------------------------------ Delta-H ----
 // term(t, x) = lambda[t] * (x - target[t])^2, powi(2) == x*x (energy.rs:85-88).
 __device__ __forceinline__ double quad_term(double lambda, uint32_t target, double x) {

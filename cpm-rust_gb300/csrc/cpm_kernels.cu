@@ -169,11 +169,14 @@ __device__ void color_pass(const SimDesc& s, const PassInfo& p, uint64_t mcs, ui
             if (idx >= p.n) break;
             int x[3];
             const int t = site_of<D>(s, p, idx, x);
+            const uint32_t L = sig[t];
+            ct.attempts++;
+            // every copy neighbour holds the target's cell: null whatever the
+            // copy direction, so the draw (a counter, not a stream) is skipped
+            if (copy_uniform(s, sig, t, L)) continue;
             const uint4 r = site_draw(s.seed, mcs, (uint32_t)t);
             const int k = (int)(((unsigned long long)r.x * (unsigned)s.n_copy) >> 32);
-            const uint32_t L = sig[t];
             const uint32_t G = sig[t + (int)s.copy_off[k]];
-            ct.attempts++;
             if (L == G) continue;  // early-out (monte_carlo.rs:60-64)
             ct.nonnull++;
             if (!s.no_connectivity && !preserves_topology<D, uint32_t>(s, sig, t, L, s.table2d, t3)) {

@@ -29,6 +29,7 @@
 #include <stdint.h>
 
 #include <mutex>
+#include <type_traits>
 
 #include "cpm_common.h"
 #include "cpm_device.cuh"
@@ -248,11 +249,150 @@ struct Resident {
         if (G) dirty[G] = 1;
     }
 
+    // The same outcome as resolve() for n <= 32 (K = 1) or n <= 64 (K = 2)
+    // candidates, by one warp, candidate c = lane + 32 q: `lower` holds the
+    // lower-priority candidates sharing a cell (the medium is not a cell);
+    // a pending candidate is final once every lower pending one is a final
+    // reject; final accepts are pairwise cell-disjoint and commit; a
+    // pending candidate with a committed lower neighbour decides again.
+    // Every candidate has been evaluated; b0 and b1 are free.
+    template <int K>
+    using Mask = typename std::conditional<K == 1, uint32_t, uint64_t>::type;
+    template <int K>
+    __device__ __forceinline__ static Mask<K> ballot_k(const bool (&p)[K]) {
+        Mask<K> m = __ballot_sync(0xffffffffu, p[0]);
+        if (K > 1) m |= (Mask<K>)__ballot_sync(0xffffffffu, p[K > 1 ? 1 : 0]) << (K > 1 ? 32 : 0);
+        return m;
+    }
+    template <int K>
+    __device__ void resolve_warp(int n, uint64_t mcs, CountersR& ct) {
+        const int lane = threadIdx.x & 31;
+        uint32_t Lc[K], Gc[K], key[K], fl[K];
+        Mask<K> lower[K];
+        bool have[K];
+#pragma unroll
+        for (int q = 0; q < K; ++q) {
+            const int c = lane + 32 * q;
+            have[q] = c < n;
+            const uint32_t cells = have[q] ? c_cells[c] : 0u;
+            key[q] = have[q] ? c_key[c] : 0xFFFFFFFFu;
+            Lc[q] = cells & 0xFFFFu;
+            Gc[q] = cells >> 16;
+        }
+#pragma unroll
+        for (int q = 0; q < K; ++q) {
+            if (Lc[q]) { b0[Lc[q]] = 0u; if (K > 1) b1[Lc[q]] = 0u; }
+            if (Gc[q]) { b0[Gc[q]] = 0u; if (K > 1) b1[Gc[q]] = 0u; }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < K; ++q) {
+            uint32_t* bm = q == 0 ? b0 : b1;
+            if (Lc[q]) atomicOr(&bm[Lc[q]], 1u << lane);
+            if (Gc[q]) atomicOr(&bm[Gc[q]], 1u << lane);
+        }
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < K; ++q) {
+            Mask<K> sh = 0;
+            if (Lc[q]) sh |= (Mask<K>)b0[Lc[q]] | (K > 1 ? (Mask<K>)b1[Lc[q]] << (K > 1 ? 32 : 0) : (Mask<K>)0);
+            if (Gc[q]) sh |= (Mask<K>)b0[Gc[q]] | (K > 1 ? (Mask<K>)b1[Gc[q]] << (K > 1 ? 32 : 0) : (Mask<K>)0);
+            sh &= ~((Mask<K>)1 << (lane + 32 * q));
+            Mask<K> lw = 0;
+            while (sh) {
+                const int j = K == 1 ? __ffs((uint32_t)sh) - 1 : __ffsll((long long)sh) - 1;
+                sh &= sh - 1;
+                if (c_key[j] < key[q]) lw |= (Mask<K>)1 << j;
+            }
+            lower[q] = lw;
+        }
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < K; ++q) fl[q] = have[q] ? c_flags[lane + 32 * q] : 0u;
+        Mask<K> pending = ballot_k<K>(have);
+        while (pending) {
+            bool mine[K], rej[K];
+#pragma unroll
+            for (int q = 0; q < K; ++q) {
+                mine[q] = (pending >> (lane + 32 * q)) & 1u;
+                rej[q] = (fl[q] & F_GUARD) || !(fl[q] & F_ACC);
+            }
+            Mask<K> fin = 0;
+            for (;;) {
+                bool fr[K], nf[K];
+#pragma unroll
+                for (int q = 0; q < K; ++q) fr[q] = ((fin >> (lane + 32 * q)) & 1u) && rej[q];
+                const Mask<K> frej = ballot_k<K>(fr);
+#pragma unroll
+                for (int q = 0; q < K; ++q) nf[q] = mine[q] && (lower[q] & pending & ~frej) == 0;
+                const Mask<K> f2 = ballot_k<K>(nf);
+                ct.iters += lane == 0;
+                if (f2 == fin) break;
+                fin = f2;
+            }
+            bool cm[K];
+#pragma unroll
+            for (int q = 0; q < K; ++q) {
+                const bool is_fin = (fin >> (lane + 32 * q)) & 1u;
+                cm[q] = is_fin && !rej[q];
+                if (is_fin) {
+                    if (fl[q] & F_GUARD) ct.guard++;
+                    else ct.evaluated++;
+                }
+                if (cm[q]) {
+                    commit(lane + 32 * q, mcs);
+                    ct.accepted++;
+                }
+            }
+            const Mask<K> committed = ballot_k<K>(cm);
+            pending &= ~fin;
+            ct.rounds += lane == 0;
+            __syncwarp();
+#pragma unroll
+            for (int q = 0; q < K; ++q) {
+                const int c = lane + 32 * q;
+                if (((pending >> c) & 1u) && (lower[q] & committed)) {
+                    evaluate(c, mcs);
+                    fl[q] = c_flags[c];
+                }
+            }
+            __syncwarp();
+        }
+        // commit() marks the cells it changes dirty; clear those marks
+#pragma unroll
+        for (int q = 0; q < K; ++q) {
+            if (Lc[q]) dirty[Lc[q]] = 0;
+            if (Gc[q]) dirty[Gc[q]] = 0;
+        }
+        __syncwarp();
+    }
+
     // Resolve the candidates [0, n) of one chunk in priority order.
     __device__ void resolve(int n, uint64_t mcs, CountersR& ct) {
         const int tid = threadIdx.x;
-        for (int c = tid; c < n; c += RB) evaluate(c, mcs);
-        __syncthreads();
+        bool any_acc = false;
+        for (int c = tid; c < n; c += RB) {
+            evaluate(c, mcs);
+            any_acc |= (c_flags[c] & (F_ACC | F_GUARD)) == F_ACC;
+        }
+        if (!__syncthreads_or(any_acc)) {
+            // no candidate accepts: every one is a final reject
+            for (int c = tid; c < n; c += RB) {
+                if (c_flags[c] & F_GUARD) ct.guard++;
+                else ct.evaluated++;
+            }
+            ct.rounds += tid == 0;
+            return;
+        }
+        if (n <= 64) {
+            // one warp on register masks, no block barrier inside
+            if (tid < 32) {
+                if (n > 32) resolve_warp<2>(n, mcs, ct);
+                else resolve_warp<1>(n, mcs, ct);
+            }
+            __syncthreads();
+            return;
+        }
         for (;;) {
             // ---- finality. A pending candidate is final unless an accepting
             // candidate lies in its lower closure (lower-key candidates
@@ -364,10 +504,15 @@ struct Resident {
                     if (j < len) {
                         int x[3];
                         t = site_r<D>(s, p, start + j, x);
-                        const uint4 r = site_draw(s.seed, mcs, (uint32_t)t);
-                        k = (int)(((unsigned long long)r.x * (unsigned)s.n_copy) >> 32);
                         L = sig[t];
-                        G = sig[t + (int)s.copy_off[k]];
+                        G = L;
+                        // every copy neighbour holds the target's cell: null
+                        // whatever the copy direction (the draw is skipped)
+                        if (!copy_uniform(s, sig, t, L)) {
+                            const uint4 r = site_draw(s.seed, mcs, (uint32_t)t);
+                            k = (int)(((unsigned long long)r.x * (unsigned)s.n_copy) >> 32);
+                            G = sig[t + (int)s.copy_off[k]];
+                        }
                         if (L != G) {
                             ++nonnull;
                             if (preserves_topology<D, uint16_t>(s, sig, t, L, s.table2d, t3)) cand = true;
@@ -412,7 +557,7 @@ __global__ void __launch_bounds__(RB, 512 / RB) resident_kernel(SimDesc* sims, c
     extern __shared__ __align__(16) unsigned char sm[];
     __shared__ SimDesc sd;
     __shared__ int s_plan, s_n, s_flag;
-    __shared__ int perm[27];
+    __shared__ int perm[27], s_swap[27];
     __shared__ PassInfoR pinfo;
     __shared__ double scratch[RB / 32];
     __shared__ unsigned long long sstat[10];
@@ -456,12 +601,18 @@ __global__ void __launch_bounds__(RB, 512 / RB) resident_kernel(SimDesc* sims, c
         CountersR ct = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
         uint64_t mcs = sd.mcs;
         auto one_mcs = [&](uint64_t m) {
+            // Fisher-Yates over the colours: the draws one per thread, then
+            // the swaps
+            if (tid > 0 && tid < sd.n_colors) {
+                const uint4 r = aux_draw(sd.seed, m, TAG_ORDER, (uint32_t)tid, 0u);
+                s_swap[tid] = (int)(((unsigned long long)r.x * (unsigned)(tid + 1)) >> 32);
+            }
+            __syncthreads();
             if (tid == 0) {
                 const int nc = sd.n_colors;
                 for (int c = 0; c < nc; ++c) perm[c] = c;
                 for (int c = nc - 1; c > 0; --c) {
-                    const uint4 r = aux_draw(sd.seed, m, TAG_ORDER, (uint32_t)c, 0u);
-                    const int j = (int)(((unsigned long long)r.x * (unsigned)(c + 1)) >> 32);
+                    const int j = s_swap[c];
                     const int tmp = perm[c]; perm[c] = perm[j]; perm[j] = tmp;
                 }
             }

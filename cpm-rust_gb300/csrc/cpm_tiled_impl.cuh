@@ -521,7 +521,7 @@ struct TileProc {
 };
 
 struct TileShared {
-    uint32_t sig, sid, skd, sgf, sz, vol, itf, b0, b1, adh, dirty, own, mod, clist, ssp, sso, rseen, rslot, chg, pass, c_site,
+    uint32_t sig, sid, vol, itf, b0, b1, adh, dirty, own, mod, clist, ssp, sso, rseen, rslot, chg, pass, c_site,
         c_key, c_cells, c_flags, c_gf, c_z, c_dl, c_adh, c_sabs, c_xy, c_x2, total;
 };
 
@@ -538,9 +538,6 @@ __host__ __device__ inline TileShared tile_shared(int box_sites, int n_cells, in
     // slots: the medium and at most one per box site (or per cell)
     const uint64_t n1 = (uint64_t)(box_sites < n_cells ? box_sites : n_cells) + 1;
     s.sig = tl_take(off, (uint64_t)box_sites * 2);
-    s.skd = tl_take(off, (uint64_t)box_sites);      // copy direction of each tile site's attempt
-    s.sgf = tl_take(off, (uint64_t)box_sites * 4);  // its global flat index (the draw's counter)
-    s.sz = tl_take(off, (uint64_t)box_sites * 4);   // the top word of its uniform
     s.vol = tl_take(off, n1 * 4);
     s.itf = tl_take(off, n1 * 4);
     s.b0 = tl_take(off, n1 * 4);
@@ -785,9 +782,6 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                               (float*)(sm + ts.c_sabs), (uint16_t*)(sm + ts.c_x2),
                               clist, (long long*)(sm + ts.ssp), (long long*)(sm + ts.sso), cl_cap};
             uint32_t* sid = (uint32_t*)(sm + ts.sid);
-            uint8_t* skd = (uint8_t*)(sm + ts.skd);
-            uint32_t* sgf = (uint32_t*)(sm + ts.sgf);
-            uint32_t* sz = (uint32_t*)(sm + ts.sz);
             // Stage the box of the current tile: each distinct cell of the
             // box listed once (and claimed when `claim`) and given the next
             // slot, the box's sigma as slots, then the listed cells' V, I,
@@ -824,27 +818,12 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                         const unsigned peers = __match_any_sync(0xffffffffu, id);
                         const bool leader = (int)(threadIdx.x & 31) == __ffs(peers) - 1;
                         if (!valid) continue;
-                        const int gf = gfs[u];
                         sid[q] = id;
                         if (id && leader && reg_first(id, stamp)) {
                             if (claim) atomicMin(claims + id, key);
                             const int k1 = atomicAdd(&s_ncell, 1);
                             clist[k1] = id;
                             reg_set(id, (uint32_t)(k1 + 1));
-                        }
-                        // this MCS's draw of each tile site (site_draw keyed by the global flat index)
-                        bool interior = true;
-                        int r = q;
-                        for (int d = D - 1; d >= 0; --d) {
-                            const int li = r % s_box_dims[d];
-                            r /= s_box_dims[d];
-                            if (li == 0 || li == s_box_dims[d] - 1) interior = false;
-                        }
-                        if (interior) {
-                            const uint4 rd = site_draw(g.seed, mcs, (uint32_t)gf);
-                            skd[q] = (uint8_t)(((unsigned long long)rd.x * (unsigned)g.n_copy) >> 32);
-                            sgf[q] = (uint32_t)gf;
-                            sz[q] = rd.z;
                         }
                     }
                 }
@@ -1045,8 +1024,19 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                         if (x >= g.dims[d]) x -= g.dims[d];
                         xg[d] = x;
                     }
-                    const int kd = skd[t];
+                    // this MCS's draw of the site (site_draw keyed by the global
+                    // flat index), skipped when every copy neighbour holds the
+                    // site's cell: the attempt is null for any copy direction
                     const uint32_t L = P.sig[t];
+                    {
+                        bool uniform = true;
+                        for (int k = 0; k < g.n_copy; ++k) uniform &= (uint32_t)P.sig[t + s_coff[k]] == L;
+                        if (uniform) return;
+                    }
+                    int gf = 0;
+                    for (int d = 0; d < D; ++d) gf += (xg[d] + 1) * (int)g.strides[d];
+                    const uint4 rd = site_draw(g.seed, mcs, (uint32_t)gf);
+                    const int kd = (int)(((unsigned long long)rd.x * (unsigned)g.n_copy) >> 32);
                     const uint32_t G = P.sig[t + s_coff[kd]];
                     if (L == G) return;
                     if (spec) atomicAdd(&s_pnonnull[pi], 1); else ct.nonnull++;
@@ -1061,14 +1051,13 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                     const int pos = atomicAdd(cnt, 1);
                     if (pos >= cap) return;
                     const int c = off + pos;
-                    const int gf = (int)sgf[t];
                     // the neighbour half of the decision, fixed for the pass
                     const NeighbourPart nb = decide_neighbours<NE, uint16_t, int>(lsd, P.sig, P.adh, s_eoff, t, L, G);
                     P.b_site[c] = (uint32_t)t;
                     P.b_cells[c] = L | (G << 16);
                     P.b_key[c] = (mix32((uint32_t)j * 0x9E3779B9u ^ s_pkey[pi]) & 0xFFFFC000u) | (uint32_t)j;
                     P.b_gf[c] = (uint32_t)gf;
-                    P.b_z[c] = sz[t];
+                    P.b_z[c] = rd.z;
                     P.b_adh[c] = nb.adh;
                     P.b_sabs[c] = nb.sabs;
                     P.b_dl[c] = (int16_t)((nb.dl & 0xFF) | ((nb.dg & 0xFF) << 8));
@@ -1081,7 +1070,7 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                         fl |= T_GUARD;
                         atomicAdd(&s_pguard[pi], 1);
                     } else {
-                        const TileDraw draw{g.seed, mcs, (uint32_t)gf, sz[t]};
+                        const TileDraw draw{g.seed, mcs, (uint32_t)gf, rd.z};
                         int rr = decide_cells(lsd, nb, P.adh[L], P.adh[G], P.vol, P.itf, L, G, draw);
                         if (rr < 0) rr = decide_exact<NE, uint16_t>(lsd, P.sig, P.adh, P.vol, P.itf, t, L, G, draw) ? 1 : 0;
                         if (rr) {
