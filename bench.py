@@ -20,11 +20,20 @@ attempts per second.
   step is one whole run of the workload's 20,000 MCS window (`--e2e-mcs`).
 * roofline: algorithmic HBM bytes per attempt = 4 + 4*f_acc (sigma read
   once, written on accept) times the attempts of one launch, over the
-  launch's average duration, against the measured copy bandwidth.
+  launch's average duration, against the measured copy bandwidth; and the
+  L2 figure, B_L2 = B_HBM + 16*f_nonnull + 16*f_acc (the two cells' V and I
+  read on non-null attempts, written on accepts), against an L2-resident
+  copy bandwidth measured in the same run.
 * cpu_baseline: the CPU oracle (a restatement of the reference's run_mcs)
   on one host thread over a bounded sample of the same workload.
 * --impl reference: the oracle on every host core (one replica of the
   workload per thread, the reference's run_batch parallelism).
+
+Extra legs in the same line (1 GPU): `c3` (the 128^3 organoid, device and
+end to end), `c1` (the 30x30 quickstart end to end, beside the oracle on one
+thread), `sparse` (the reference's 150x150 proposal-mode case, both modes),
+`batch` (4096 thetas in one call against a loop of single runs) and `serve`
+(the serving loop under Poisson arrivals).
 
 Multi-GPU: the path does not shard within one lattice; under torchrun each
 rank runs an independent replica ("replicas only") and `value` sums them.
@@ -304,7 +313,9 @@ def c3_sim(seed=SEED):
 
 def run_c3_bench(args):
     """Device attempts/s of the 3D organoid (config 3) on the tiled sweep,
-    after a burn-in, CUDA events on the engine stream."""
+    after a burn-in, CUDA events on the engine stream; then (`e2e`) the
+    workload's window, 5000 MCS with a sample every 100, through
+    cpm.CPM(...).run."""
     import torch
 
     from cpm import _cpm
@@ -324,11 +335,28 @@ def run_c3_bench(args):
     s1 = eng.stats()
     att = s1["attempts"] - s0["attempts"]
     assert eng.recount_check()[0]
-    return {"workload": "3D organoid 128^3 periodic, 3 types x 534 cells (phi=0.8), V*=1048 I*=600, 26-neighbour "
-                        "energy, nested-layer placement", "attempts_per_s": att / (ms / 1000.0),
-            "mcs_timed": args.c3_mcs, "after_mcs": args.c3_warmup, "ms": ms,
-            "f_nonnull": (s1["nonnull"] - s0["nonnull"]) / att, "f_acc": (s1["accepted"] - s0["accepted"]) / att,
-            "deferred": s1["deferred"] - s0["deferred"]}
+    out = {"workload": "3D organoid 128^3 periodic, 3 types x 534 cells (phi=0.8), V*=1048 I*=600, 26-neighbour "
+                       "energy, nested-layer placement", "attempts_per_s": att / (ms / 1000.0),
+           "mcs_timed": args.c3_mcs, "after_mcs": args.c3_warmup, "ms": ms,
+           "f_nonnull": (s1["nonnull"] - s0["nonnull"]) / att, "f_acc": (s1["accepted"] - s0["accepted"]) / att,
+           "deferred": s1["deferred"] - s0["deferred"]}
+    del eng
+    if args.c3_e2e_mcs > 0:
+        # the workload's whole window through the public API: placement
+        # checks, upload, the sweep, 50 samples with device topology readouts,
+        # read-back and result assembly
+        sim = c3_sim()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = sim.run(burn_in_mcs=0, readout_mcs=args.c3_e2e_mcs, sampling_interval_mcs=100)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        out["e2e"] = {"value": args.c3_e2e_mcs * 128 ** 3 / dt, "unit": "attempts/s", "seconds": dt,
+                      "samples": len(res.samples), "h2d_bytes": res.stats["h2d_bytes"],
+                      "d2h_bytes": res.stats["d2h_bytes"],
+                      "step": f"cpm.CPM(...).run(burn_in_mcs=0, readout_mcs={args.c3_e2e_mcs}, "
+                              "sampling_interval_mcs=100)"}
+    return out
 
 
 def run_serve_bench(args):
@@ -400,6 +428,144 @@ def run_serve_bench(args):
                      for q, a, m in zip(reqs, alone, lat)],
         "requests_columns": ["D", "side", "MCS", "isolated_s", "in_stream_s"],
     }
+
+
+# --------------------------------------------- quickstart and sparse cases ----
+def c1_public(seed=1):
+    """Config 1, the reference's quickstart (README.md:47-83): 30x30 periodic,
+    one type (V*=50, I*=75, lambda_V=10, lambda_I=2), 5 cells, J=[[0,5],[5,2]],
+    scatter-and-grow placement; copy = connectivity = von Neumann, energy =
+    Moore."""
+    import cpm
+
+    sim = cpm.CPM(grid=(30, 30), boundary="periodic", seed=seed)
+    sim.register_cell_type("epithelial", 50, 75, 10.0, 2.0)
+    sim.add_cells("epithelial", 5)
+    sim.set_adhesion([[0.0, 5.0], [5.0, 2.0]])
+    sim.initialize(warn_on_default_init=False)
+    return sim
+
+
+def sparse_public(proposal, seed=1):
+    """The reference's sparse proposal-mode case (notebooks/performance_demo.ipynb
+    cell 5): 150x150 periodic, 10 cells (V*=30, I*=40, lambda_V=1,
+    lambda_I=0.2), J=[[0,3],[3,1]], von Neumann copy and connectivity."""
+    import cpm
+
+    sim = cpm.CPM(grid=(150, 150), boundary="periodic", seed=seed, copy_neighborhood="von_neumann",
+                  connectivity_neighborhood="von_neumann", proposal=proposal)
+    sim.register_cell_type(name="a", target_volume=30, target_interface=40, lambda_volume=1.0, lambda_interface=0.2)
+    sim.add_cells(cell_type="a", n=10)
+    sim.set_adhesion([[0.0, 3.0], [3.0, 1.0]])
+    sim.initialize(warn_on_default_init=False)
+    return sim
+
+
+def run_c1_bench(args):
+    """Config 1 end to end through cpm.CPM(...).run (5000 burn-in + 5000
+    readout MCS, a sample every 100: the quickstart's window), against the
+    oracle's run of the same window on one host thread."""
+    import torch
+
+    c1_public(2).run(burn_in_mcs=10, readout_mcs=10, sampling_interval_mcs=10)  # warm-up call
+    times = []
+    for i in range(args.c1_runs):
+        sim = c1_public(1 + i)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sim.run(burn_in_mcs=5000, readout_mcs=5000, sampling_interval_mcs=100)
+        times.append(time.perf_counter() - t0)
+    t = sum(times) / len(times)
+    out = {"workload": "quickstart 30x30 periodic, 5 cells (V*=50, I*=75), 5000 + 5000 MCS, a sample every 100, "
+                       "through cpm.CPM(...).run", "runs": args.c1_runs, "seconds_per_run": t,
+           "mcs_per_s": 10000 / t, "attempts_per_s": 10000 * 900 / t,
+           "reference_published_mcs_per_s": {"value": 68579.0, "case": "30x30, 10 cells V*=30, uniform, unstated "
+                                                                           "CPU, one thread "
+                                                                           "(notebooks/performance_demo.ipynb cell 3)"}}
+    if not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+
+        O.build()
+        spec = O.ModelSpec((30, 30), True, [(50, 75, 10.0, 2.0)], [[0, 5], [5, 2]], cell_counts=[5])
+        t0 = time.perf_counter()
+        failed, *_ = O.run_many(spec, [1], burn_in=5000, readout=5000, threads=1, local_halo=True)
+        dt = time.perf_counter() - t0
+        assert failed == 0
+        out["cpu_oracle_mcs_per_s"] = 10000 / dt
+    return out
+
+
+def run_sparse_bench(args):
+    """The sparse proposal-mode case through cpm.CPM(...).run, both proposal
+    modes (2000 MCS, as the reference's notebook times them). The device chain
+    is the same for both: EdgeList is the Uniform chain without its null
+    attempts (edge_list.rs:1-16), and the sweeps skip the draw of every
+    attempt whose copy neighbours all hold its cell."""
+    out = {"workload": "150x150 periodic, 10 cells (V*=30, I*=40), 2000 MCS through cpm.CPM(...).run "
+                       "(notebooks/performance_demo.ipynb cell 5)",
+           "reference_published_mcs_per_s": {"uniform": 2405.6, "edge_list": 80276.3,
+                                             "hardware": "unstated CPU, one thread"}}
+    sparse_public("uniform", 2).run(burn_in_mcs=0, readout_mcs=10, sampling_interval_mcs=10)
+    for prop in ("uniform", "edge_list"):
+        sim = sparse_public(prop)
+        t0 = time.perf_counter()
+        sim.run(burn_in_mcs=0, readout_mcs=2000, sampling_interval_mcs=2000)
+        out[f"{prop}_mcs_per_s"] = 2000 / (time.perf_counter() - t0)
+    if not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+
+        spec = O.ModelSpec((150, 150), True, [(30, 40, 1.0, 0.2)], [[0, 3], [3, 1]], cell_counts=[10])
+        t0 = time.perf_counter()
+        failed, *_ = O.run_many(spec, [1], burn_in=2000, readout=0, threads=1, local_halo=True)
+        assert failed == 0
+        out["cpu_oracle_uniform_mcs_per_s"] = 2000 / (time.perf_counter() - t0)
+    return out
+
+
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        p = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10)
+        for line in p.stdout.splitlines():
+            if line.strip().startswith("Model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return "unknown"
+
+
+def l2_copy_gbs():
+    """L2-resident copy bandwidth of this GPU, measured here: two 32 MB
+    buffers (together half the 129 MB L2) copied back and forth, read +
+    write bytes over CUDA-event time, best of 5 bursts of 50 copies."""
+    import torch
+
+    n = 32 * 1024 * 1024 // 4
+    a = torch.ones(n, dtype=torch.float32, device="cuda")
+    b = torch.empty_like(a)
+    for _ in range(20):
+        b.copy_(a)
+    best = 0.0
+    for _ in range(5):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(25):
+            b.copy_(a)
+            a.copy_(b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 50 * 2 * n * 4 / (e0.elapsed_time(e1) / 1000.0) / 1e9)
+    return best
 
 
 # --------------------------------------------------------------- clocks ----
@@ -527,6 +693,7 @@ def run_reference(args, rank, world):
         "data": "synthetic (seeded scatter-and-grow placement)",
         "config": dict(workload_config(), sample=f"{threads} replicas x {mcs} MCS per step (incl. placement)"),
         "cpu_baseline": {"value": value, "unit": "attempts/s", "cores": threads, "kind": "port",
+                         "cpu_model": cpu_model(),
                          "sample": f"{threads} threads, one replica each, {mcs} MCS per step"},
         "e2e": {"value": value, "unit": "attempts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -557,7 +724,7 @@ def cpu_baseline(args):
     sim.run_mcs(args.cpu_mcs)
     dt = time.perf_counter() - t0
     att = args.cpu_mcs * GRID[0] * GRID[1]
-    return {"value": att / dt, "unit": "attempts/s", "cores": 1, "kind": "port",
+    return {"value": att / dt, "unit": "attempts/s", "cores": 1, "kind": "port", "cpu_model": cpu_model(),
             "sample": f"{args.cpu_mcs} MCS of the same 512x512 lattice from the same placement, one thread"}
 
 
@@ -611,6 +778,11 @@ def run_gpu(args, rank, world, dist):
     achieved = bytes_per_attempt * (attempts / args.steps) / launch_s / 1e9
     peaks, src = measured_peaks()
     traffic_launch = profiled_traffic(args.mcs_per_step)
+    # the L2 figure: B_L2 = B_HBM + 16 f_nonnull + 16 f_acc bytes per attempt
+    # (V and I of both cells read on non-null attempts, written on accepts)
+    l2_bytes = bytes_per_attempt + 16.0 * f_nonnull + 16.0 * f_acc
+    l2_achieved = l2_bytes * (attempts / args.steps) / launch_s / 1e9
+    l2_peak = l2_copy_gbs() if rank == 0 else None
 
     # ---- e2e through the public API (host buffers, copies inside the timed region)
     e2e = None
@@ -663,6 +835,11 @@ def run_gpu(args, rank, world, dist):
             "traffic": traffic_launch,
             "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)" if src == "measured" else "fallback",
             "algorithmic_bytes_per_attempt": bytes_per_attempt,
+            "l2_bytes_per_attempt": l2_bytes,
+            "l2_achieved": l2_achieved,
+            "l2_peak": l2_peak,
+            "l2_peak_source": "measured in this run: L2-resident copy between two 32 MB buffers (read + write bytes)",
+            "l2_frac": l2_achieved / l2_peak if l2_peak else None,
         },
         "stats": {"f_nonnull": f_nonnull, "f_acc": f_acc,
                   "rounds_per_pass": (s1["rounds"] - s0["rounds"]) / max(1, s1["passes"] - s0["passes"]),
@@ -673,6 +850,10 @@ def run_gpu(args, rank, world, dist):
         line["cpu_baseline"] = cpu_baseline(args)
     if args.c3_mcs > 0 and world == 1:
         line["c3"] = run_c3_bench(args)
+    if args.c1_runs > 0 and world == 1:
+        line["c1"] = run_c1_bench(args)
+    if not args.no_sparse and world == 1:
+        line["sparse"] = run_sparse_bench(args)
     if args.batch_n > 0:
         line["batch"] = run_batch_bench(args)
     if args.serve_n > 0:
@@ -697,6 +878,10 @@ def main():
                     help="burn-in,readout,interval MCS of each batch member")
     ap.add_argument("--c3-mcs", type=int, default=100, help="timed MCS of the 3D organoid case (0 skips it)")
     ap.add_argument("--c3-warmup", type=int, default=100, help="MCS run before the timed 3D MCS")
+    ap.add_argument("--c3-e2e-mcs", type=int, default=5000,
+                    help="MCS of the 3D organoid's end-to-end run through cpm.CPM.run (0 skips it)")
+    ap.add_argument("--c1-runs", type=int, default=3, help="end-to-end runs of the quickstart (0 skips them)")
+    ap.add_argument("--no-sparse", action="store_true", help="skip the sparse proposal-mode case")
     ap.add_argument("--serve-n", type=int, default=16, help="requests of the serving workload (0 skips it)")
     ap.add_argument("--serve-rate", type=float, default=1.0,
                     help="Poisson arrival rate of the requests (1/s); the workload's nominal 200/s offers ~100x what "

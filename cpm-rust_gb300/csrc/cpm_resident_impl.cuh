@@ -90,6 +90,9 @@ __host__ __device__ inline ResLayout res_layout(int64_t n_padded, int n_cells, i
 
 struct PassInfoR {
     int cnt[3], base[3], step[3], n;
+    // a reciprocal of cnt: idx / cnt == (idx * mg) >> 32 whenever
+    // idx * cnt < 2^32 (every class index of a resident lattice)
+    unsigned long long mg[3];
 };
 
 __device__ __forceinline__ void make_pass_r(const SimDesc& s, int color, PassInfoR& p) {
@@ -103,6 +106,9 @@ __device__ __forceinline__ void make_pass_r(const SimDesc& s, int color, PassInf
         p.n *= p.cnt[d];
     }
     for (int d = s.D; d < 3; ++d) { p.cnt[d] = 1; p.base[d] = 0; p.step[d] = 0; }
+    // (2^32 - 1) / cnt + 1 equals floor(2^32 / cnt) + 1 unless cnt is a power
+    // of two, where it is 2^32 / cnt exactly: both give exact quotients
+    for (int d = 0; d < 3; ++d) p.mg[d] = p.cnt[d] > 0 ? (unsigned long long)(0xFFFFFFFFu / (unsigned)p.cnt[d]) + 1ull : 0ull;
 }
 
 template <int D>
@@ -110,8 +116,9 @@ __device__ __forceinline__ int site_r(const SimDesc& s, const PassInfoR& p, int 
     int f = 0;
 #pragma unroll
     for (int d = D - 1; d >= 0; --d) {
-        const int i = idx % p.cnt[d];
-        idx /= p.cnt[d];
+        const int q = (int)(((unsigned long long)(unsigned)idx * p.mg[d]) >> 32);
+        const int i = idx - q * p.cnt[d];
+        idx = q;
         x[d] = p.base[d] + p.step[d] * i;
         f += (x[d] + 1) * (int)s.strides[d];
     }
