@@ -740,7 +740,10 @@ def run_gpu(args, rank, world, dist):
     n_sites = GRID[0] * GRID[1]
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
-    for _ in range(args.warmup):
+    # the first warm-up call is long enough for the grid tuner's trial
+    # launches (the tuned grid is then used by every later launch)
+    eng.run_mcs(max(args.mcs_per_step, 100))
+    for _ in range(args.warmup - 1):
         eng.run_mcs(args.mcs_per_step)
     torch.cuda.synchronize()
     s0 = eng.stats()
@@ -850,6 +853,9 @@ def run_gpu(args, rank, world, dist):
         line["cpu_baseline"] = cpu_baseline(args)
     if args.c3_mcs > 0 and world == 1:
         line["c3"] = run_c3_bench(args)
+    # the tiled sweep's grid tuner: candidate grids timed on each shape's
+    # first MCS (microseconds per MCS) and the grid in use
+    line["tuning"] = _cpm.tuning_report()
     if args.c1_runs > 0 and world == 1:
         line["c1"] = run_c1_bench(args)
     if not args.no_sparse and world == 1:

@@ -925,6 +925,17 @@ extern "C" int cpm_builder_hashes(const cpm_builder* b, uint64_t burn, uint64_t 
 
 extern "C" uint64_t cpm_derive_seed_u64(uint64_t master, uint64_t index) { return derive_seed_u64(master, index); }
 
+extern "C" int cpm_tuning_report(char* buf, size_t capacity, size_t* needed) {
+    const std::string r = tuning_report();
+    if (needed) *needed = r.size() + 1;
+    if (buf && capacity > 0) {
+        const size_t n = std::min(capacity - 1, r.size());
+        std::memcpy(buf, r.data(), n);
+        buf[n] = 0;
+    }
+    return ok();
+}
+
 extern "C" int cpm_run_status(const double* energy_trace, size_t n_trace, size_t n_samples, const uint64_t* sample_mcs,
                               uint32_t n_cells, const uint32_t* volumes, const uint32_t* first_fragmented,
                               const uint32_t* last_contact_pairs, size_t n_pairs, uint32_t min_cell_volume,

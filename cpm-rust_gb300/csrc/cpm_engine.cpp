@@ -10,6 +10,7 @@
 #include "cpm_engine.h"
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <chrono>
 #include <cmath>
@@ -422,6 +423,57 @@ DeviceSims::Path DeviceSims::path(size_t i) const {
     return tiled_ok && !modes ? TILED : GLOBAL;
 }
 
+// ------------------------------------------------------ grid tuner ----
+// The tiled sweep's grid (how many CTAs share the tiles of a colour) is the
+// one launch parameter the trajectory does not depend on: tiles, claims and
+// priorities are functions of (seed, MCS, tile id). The tuner times it on
+// the simulation's own first MCS: while a shape has no choice yet, the run
+// starts with short trial launches of each candidate grid (one, two, three
+// and four tiles per CTA), each twice, bracketed by CUDA events; then it
+// waits for them, keeps the fastest per MCS for the rest of the run and for
+// every later run of the same shape in the process. The trials are MCS the
+// run performs anyway, so tuning changes no result.
+namespace {
+struct TuneEntry {
+    std::vector<int> cand;
+    std::vector<double> us_per_mcs;  // best measurement per candidate
+    int chosen = 0;
+    bool done = false;
+};
+std::mutex g_tune_mu;
+std::map<std::array<int, 8>, TuneEntry>& tune_table() {
+    static std::map<std::array<int, 8>, TuneEntry> t;
+    return t;
+}
+}  // namespace
+
+std::string tuning_report() {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    std::string o = "[";
+    bool first = true;
+    for (auto& kv : tune_table()) {
+        const auto& k = kv.first;
+        const TuneEntry& e = kv.second;
+        if (!first) o += ",";
+        first = false;
+        o += "{\"dim\":" + std::to_string(k[0]) + ",\"energy_neighbours\":" + std::to_string(k[1]) +
+             ",\"odd\":" + std::to_string(k[2]) + ",\"tiles_per_axis\":[" + std::to_string(k[3]) + "," +
+             std::to_string(k[4]) + "," + std::to_string(k[5]) + "],\"tiles_per_colour\":" + std::to_string(k[6]) +
+             ",\"done\":" + (e.done ? "true" : "false") + ",\"grid\":" + std::to_string(e.chosen) +
+             ",\"candidates\":[";
+        for (size_t i = 0; i < e.cand.size(); ++i) {
+            // untimed candidates (a shape whose runs were too short for the
+            // trials) report -1
+            const double us = i < e.us_per_mcs.size() && e.us_per_mcs[i] < 1e200 ? e.us_per_mcs[i] : -1.0;
+            char b[96];
+            std::snprintf(b, sizeof b, "%s[%d,%.3f]", i ? "," : "", e.cand[i], us);
+            o += b;
+        }
+        o += "]}";
+    }
+    return o + "]";
+}
+
 // One simulation on the tiled sweep: the run window is replayed from the
 // host, one cooperative launch per chunk plus energy and sample launches.
 std::string DeviceSims::run_tiled(const RunPlan& p, const uint64_t* t3) {
@@ -451,9 +503,34 @@ std::string DeviceSims::run_tiled(const RunPlan& p, const uint64_t* t3) {
     int grid = std::max(1, std::min(tiles >> L.g.D, std::max(1, per_sm) * sms));
     // CPM_GPU_TILED_GRID caps the grid (several tiles per CTA); the tiling,
     // and so the trajectory, does not depend on it
-    if (const char* cap = std::getenv("CPM_GPU_TILED_GRID")) grid = std::max(1, std::min(grid, std::atoi(cap)));
+    const char* grid_env = std::getenv("CPM_GPU_TILED_GRID");
+    if (grid_env) grid = std::max(1, std::min(grid, std::atoi(grid_env)));
     if (tiled_grid_cap_ > 0) grid = std::max(1, std::min(grid, tiled_grid_cap_));
     if ((tiles >> L.g.D) > 511 * grid) return "tiled sweep: too many tiles per CTA for this lattice";
+    // the tuner's entry for this shape (none when the grid is set from
+    // outside: the environment, a serving cap, or CPM_GPU_NO_TUNE)
+    const int per_color = tiles >> L.g.D;
+    const std::array<int, 8> tkey = {L.g.D, L.NE, odd, nt[0], L.g.D > 1 ? nt[1] : 1, L.g.D > 2 ? nt[2] : 1,
+                                     per_color, (int)smem};
+    const bool tune = !grid_env && tiled_grid_cap_ <= 0 && !std::getenv("CPM_GPU_NO_TUNE");
+    std::vector<int> trials;  // grids still to time in this run, in order
+    if (tune) {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        TuneEntry& te = tune_table()[tkey];
+        if (te.cand.empty()) {
+            for (int k = 1; k <= 4; ++k) {
+                const int g = (per_color + k - 1) / k;
+                if (g < 1 || g > grid || per_color > 511 * g) continue;
+                if (std::find(te.cand.begin(), te.cand.end(), g) == te.cand.end()) te.cand.push_back(g);
+            }
+            te.us_per_mcs.assign(te.cand.size(), 1e300);
+            te.chosen = grid;
+        }
+        if (te.done) grid = te.chosen;
+        else if (te.cand.size() > 1)
+            for (int rep = 0; rep < 2; ++rep) trials.insert(trials.end(), te.cand.begin(), te.cand.end());
+    }
+    const int grid_max = grid;  // the largest grid any launch of this run uses
     // CPM_GPU_TEST_BARRIER_TIMEOUT (tests only): the grid barrier waits for
     // one CTA more than the grid has, so every bounded wait runs out, the
     // kernel records the timeout and returns; nothing else changes
@@ -461,7 +538,7 @@ std::string DeviceSims::run_tiled(const RunPlan& p, const uint64_t* t3) {
     if (!d_bar_) CUDA_TRY(dev_alloc(&d_bar_, 64));
     // each CTA's cell registry in HBM (when it is not in shared memory): a
     // stamp and a box slot per cell id
-    const size_t reg = reg_smem ? 0 : 2 * (size_t)grid * (size_t)(L.n_cells + 1) * 4;
+    const size_t reg = reg_smem ? 0 : 2 * (size_t)grid_max * (size_t)(L.n_cells + 1) * 4;
     if (reg > reg_cap_) {
         if (d_reg_) dev_free(d_reg_);
         d_reg_ = nullptr;
@@ -472,15 +549,51 @@ std::string DeviceSims::run_tiled(const RunPlan& p, const uint64_t* t3) {
     }
     SimDesc* d_sim = d_descs_ + p.sim;
     unsigned long long* claims = descs_[p.sim].slots;
+    auto launch = [&](uint64_t m, int g) -> cudaError_t {
+        cudaError_t e = cudaMemsetAsync(d_bar_, 0, 64, stream_);
+        if (e == cudaSuccess)
+            e = cpmgpu::launch_tiled(L.g.D, L.NE, odd, d_sim, m, nt, d_bar_, claims, reg_smem ? nullptr : d_reg_, t3,
+                                     max_box, tables_in_smem, barrier_extra, cl_cap, reg_smem, smem, g, stream_,
+                                     L.n_cells);
+        return e;
+    };
+    // trial launches of TRIAL_MCS each (3D MCS cost more: fewer)
+    const uint64_t TRIAL_MCS = L.g.D == 2 ? 8 : 4;
     auto chunk = [&](uint64_t n) -> std::string {
+        if (!trials.empty() && n >= TRIAL_MCS * trials.size() + 1) {
+            std::vector<cudaEvent_t> ev(trials.size() + 1);
+            for (auto& x : ev) CUDA_TRY(cudaEventCreate(&x));
+            CUDA_TRY(cudaEventRecord(ev[0], stream_));
+            for (size_t i = 0; i < trials.size(); ++i) {
+                CUDA_TRY(launch(TRIAL_MCS, trials[i]));
+                CUDA_TRY(cudaEventRecord(ev[i + 1], stream_));
+            }
+            n -= TRIAL_MCS * trials.size();
+            CUDA_TRY(cudaEventSynchronize(ev.back()));
+            {
+                std::lock_guard<std::mutex> lk(g_tune_mu);
+                TuneEntry& te = tune_table()[tkey];
+                for (size_t i = 0; i < trials.size(); ++i) {
+                    float ms = 0.f;
+                    CUDA_TRY(cudaEventElapsedTime(&ms, ev[i], ev[i + 1]));
+                    const size_t c = std::find(te.cand.begin(), te.cand.end(), trials[i]) - te.cand.begin();
+                    te.us_per_mcs[c] = std::min(te.us_per_mcs[c], 1000.0 * ms / (double)TRIAL_MCS);
+                }
+                size_t best = 0;
+                for (size_t c = 1; c < te.cand.size(); ++c)
+                    if (te.us_per_mcs[c] < te.us_per_mcs[best]) best = c;
+                te.chosen = te.cand[best];
+                te.done = true;
+                grid = te.chosen;
+            }
+            for (auto& x : ev) cudaEventDestroy(x);
+            trials.clear();
+        }
         // at most 2^18 MCS per launch: the barrier counter (32 bits) grows by
         // grid x 2 x colours per MCS within a launch
         while (n > 0) {
             const uint64_t m = std::min<uint64_t>(n, 1ull << 18);
-            CUDA_TRY(cudaMemsetAsync(d_bar_, 0, 64, stream_));
-            CUDA_TRY(cpmgpu::launch_tiled(L.g.D, L.NE, odd, d_sim, m, nt, d_bar_, claims, reg_smem ? nullptr : d_reg_,
-                                          t3, max_box, tables_in_smem, barrier_extra, cl_cap, reg_smem, smem, grid,
-                                          stream_, L.n_cells));
+            CUDA_TRY(launch(m, grid));
             n -= m;
         }
         return "";

@@ -155,6 +155,11 @@ struct Result {
 Status run_status(uint32_t min_cell_volume, const std::vector<double>& trace, const std::vector<Sample>& samples,
                   int n_cells, bool have_topology);
 
+// The tiled sweep's grid tuner: its table as JSON text (one object per
+// lattice shape: the candidate grids with their best time per MCS in
+// microseconds, and the grid chosen).
+std::string tuning_report();
+
 // Readout knobs: what each sample carries besides the per-cell summary.
 struct ReadoutOptions {
     bool include_lattice = false;  // Sample.lattice

@@ -168,7 +168,7 @@ EXPORTED_SYMBOLS = (
     "cpm_engine_evaluate_moves", "cpm_engine_commit_moves", "cpm_engine_take_sample", "cpm_engine_write_act_state",
     "cpm_engine_read_birth", "cpm_engine_destroy",
     "cpm_run_many",
-    "cpm_builder_initial_state", "cpm_builder_hashes", "cpm_derive_seed_u64", "cpm_run_status",
+    "cpm_builder_initial_state", "cpm_builder_hashes", "cpm_derive_seed_u64", "cpm_run_status", "cpm_tuning_report",
     "cpm_run_mcs_noalloc",
     "cpm_serve_start", "cpm_serve_submit", "cpm_serve_poll", "cpm_serve_wait", "cpm_serve_cancel",
     "cpm_serve_stats_get", "cpm_serve_stop", "cpm_result_samples_sizes", "cpm_result_samples_read",
@@ -235,6 +235,7 @@ def _load():
     L.cpm_builder_hashes.argtypes = [_P, U64, U64, U64, _P, SZ, _P, SZ, ctypes.c_char_p, ctypes.c_char_p]
     L.cpm_derive_seed_u64.argtypes = [U64, U64]
     L.cpm_derive_seed_u64.restype = U64
+    L.cpm_tuning_report.argtypes = [ctypes.c_char_p, SZ, ctypes.POINTER(SZ)]
     L.cpm_run_status.argtypes = [_P, SZ, SZ, _P, ctypes.c_uint32, _P, _P, _P, SZ, ctypes.c_uint32, _P, _P, _P]
     L.cpm_result_samples_sizes.argtypes = [_P, _P]
     L.cpm_result_samples_read.argtypes = [_P, _P]
@@ -668,6 +669,17 @@ def derive_seed_u64(master_seed: int, index: int) -> int:
 
 
 STATUS_KINDS = ("Ok", "NotEquilibrated", "Fragmented", "CellLost", "Degenerate")
+
+
+def tuning_report():
+    """The tiled sweep's grid tuner table (``cpm_tuning_report``), parsed."""
+    import json
+
+    need = ctypes.c_size_t(0)
+    _check(_lib.cpm_tuning_report(None, 0, ctypes.byref(need)))
+    buf = ctypes.create_string_buffer(int(need.value) + 1)
+    _check(_lib.cpm_tuning_report(buf, len(buf), ctypes.byref(need)))
+    return json.loads(buf.value.decode())
 
 
 def run_status(trace, sample_mcs, volumes, first_fragmented=None, last_pairs=(), min_cell_volume=1):

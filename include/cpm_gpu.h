@@ -295,6 +295,13 @@ int cpm_builder_hashes(const cpm_builder* b, uint64_t burn_in_mcs, uint64_t read
                        char* convention_hash_out, char* model_hash_out);
 /* rng.rs:37-40: first 8 LE bytes of BLAKE3(master LE || index LE). */
 uint64_t cpm_derive_seed_u64(uint64_t master_seed, uint64_t simulation_index);
+/* No counterpart in the reference (it has no launch parameters). The tiled
+ * sweep's grid tuner: for every lattice shape it has met in this process,
+ * the grids it timed (tiles per CTA 1..4; the trajectory does not depend on
+ * the grid), their best time per MCS in microseconds and the grid in use, as
+ * JSON text. *needed receives the length plus one; the text is cut to fit
+ * `capacity`. */
+int cpm_tuning_report(char* buf, size_t capacity, size_t* needed);
 /* The run status of output.rs:456-522 (SimulationStatus, with the priority
  * NotEquilibrated > Fragmented > CellLost > Degenerate) over given readouts:
  * the burn-in energy trace (not_equilibrated, output.rs:388-420), then per

@@ -382,6 +382,43 @@ def test_tiled_sweep_independent_of_grid(D, cuda_required, monkeypatch):
 
 
 
+def test_grid_tuner_trials_leave_the_trajectory_unchanged(cuda_required, monkeypatch):
+    """The tiled sweep's grid tuner times its candidate grids on the run's own
+    first MCS (short trial launches, each candidate twice) and keeps the
+    fastest: the run equals one with the grid fixed, and one with tuning off.
+    The 132x120 shape is used by no other test, so this process has not tuned
+    it yet."""
+    from cpm import _cpm
+
+    monkeypatch.setenv("CPM_GPU_FORCE_TILED", "1")
+    model = sorting_model(side=64, seed=21)
+    model = Model((132, 120), "periodic", model.types, model.adhesion, [60] * 4, seed=21)
+    n = 100
+    tuned = _engine(model)
+    tuned.run_mcs(n)
+    tuned.synchronize()
+    rep = [e for e in _cpm.tuning_report() if e["dim"] == 2 and e["done"] and e["tiles_per_axis"][:2] == [8, 8]
+           and len(e["candidates"]) > 1]
+    assert rep, _cpm.tuning_report()
+    grid = rep[0]["grid"]
+    assert grid in [c[0] for c in rep[0]["candidates"]]
+    assert all(c[1] > 0 for c in rep[0]["candidates"])
+    others = []
+    monkeypatch.setenv("CPM_GPU_NO_TUNE", "1")
+    others.append(_engine(model))
+    monkeypatch.setenv("CPM_GPU_TILED_GRID", "5")
+    others.append(_engine(model))
+    for e in others:
+        e.run_mcs(n)
+        e.synchronize()
+        assert np.array_equal(tuned.lattice(), e.lattice())
+        a, b = tuned.stats(), e.stats()
+        for k in ("attempts", "nonnull", "accepted", "evaluated", "deferred"):
+            assert a[k] == b[k], (k, a[k], b[k])
+        assert np.array_equal(tuned.cells()[2], e.cells()[2])
+    assert tuned.recount_check()[0]
+
+
 def test_tiled_barrier_timeout_is_reported_and_the_context_survives(cuda_required, monkeypatch):
     """The grid barrier's bounded wait: with a barrier that waits for one CTA
     more than the grid has (test hook), every CTA gives up after its time
