@@ -109,7 +109,9 @@ struct SimDesc {
     int32_t no_connectivity;
     // ---- state ----
     int32_t n_cells;
-    int32_t pad0;
+    // bit 0: the resident sweep builds every site of a chunk (no
+    // active-block skip; same result); a test switch (CPM_GPU_NO_SKIP)
+    int32_t sweep_flags;
     uint32_t* sigma;                // n_padded
     const uint16_t* adh_of;         // per id: type + 1 (0 for medium)
     uint32_t* volume;               // per id

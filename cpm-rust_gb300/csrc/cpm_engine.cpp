@@ -123,6 +123,7 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
     // Skips the connectivity check of every attempt, on the global-memory
     // sweep (the exact-Boltzmann test; never set in production).
     no_connectivity_ = std::getenv("CPM_GPU_TEST_NO_CONNECTIVITY") != nullptr;
+    no_skip_ = std::getenv("CPM_GPU_NO_SKIP") != nullptr;
     prefer_tiled_ = std::getenv("CPM_GPU_PREFER_TILED") != nullptr;
     const size_t N = configs.size();
     layouts_.resize(N);
@@ -300,6 +301,7 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
         s.n_sites = L.g.n_sites;
         s.n_padded = L.g.n_padded;
         s.no_connectivity = no_connectivity_ ? 1 : 0;
+        s.sweep_flags = no_skip_ ? 1 : 0;
         s.n_colors = 1;
         s.max_class = 1;
         for (int d = 0; d < 3; ++d) {

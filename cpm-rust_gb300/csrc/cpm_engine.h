@@ -120,6 +120,7 @@ class DeviceSims {
     bool force_global_ = false;
     bool force_tiled_ = false;
     bool no_connectivity_ = false;
+    bool no_skip_ = false;        // CPM_GPU_NO_SKIP: the resident sweep builds every site
     bool prefer_tiled_ = false;
     void* d_bar_ = nullptr;
     uint32_t* d_reg_ = nullptr;  // tiled sweep: per-CTA cell registries

@@ -48,6 +48,20 @@ struct ResCfg {
     static constexpr int CHUNK = BS == 512 ? 8192 : 4096;  // sites per chunk (halved while a chunk overflows CMAX)
 };
 
+// Active blocks: the lattice is cut into blocks of ABS^D sites (8 x 8 in
+// 2D, 4 x 4 x 4 in 3D); a block is active when one of its sites may hold a
+// non-null attempt (a copy neighbour with another cell). A bitmap of at
+// most ACT_MAX blocks lives in shared memory; lattices with more blocks
+// always take the plain build.
+constexpr int ACT_WORDS = 64;
+constexpr int ACT_MAX = ACT_WORDS * 32;
+template <int D>
+struct ActGeom {
+    static constexpr int B = D == 2 ? 8 : 4;          // block side
+    static constexpr int S = D == 2 ? 16 : 8;         // sites of one colour class in a block ((B/2)^D)
+    static constexpr int SH = D == 2 ? 2 : 1;         // log2(B/2): sub-index bits per axis
+};
+
 // flag bits of a candidate
 enum : uint32_t {
     F_K = 7u,           // copy direction (bits 0..2)
@@ -209,6 +223,52 @@ struct Resident {
     const uint64_t* t3;
     int* s_n;
     int* s_flag;
+    uint32_t* act;  // active-block bitmap (ACT_WORDS words)
+    int* apfx;      // active blocks before each bitmap word (ACT_WORDS + 1)
+    int nb[3];      // blocks per axis (0: the lattice has more than ACT_MAX blocks)
+
+    __device__ __forceinline__ int block_of(const int* x) const {
+        constexpr int B = ActGeom<D>::B;
+        int b = 0;
+#pragma unroll
+        for (int d = 0; d < D; ++d) b = b * nb[d] + x[d] / B;
+        return b;
+    }
+    __device__ __forceinline__ void mark(const int* x) { const int b = block_of(x); atomicOr(&act[b >> 5], 1u << (b & 31)); }
+    // After sigma[x] changed: x and its copy neighbours may now have a
+    // non-null attempt (periodic neighbours wrap; fixed ones outside are the
+    // medium halo, which never changes).
+    __device__ void mark_around(const int* x) {
+        if (nb[0] == 0) return;
+        mark(x);
+        for (int d = 0; d < D; ++d)
+            for (int sg = -1; sg <= 1; sg += 2) {
+                int y[3] = {x[0], D > 1 ? x[1] : 0, D > 2 ? x[2] : 0};
+                y[d] += sg;
+                if (y[d] < 0 || y[d] >= s.dims[d]) {
+                    if (!s.periodic) continue;
+                    y[d] = y[d] < 0 ? s.dims[d] - 1 : 0;
+                }
+                mark(y);
+            }
+    }
+    // Rebuilds the bitmap from sigma (every thread; ends with a barrier).
+    __device__ void rescan() {
+        if (nb[0] == 0) return;
+        for (int w = threadIdx.x; w < ACT_WORDS; w += RB) act[w] = 0u;
+        __syncthreads();
+        for (int q = threadIdx.x; q < (int)s.n_sites; q += RB) {
+            int x[3] = {0, 0, 0}, r = q, f = 0;
+#pragma unroll
+            for (int d = D - 1; d >= 0; --d) {
+                x[d] = r % s.dims[d];
+                r /= s.dims[d];
+                f += (x[d] + 1) * (int)s.strides[d];
+            }
+            if (!copy_uniform(s, sig, f, (uint32_t)sig[f])) mark(x);
+        }
+        __syncthreads();
+    }
 
     // Evaluate candidate c on the current state (guard, Delta-H, Metropolis).
     __device__ void evaluate(int c, uint64_t mcs) {
@@ -254,6 +314,7 @@ struct Resident {
         }
         if (L) dirty[L] = 1;
         if (G) dirty[G] = 1;
+        mark_around(x);
     }
 
     // The same outcome as resolve() for n <= 32 (K = 1) or n <= 64 (K = 2)
@@ -491,8 +552,51 @@ struct Resident {
         __syncthreads();
     }
 
-    // One colour pass: chunks of the class in index order.
+    // Site j of a chunk (class index start + j) at padded index t: the
+    // early-out (the draw only when a copy neighbour differs), the
+    // connectivity test; a candidate keeps its copy direction in k.
+    __device__ __forceinline__ bool try_site(int t, uint64_t mcs, int& k, uint32_t& L, uint32_t& G,
+                                             unsigned long long& nonnull, unsigned long long& topo) {
+        L = sig[t];
+        G = L;
+        // every copy neighbour holds the target's cell: null whatever the
+        // copy direction (the draw is skipped)
+        if (!copy_uniform(s, sig, t, L)) {
+            const uint4 r = site_draw(s.seed, mcs, (uint32_t)t);
+            k = (int)(((unsigned long long)r.x * (unsigned)s.n_copy) >> 32);
+            G = sig[t + (int)s.copy_off[k]];
+        }
+        if (L == G) return false;
+        ++nonnull;
+        if (preserves_topology<D, uint16_t>(s, sig, t, L, s.table2d, t3)) return true;
+        ++topo;
+        return false;
+    }
+    __device__ __forceinline__ void add_candidate(bool cand, int j, int t, int k, uint32_t L, uint32_t G,
+                                                  uint32_t pass_key) {
+        const int lane = threadIdx.x & 31;
+        const unsigned m = __ballot_sync(0xffffffffu, cand);
+        int base = 0;
+        if (lane == 0 && m) base = atomicAdd(s_n, __popc(m));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (cand) {
+            const int pos = base + __popc(m & ((1u << lane) - 1));
+            if (pos < CMAX) {
+                c_site[pos] = (uint32_t)t;
+                c_cells[pos] = L | (G << 16);
+                c_key[pos] = (mix32((uint32_t)j * 0x9E3779B9u ^ pass_key) & 0xFFFFC000u) | (uint32_t)j;
+                c_flags[pos] = (uint32_t)k | F_PEND;
+            }
+        }
+    }
+
+    // One colour pass: chunks of the class in index order. A chunk whose
+    // active blocks hold fewer than half its sites visits only their sites
+    // of the class: every other site has copy neighbours of its own cell,
+    // a null attempt that neither draws nor counts, so the candidates (and
+    // their keys, from the class index) are those of the plain build.
     __device__ void pass(const PassInfoR& p, uint64_t mcs, uint32_t pass_key, CountersR& ct) {
+        constexpr int B = ActGeom<D>::B, S = ActGeom<D>::S, SH = ActGeom<D>::SH;
         const int tid = threadIdx.x;
         const int lane = tid & 31;
         int start = 0;
@@ -500,51 +604,85 @@ struct Resident {
             int len = min(CHUNK, p.n - start);
             for (;;) {
                 const long long t0 = clock64();
+                int nact = 0;
+                if (nb[0] > 0)
+                    nact = __reduce_add_sync(0xffffffffu, (unsigned)(__popc(act[lane]) + __popc(act[lane + 32])));
                 if (tid == 0) *s_n = 0;
                 __syncthreads();
                 unsigned long long nonnull = 0, topo = 0;
-                for (int j0 = 0; j0 < len; j0 += RB) {
-                    const int j = j0 + tid;
-                    bool cand = false;
-                    int t = 0, k = 0;
-                    uint32_t L = 0, G = 0;
-                    if (j < len) {
-                        int x[3];
-                        t = site_r<D>(s, p, start + j, x);
-                        L = sig[t];
-                        G = L;
-                        // every copy neighbour holds the target's cell: null
-                        // whatever the copy direction (the draw is skipped)
-                        if (!copy_uniform(s, sig, t, L)) {
-                            const uint4 r = site_draw(s.seed, mcs, (uint32_t)t);
-                            k = (int)(((unsigned long long)r.x * (unsigned)s.n_copy) >> 32);
-                            G = sig[t + (int)s.copy_off[k]];
+                if (nb[0] > 0 && 2 * nact * S < len) {
+                    // the sites of the active blocks, spread over all
+                    // threads: item q is site q % S of the (q / S)-th active
+                    // block in bitmap order (word prefix sums in apfx)
+                    if (tid < 32) {
+                        const int c0 = __popc(act[lane]), c1 = __popc(act[lane + 32]);
+                        int i0 = c0, i1 = c1;
+                        for (int o = 1; o < 32; o <<= 1) {
+                            const int y0 = __shfl_up_sync(0xffffffffu, i0, o), y1 = __shfl_up_sync(0xffffffffu, i1, o);
+                            if (lane >= o) { i0 += y0; i1 += y1; }
                         }
-                        if (L != G) {
-                            ++nonnull;
-                            if (preserves_topology<D, uint16_t>(s, sig, t, L, s.table2d, t3)) cand = true;
-                            else ++topo;
-                        }
+                        const int tot0 = __shfl_sync(0xffffffffu, i0, 31);
+                        apfx[lane] = i0 - c0;
+                        apfx[lane + 32] = tot0 + i1 - c1;
+                        if (lane == 31) apfx[64] = tot0 + i1;
                     }
-                    const unsigned m = __ballot_sync(0xffffffffu, cand);
-                    int base = 0;
-                    if (lane == 0 && m) base = atomicAdd(s_n, __popc(m));
-                    base = __shfl_sync(0xffffffffu, base, 0);
-                    if (cand) {
-                        const int pos = base + __popc(m & ((1u << lane) - 1));
-                        if (pos < CMAX) {
-                            c_site[pos] = (uint32_t)t;
-                            c_cells[pos] = L | (G << 16);
-                            c_key[pos] = (mix32((uint32_t)j * 0x9E3779B9u ^ pass_key) & 0xFFFFC000u) | (uint32_t)j;
-                            c_flags[pos] = (uint32_t)k | F_PEND;
+                    __syncthreads();
+                    const int total = apfx[64] * S;
+                    for (int q0 = 0; q0 < total; q0 += RB) {
+                        const int q = q0 + tid;
+                        bool cand = false, valid = q < total;
+                        int t = 0, k = 0, jj = 0;
+                        uint32_t L = 0, G = 0;
+                        if (valid) {
+                            const int a = q / S, sub = q % S;
+                            int lo = 0, hi = ACT_WORDS - 1;  // the word holding active block a
+                            while (lo < hi) {
+                                const int mid = (lo + hi + 1) >> 1;
+                                if (apfx[mid] <= a) lo = mid; else hi = mid - 1;
+                            }
+                            int blk = lo * 32 + (int)__fns(act[lo], 0, a - apfx[lo] + 1);
+                            int bc[3], jc = 0;
+                            for (int d = D - 1; d >= 0; --d) { bc[d] = blk % nb[d]; blk /= nb[d]; }
+                            for (int d = 0; d < D && valid; ++d) {
+                                const int sd = (sub >> (SH * (D - 1 - d))) & ((1 << SH) - 1);
+                                int i, x;
+                                if (p.step[d] == 0) {
+                                    i = 0;
+                                    x = p.base[d];
+                                    valid = sd == 0 && x >= B * bc[d] && x < B * bc[d] + B;
+                                } else {
+                                    const int lo2 = B * bc[d] > p.base[d] ? (B * bc[d] - p.base[d] + 1) >> 1 : 0;
+                                    i = lo2 + sd;
+                                    x = p.base[d] + 2 * i;
+                                    valid = i < p.cnt[d] && x < B * bc[d] + B;
+                                }
+                                jc = jc * p.cnt[d] + i;
+                                t += (x + 1) * (int)s.strides[d];
+                            }
+                            jj = jc - start;
+                            valid = valid && jj >= 0 && jj < len;
+                            if (valid) cand = try_site(t, mcs, k, L, G, nonnull, topo);
                         }
+                        add_candidate(cand, jj, t, k, L, G, pass_key);
+                    }
+                } else {
+                    for (int j0 = 0; j0 < len; j0 += RB) {
+                        const int j = j0 + tid;
+                        bool cand = false;
+                        int t = 0, k = 0;
+                        uint32_t L = 0, G = 0;
+                        if (j < len) {
+                            int x[3];
+                            t = site_r<D>(s, p, start + j, x);
+                            cand = try_site(t, mcs, k, L, G, nonnull, topo);
+                        }
+                        add_candidate(cand, j, t, k, L, G, pass_key);
                     }
                 }
                 __syncthreads();
                 const int n = *s_n;
                 __syncthreads();
                 if (n > CMAX) { len >>= 1; continue; }  // retry this chunk with fewer sites
-                ct.attempts += 0;  // attempts are counted per MCS (every site once)
                 ct.nonnull += nonnull;
                 ct.topo += topo;
                 const long long t1 = clock64();
@@ -555,6 +693,7 @@ struct Resident {
             }
             start += len;
         }
+        (void)lane;
     }
 };
 
@@ -565,6 +704,8 @@ __global__ void __launch_bounds__(RB, 512 / RB) resident_kernel(SimDesc* sims, c
     __shared__ SimDesc sd;
     __shared__ int s_plan, s_n, s_flag;
     __shared__ int perm[27], s_swap[27];
+    __shared__ uint32_t s_act[ACT_WORDS];
+    __shared__ int s_apfx[ACT_WORDS + 1];
     __shared__ PassInfoR pinfo;
     __shared__ double scratch[RB / 32];
     __shared__ unsigned long long sstat[10];
@@ -596,6 +737,18 @@ __global__ void __launch_bounds__(RB, 512 / RB) resident_kernel(SimDesc* sims, c
                           t3,
                           &s_n,
                           &s_flag};
+        R.act = s_act;
+        R.apfx = s_apfx;
+        {
+            constexpr int B = ActGeom<D>::B;
+            int nbt = 1;
+            for (int d = 0; d < 3; ++d) {
+                R.nb[d] = d < D ? (sd.dims[d] + B - 1) / B : 1;
+                nbt *= R.nb[d];
+            }
+            // too many blocks, or the test switch: the plain build only
+            if (nbt > ACT_MAX || (sd.sweep_flags & 1)) R.nb[0] = 0;
+        }
         // ---- stage the state into shared memory
         for (int f = tid; f < (int)sd.n_padded; f += RB) R.sig[f] = (uint16_t)sd.sigma[f];
         for (int id = tid; id <= sd.n_cells; id += RB) {
@@ -607,7 +760,10 @@ __global__ void __launch_bounds__(RB, 512 / RB) resident_kernel(SimDesc* sims, c
         __syncthreads();
         CountersR ct = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
         uint64_t mcs = sd.mcs;
+        R.rescan();
         auto one_mcs = [&](uint64_t m) {
+            // commits only add active blocks; clear the stale ones now and then
+            if ((m & 15u) == 0u && m != sd.mcs) R.rescan();
             // Fisher-Yates over the colours: the draws one per thread, then
             // the swaps
             if (tid > 0 && tid < sd.n_colors) {
