@@ -30,8 +30,9 @@ attempts per second.
   workload per thread, the reference's run_batch parallelism).
 
 Extra legs in the same line (1 GPU): `c3` (the 128^3 organoid, device and
-end to end), `c1` (the 30x30 quickstart end to end, beside the oracle on one
-thread), `sparse` (the reference's 150x150 proposal-mode case, both modes),
+end to end), `modes` (the 512x512 lattice under Metropolis-Hastings
+acceptance and under the Act term), `c1` (the 30x30 quickstart end to end,
+beside the oracle on one thread), `sparse` (the reference's 150x150 proposal-mode case, both modes),
 `batch` (4096 thetas in one call against a loop of single runs) and `serve`
 (the serving loop under Poisson arrivals).
 
@@ -95,6 +96,63 @@ def build_raw(seed=SEED):
     b.set_adhesion(adhesion(seed))
     b.initialize(warn_on_default_init=False)
     return b
+
+
+def build_modes(mode, seed=SEED):
+    """The headline 512x512 sorting lattice under the loop's other modes:
+    Metropolis-Hastings acceptance ("mh", monte_carlo.rs:168-196) or the
+    Act term ("act", energy.rs:329-471; lambda_Act = 20, Max_Act = 20 for
+    every type)."""
+    from cpm import _cpm
+
+    b = _cpm.CPM(grid=list(GRID), boundary="periodic", seed=seed,
+                 acceptance="metropolis_hastings" if mode == "mh" else None,
+                 active_terms={"act": True} if mode == "act" else None)
+    for t in TYPES:
+        if mode == "act":
+            b.register_cell_type(*t, lambda_act=20.0, max_act=20)
+        else:
+            b.register_cell_type(*t)
+    for t in TYPES:
+        b.add_cells(t[0], PER_TYPE)
+    b.set_adhesion(adhesion(seed))
+    b.initialize(warn_on_default_init=False)
+    return b
+
+
+def run_modes_bench(args):
+    """Device attempts/s of the headline lattice under Metropolis-Hastings
+    acceptance and under the Act term (both on the tiled sweep), CUDA
+    events on the engine stream after a warm-up; the state is recounted
+    after the timed MCS."""
+    import torch
+
+    from cpm import _cpm
+
+    stream = torch.cuda.current_stream()
+    out = {"workload": "the 512x512 sorting lattice with Metropolis-Hastings acceptance (mh) or the Act term "
+                       "(act: lambda_Act=20, Max_Act=20 per type), tiled sweep"}
+    for mode in ("mh", "act"):
+        eng = _cpm.Engine(build_modes(mode), stream=stream.cuda_stream)
+        eng.run_mcs(100)  # also the grid tuner's trials for this shape and mode
+        torch.cuda.synchronize()
+        s0 = eng.stats()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        eng.run_mcs(args.modes_mcs)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b)
+        s1 = eng.stats()
+        att = s1["attempts"] - s0["attempts"]
+        assert att == args.modes_mcs * GRID[0] * GRID[1]
+        assert eng.recount_check()[0]
+        out[mode] = {"attempts_per_s": att / (ms / 1000.0), "mcs_timed": args.modes_mcs, "after_mcs": 100, "ms": ms,
+                     "f_nonnull": (s1["nonnull"] - s0["nonnull"]) / att,
+                     "f_acc": (s1["accepted"] - s0["accepted"]) / att}
+        del eng
+    return out
 
 
 def build_public(seed=SEED):
@@ -856,6 +914,8 @@ def run_gpu(args, rank, world, dist):
     # the tiled sweep's grid tuner: candidate grids timed on each shape's
     # first MCS (microseconds per MCS) and the grid in use
     line["tuning"] = _cpm.tuning_report()
+    if args.modes_mcs > 0 and world == 1:
+        line["modes"] = run_modes_bench(args)
     if args.c1_runs > 0 and world == 1:
         line["c1"] = run_c1_bench(args)
     if not args.no_sparse and world == 1:
@@ -886,6 +946,8 @@ def main():
     ap.add_argument("--c3-warmup", type=int, default=100, help="MCS run before the timed 3D MCS")
     ap.add_argument("--c3-e2e-mcs", type=int, default=5000,
                     help="MCS of the 3D organoid's end-to-end run through cpm.CPM.run (0 skips it)")
+    ap.add_argument("--modes-mcs", type=int, default=200,
+                    help="timed MCS of the headline lattice under MH and under the Act term (0 skips them)")
     ap.add_argument("--c1-runs", type=int, default=3, help="end-to-end runs of the quickstart (0 skips them)")
     ap.add_argument("--no-sparse", action="store_true", help="skip the sparse proposal-mode case")
     ap.add_argument("--serve-n", type=int, default=16, help="requests of the serving workload (0 skips it)")

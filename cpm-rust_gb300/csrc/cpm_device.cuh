@@ -369,9 +369,10 @@ __device__ __forceinline__ bool decide_move(const SimDesc& s, const SigT* sig, c
 // ------------------------------------------------------ modes of the loop ----
 // Acceptance by Metropolis-Hastings and the Act term, on a whole padded
 // lattice (the global sweep, the shared-memory resident sweep and the
-// parity harness; the tiled sweep never runs these modes). Both decide in
-// FP64 with the reference's operation order; pow and exp are CUDA's, within
-// an ulp of the host library's. The acquisition MCS lives in HBM.
+// parity harness; the tiled sweep restates the Act term's geometric means
+// on its box, TileProc::act_gm). Both decide in FP64 with the reference's
+// operation order; pow and exp are CUDA's, within an ulp of the host
+// library's. The acquisition MCS lives in HBM.
 
 // Interior padded index a (possibly halo) padded index stands for under a
 // periodic boundary (energy.rs:363-376 canonical_flat); itself otherwise.

@@ -404,9 +404,8 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
 DeviceSims::Path DeviceSims::path(size_t i) const {
     const SimLayout& L = layouts_[i];
     if (force_global_ || no_connectivity_) return GLOBAL;
-    // Metropolis-Hastings acceptance and the Act term run on the resident
-    // sweep when the lattice fits, else on the global sweep (not tiled)
-    const bool modes = descs_[i].acceptance || descs_[i].act;
+    // Metropolis-Hastings acceptance and the Act term run on the same
+    // sweeps as Metropolis, in kernel variants of their own
     int dims[3] = {(int)L.g.dims[0], (int)L.g.dims[1], (int)L.g.dims[2]}, nt[3] = {1, 1, 1}, max_box = 0;
     const bool tiled_ok = cpmgpu::tiled_plan(L.g.D, dims, L.g.periodic, nt, &max_box) &&
                           cpmgpu::tiled_smem_bytes(max_box, L.n_cells, 0, L.g.D, 0) <= cpmgpu::resident_smem_limit();
@@ -419,10 +418,10 @@ DeviceSims::Path DeviceSims::path(size_t i) const {
         // colour into the tiled sweep (many SMs instead of one; a different,
         // equally exact chain, hence opt-in).
         const int per_color = (nt[0] * nt[1] * nt[2]) >> L.g.D;
-        if (prefer_tiled_ && tiled_ok && per_color >= 8 && !modes) return TILED;
+        if (prefer_tiled_ && tiled_ok && per_color >= 8) return TILED;
         return RESIDENT;
     }
-    return tiled_ok && !modes ? TILED : GLOBAL;
+    return tiled_ok ? TILED : GLOBAL;
 }
 
 // ------------------------------------------------------ grid tuner ----
@@ -443,8 +442,8 @@ struct TuneEntry {
     bool done = false;
 };
 std::mutex g_tune_mu;
-std::map<std::array<int, 8>, TuneEntry>& tune_table() {
-    static std::map<std::array<int, 8>, TuneEntry> t;
+std::map<std::array<int, 9>, TuneEntry>& tune_table() {
+    static std::map<std::array<int, 9>, TuneEntry> t;
     return t;
 }
 }  // namespace
@@ -459,8 +458,9 @@ std::string tuning_report() {
         if (!first) o += ",";
         first = false;
         o += "{\"dim\":" + std::to_string(k[0]) + ",\"energy_neighbours\":" + std::to_string(k[1]) +
-             ",\"odd\":" + std::to_string(k[2]) + ",\"tiles_per_axis\":[" + std::to_string(k[3]) + "," +
-             std::to_string(k[4]) + "," + std::to_string(k[5]) + "],\"tiles_per_colour\":" + std::to_string(k[6]) +
+             ",\"odd\":" + std::to_string(k[2]) + ",\"modes\":" + std::to_string(k[3]) + ",\"tiles_per_axis\":[" +
+             std::to_string(k[4]) + "," + std::to_string(k[5]) + "," + std::to_string(k[6]) +
+             "],\"tiles_per_colour\":" + std::to_string(k[7]) +
              ",\"done\":" + (e.done ? "true" : "false") + ",\"grid\":" + std::to_string(e.chosen) +
              ",\"candidates\":[";
         for (size_t i = 0; i < e.cand.size(); ++i) {
@@ -497,7 +497,8 @@ std::string DeviceSims::run_tiled(const RunPlan& p, const uint64_t* t3) {
     int per_sm = 0, dev = 0, sms = 1;
     int odd = 0;
     for (int d = 0; d < L.g.D; ++d) odd |= L.g.periodic && (L.g.dims[d] & 1);
-    CUDA_TRY(cpmgpu::tiled_occupancy(L.g.D, L.NE, odd, smem, &per_sm));
+    const int modes = descs_[p.sim].acceptance || descs_[p.sim].act ? 1 : 0;
+    CUDA_TRY(cpmgpu::tiled_occupancy(L.g.D, L.NE, odd, modes, smem, &per_sm));
     CUDA_TRY(cudaGetDevice(&dev));
     CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     int tiles = 1;
@@ -512,7 +513,7 @@ std::string DeviceSims::run_tiled(const RunPlan& p, const uint64_t* t3) {
     // the tuner's entry for this shape (none when the grid is set from
     // outside: the environment, a serving cap, or CPM_GPU_NO_TUNE)
     const int per_color = tiles >> L.g.D;
-    const std::array<int, 8> tkey = {L.g.D, L.NE, odd, nt[0], L.g.D > 1 ? nt[1] : 1, L.g.D > 2 ? nt[2] : 1,
+    const std::array<int, 9> tkey = {L.g.D, L.NE, odd, modes, nt[0], L.g.D > 1 ? nt[1] : 1, L.g.D > 2 ? nt[2] : 1,
                                      per_color, (int)smem};
     const bool tune = !grid_env && tiled_grid_cap_ <= 0 && !std::getenv("CPM_GPU_NO_TUNE");
     std::vector<int> trials;  // grids still to time in this run, in order
@@ -554,7 +555,7 @@ std::string DeviceSims::run_tiled(const RunPlan& p, const uint64_t* t3) {
     auto launch = [&](uint64_t m, int g) -> cudaError_t {
         cudaError_t e = cudaMemsetAsync(d_bar_, 0, 64, stream_);
         if (e == cudaSuccess)
-            e = cpmgpu::launch_tiled(L.g.D, L.NE, odd, d_sim, m, nt, d_bar_, claims, reg_smem ? nullptr : d_reg_, t3,
+            e = cpmgpu::launch_tiled(L.g.D, L.NE, odd, modes, d_sim, m, nt, d_bar_, claims, reg_smem ? nullptr : d_reg_, t3,
                                      max_box, tables_in_smem, barrier_extra, cl_cap, reg_smem, smem, g, stream_,
                                      L.n_cells);
         return e;

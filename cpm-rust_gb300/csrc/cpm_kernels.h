@@ -50,26 +50,29 @@ size_t tiled_smem_bytes(int max_box, int n_cells, int cl_cap, int D, int reg_sme
 size_t tiled_table_bytes(int n_types, int tab_n);
 int tiled_block();
 // `odd`: the lattice has an odd periodic side (kernels of cpm_tiled_odd.cu).
+// `modes`: Metropolis-Hastings acceptance or the Act term (kernels of
+// cpm_tiled_modes.cu / cpm_tiled_modes_odd.cu).
 // `reg_smem`: each CTA's cell registry (stamps and box slots) in shared
 // memory; else `d_registry` holds it: 2 x grid x (n_cells + 1) words.
-cudaError_t tiled_occupancy(int D, int NE, int odd, size_t smem, int* per_sm);
-cudaError_t launch_tiled(int D, int NE, int odd, SimDesc* d_sim, uint64_t n_mcs, const int* nt, void* d_barrier,
-                         unsigned long long* d_claims, uint32_t* d_registry, const uint64_t* d_t3, int max_box,
-                         int tables_in_smem, int barrier_extra, int cl_cap, int reg_smem, size_t smem, int grid,
-                         cudaStream_t st, int n_cells);
-// The variants behind them (even site colouring / odd periodic sides).
-cudaError_t prepare_tiled_kernels_even();
-cudaError_t prepare_tiled_kernels_odd();
-cudaError_t tiled_occupancy_even(int D, int NE, size_t smem, int* per_sm);
-cudaError_t tiled_occupancy_odd(int D, int NE, size_t smem, int* per_sm);
-cudaError_t launch_tiled_even(int D, int NE, SimDesc* d_sim, uint64_t n_mcs, const int* nt, void* d_barrier,
-                              unsigned long long* d_claims, uint32_t* d_registry, const uint64_t* d_t3, int max_box,
-                              int tables_in_smem, int barrier_extra, int cl_cap, int reg_smem, size_t smem, int grid,
-                              cudaStream_t st, int n_cells);
-cudaError_t launch_tiled_odd(int D, int NE, SimDesc* d_sim, uint64_t n_mcs, const int* nt, void* d_barrier,
-                             unsigned long long* d_claims, uint32_t* d_registry, const uint64_t* d_t3, int max_box,
-                             int tables_in_smem, int barrier_extra, int cl_cap, int reg_smem, size_t smem, int grid,
-                             cudaStream_t st, int n_cells);
+cudaError_t tiled_occupancy(int D, int NE, int odd, int modes, size_t smem, int* per_sm);
+cudaError_t launch_tiled(int D, int NE, int odd, int modes, SimDesc* d_sim, uint64_t n_mcs, const int* nt,
+                         void* d_barrier, unsigned long long* d_claims, uint32_t* d_registry, const uint64_t* d_t3,
+                         int max_box, int tables_in_smem, int barrier_extra, int cl_cap, int reg_smem, size_t smem,
+                         int grid, cudaStream_t st, int n_cells);
+// The variants behind them (even site colouring / odd periodic sides, each
+// for the Metropolis chain and for the modes).
+#define CPM_TILED_VARIANT_DECLS(sfx)                                                                              \
+    cudaError_t prepare_tiled_kernels_##sfx();                                                                    \
+    cudaError_t tiled_occupancy_##sfx(int D, int NE, size_t smem, int* per_sm);                                   \
+    cudaError_t launch_tiled_##sfx(int D, int NE, SimDesc* d_sim, uint64_t n_mcs, const int* nt, void* d_barrier, \
+                                   unsigned long long* d_claims, uint32_t* d_registry, const uint64_t* d_t3,      \
+                                   int max_box, int tables_in_smem, int barrier_extra, int cl_cap, int reg_smem,  \
+                                   size_t smem, int grid, cudaStream_t st, int n_cells);
+CPM_TILED_VARIANT_DECLS(even)
+CPM_TILED_VARIANT_DECLS(odd)
+CPM_TILED_VARIANT_DECLS(modes_even)
+CPM_TILED_VARIANT_DECLS(modes_odd)
+#undef CPM_TILED_VARIANT_DECLS
 // Copies one sample (V, I, position sums, optional lattice) of simulation d_sim.
 cudaError_t launch_sample(int D, const SimDesc* d_sim, int sample, int write_lattice, int64_t n_sites, cudaStream_t st);
 // Topology readouts of lattice snapshots (cpm_readout.cu). Work is cut into

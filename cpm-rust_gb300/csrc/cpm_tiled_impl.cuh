@@ -37,6 +37,12 @@
 #include "cpm_device.cuh"
 #include "cpm_kernels.h"
 
+// The unit that compiles the even-sided Metropolis kernels also compiles the
+// host entry points the four kernel units share.
+#if !defined(CPM_TILED_ODD_UNIT) && !defined(CPM_TILED_MODES_UNIT)
+#define CPM_TILED_MAIN_UNIT
+#endif
+
 namespace cpmgpu {
 
 constexpr int TB = 256;          // threads per CTA
@@ -144,7 +150,10 @@ __device__ __forceinline__ bool tile_simple(const uint16_t* sig, const int* toff
     return D == 2 ? table2d_bit(t2, p) : table3d_bit(t3, p);
 }
 
-template <int D, int NE>
+// MODES: the simulation uses Metropolis-Hastings acceptance or the Act term
+// (compiled as separate kernels, so that the Metropolis kernels keep their
+// registers).
+template <int D, int NE, bool MODES>
 struct TileProc {
     const SimDesc& g;     // global descriptor
     SimDesc& l;           // box descriptor: local strides/offsets, same parameters
@@ -185,6 +194,8 @@ struct TileProc {
     const uint32_t* clist;
     long long *ssp, *sso;
     int cl_cap;
+    const int* bdims;  // box extent per axis (tile + rim)
+    uint64_t mcs;      // the MCS being swept (acquisition MCS of the Act term)
 
     __device__ __forceinline__ bool sums_of(uint32_t s, long long*& sp, long long*& so) const {
         const int k = (int)s - 1;
@@ -222,6 +233,94 @@ struct TileProc {
         return f;
     }
 
+    // ---- Metropolis-Hastings acceptance and the Act term (MODES kernels)
+    // The whole decision in FP64 with the reference's operation order, as
+    // decide_modes makes it on a whole lattice. The box holds the target's
+    // copy neighbourhood; the Act term also reads the source's, which can
+    // leave the box by one site. Such a site lies in a neighbouring tile of
+    // another colour (tiles are at least 8 sites wide), which no CTA changes
+    // during this sub-phase, so it is read from the lattice in HBM. The
+    // acquisition MCS of every site lives in HBM; a commit writes it for the
+    // site it changes (L2 accesses: written and read by other CTAs in later
+    // sub-phases).
+
+    // Geometric mean of the activity max(0, max_act - (mcs - birth)) over
+    // box position q and its copy neighbours owned by slot `rel`
+    // (energy.rs:377-412), in the reference's order: q, then the copy
+    // offsets in stencil order.
+    __device__ double act_gm(int q, uint32_t rel, uint32_t max_act, uint64_t m) const {
+        int x[3] = {0, 0, 0};
+        {
+            int r = q;
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                x[d] = r / (int)l.strides[d];
+                r -= x[d] * (int)l.strides[d];
+            }
+        }
+        const uint32_t rel_id = rel ? clist[rel - 1] : 0u;
+        double product = 1.0;
+        uint32_t count = 0;
+        for (int k = -1; k < g.n_copy; ++k) {
+            int y[3] = {x[0], x[1], x[2]};
+            bool in_box = true;
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                if (k >= 0) y[d] += g.copy_vec[k][d];
+                in_box &= y[d] >= 0 && y[d] < bdims[d];
+            }
+            int gf = 0;
+            if (in_box) {
+                int qq = 0;
+#pragma unroll
+                for (int d = 0; d < D; ++d) qq += y[d] * (int)l.strides[d];
+                if ((uint32_t)sig[qq] != rel) continue;
+                int xg[3];
+                gf = gflat_of_box(qq, xg);  // the interior site (periodic) or the fixed halo site
+            } else {
+                bool outside = false, padded = true;
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    const int xx = gcoord(d, y[d]);
+                    outside |= xx < 0 || xx >= g.dims[d];      // a fixed lattice's medium halo
+                    padded &= xx >= -1 && xx <= g.dims[d];   // within the padded lattice
+                    gf += (xx + 1) * (int)g.strides[d];
+                }
+                const uint32_t id = outside ? 0u : __ldcg(g.sigma + gf);
+                if (id != rel_id || !padded) continue;
+            }
+            const uint64_t b = __ldcg(g.birth + gf);
+            const uint64_t elapsed = m > b ? m - b : 0ull;
+            product = __dmul_rn(product, (double)((uint64_t)max_act > elapsed ? (uint64_t)max_act - elapsed : 0ull));
+            count += 1;
+        }
+        return pow(product, __ddiv_rn(1.0, (double)count));
+    }
+
+    // energy.rs:441-451 on the box: -(lambda_act / max_act) (GM_src - GM_tgt)
+    // of the gaining cell's type; 0 when the medium gains.
+    __device__ double act_delta_box(int t, int src, uint32_t L, uint32_t G, uint64_t m) const {
+        if (G == 0) return 0.0;
+        const int ty = adh[G] - 1;
+        const double lambda = g.lambda_act[ty];
+        const uint32_t mx = g.max_act[ty];
+        const double gs = act_gm(src, G, mx, m);
+        const double gt = act_gm(t, L, mx, m);
+        return __dmul_rn(-__ddiv_rn(lambda, (double)mx), __dsub_rn(gs, gt));
+    }
+
+    // decide_modes on the box: conservative delta-H (+ the Act term), then
+    // Metropolis or Metropolis-Hastings (accept_modes counts the target's
+    // copy neighbours, which the box holds).
+    __device__ bool decide_box_modes(int t, int src, uint32_t L, uint32_t G, uint64_t m, const TileDraw& draw, int& dl,
+                                     int& dg) const {
+        const DeltaOut o = delta_h<NE, uint16_t>(l, sig, adh, vol, itf, t, L, G);
+        dl = o.dl;
+        dg = o.dg;
+        const double dh = g.act ? __dadd_rn(o.dh, act_delta_box(t, src, L, G, m)) : o.dh;
+        return accept_modes(l, sig, t, L, G, dh, draw);
+    }
+
     // The candidate's decision on the current volumes and interfaces: the
     // cell half of decide_move over the neighbour half staged with the
     // candidate (sigma around it cannot change within its pass).
@@ -231,6 +330,11 @@ struct TileProc {
         uint32_t fl = c_flags[c] & ~(T_ACC | T_GUARD);
         if (L != 0 && vol[L] <= l.min_cell_volume) {
             fl |= T_GUARD;
+        } else if constexpr (MODES) {
+            const TileDraw draw{g.seed, mcs, c_gf[c], c_z[c]};
+            int dl = 0, dg = 0;
+            const int t = (int)c_site[c];
+            if (decide_box_modes(t, t + (int)l.copy_off[fl & 7u], L, G, mcs, draw, dl, dg)) fl |= T_ACC;
         } else {
             const int16_t dd = c_dl[c];
             NeighbourPart nb;
@@ -264,6 +368,9 @@ struct TileProc {
         {
             const int k = atomicAdd(s_nchg, 1);
             if (k < TCHG) chg[k] = (uint32_t)t;
+        }
+        if constexpr (MODES) {
+            if (g.act) __stcg(g.birth + c_gf[c], (uint32_t)mcs);  // energy.rs:453-458
         }
         if (L) {
             vol[L] -= 1;
@@ -574,7 +681,7 @@ __host__ __device__ inline TileShared tile_shared(int box_sites, int n_cells, in
 
 // Shared-memory copy of the float energy tables (J, adhesion differences,
 // term tables and their remainders): (n+1)^2 + (n+1)^3 + 4 n tab_n floats.
-#ifndef CPM_TILED_ODD_UNIT
+#ifdef CPM_TILED_MAIN_UNIT
 size_t tiled_table_bytes(int n_types, int tab_n) {
     const size_t n1 = (size_t)n_types + 1;
     return (n1 * n1 + n1 * n1 * n1 + 4 * (size_t)n_types * (size_t)tab_n) * 4;
@@ -584,7 +691,7 @@ size_t tiled_table_bytes(int n_types, int tab_n) {
 // ODD: the lattice has an odd periodic side, whose last coordinate takes a
 // third site colour (compiled separately, so that the even-sided kernels
 // keep their two-colour index arithmetic).
-template <int D, int NE, bool ODD>
+template <int D, int NE, bool ODD, bool MODES>
 __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_mcs, TileGrid tg_in, BarrierState* bar,
                                                    unsigned long long* claims, const uint64_t* t3, int max_box,
                                                    int tables_in_smem, int barrier_extra, int cl_cap,
@@ -768,7 +875,7 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                 }
                 __syncthreads();
             };
-            TileProc<D, NE> P{g, lsd, (uint16_t*)(sm + ts.sig), s_gx0, (uint32_t*)(sm + ts.vol),
+            TileProc<D, NE, MODES> P{g, lsd, (uint16_t*)(sm + ts.sig), s_gx0, (uint32_t*)(sm + ts.vol),
                               (uint32_t*)(sm + ts.itf), (uint32_t*)(sm + ts.b0), (uint32_t*)(sm + ts.b1),
                               (uint16_t*)(sm + ts.adh), (uint8_t*)(sm + ts.dirty), (uint8_t*)(sm + ts.own),
                               (uint8_t*)(sm + ts.mod), (uint32_t*)(sm + ts.c_site), (uint32_t*)(sm + ts.c_key),
@@ -780,7 +887,8 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                               (uint32_t*)(sm + ts.c_flags), (uint32_t*)(sm + ts.c_gf), (uint32_t*)(sm + ts.c_z),
                               (uint32_t*)(sm + ts.c_xy), (int16_t*)(sm + ts.c_dl), (float*)(sm + ts.c_adh),
                               (float*)(sm + ts.c_sabs), (uint16_t*)(sm + ts.c_x2),
-                              clist, (long long*)(sm + ts.ssp), (long long*)(sm + ts.sso), cl_cap};
+                              clist, (long long*)(sm + ts.ssp), (long long*)(sm + ts.sso), cl_cap,
+                              s_box_dims, mcs};
             uint32_t* sid = (uint32_t*)(sm + ts.sid);
             // Stage the box of the current tile: each distinct cell of the
             // box listed once (and claimed when `claim`) and given the next
@@ -1051,21 +1159,44 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                     const int pos = atomicAdd(cnt, 1);
                     if (pos >= cap) return;
                     const int c = off + pos;
-                    // the neighbour half of the decision, fixed for the pass
-                    const NeighbourPart nb = decide_neighbours<NE, uint16_t, int>(lsd, P.sig, P.adh, s_eoff, t, L, G);
                     P.b_site[c] = (uint32_t)t;
                     P.b_cells[c] = L | (G << 16);
                     P.b_key[c] = (mix32((uint32_t)j * 0x9E3779B9u ^ s_pkey[pi]) & 0xFFFFC000u) | (uint32_t)j;
                     P.b_gf[c] = (uint32_t)gf;
                     P.b_z[c] = rd.z;
+                    P.b_xy[c] = (uint32_t)xg[0] | ((uint32_t)xg[1] << 16);
+                    if (D > 2) P.b_x2[c] = (uint16_t)xg[2];
+                    uint32_t fl = (uint32_t)kd | T_PEND;
+                    if constexpr (MODES) {
+                        // the whole first decision in FP64 (no neighbour half)
+                        int dl = 0, dg = 0;
+                        bool acc = false;
+                        if (L != 0 && P.vol[L] <= lsd.min_cell_volume) {
+                            fl |= T_GUARD;
+                            atomicAdd(&s_pguard[pi], 1);
+                            // the interface deltas still serve a commit after a re-evaluation
+                            const DeltaOut o = delta_h<NE, uint16_t>(lsd, P.sig, P.adh, P.vol, P.itf, t, L, G);
+                            dl = o.dl;
+                            dg = o.dg;
+                        } else {
+                            const TileDraw draw{g.seed, mcs, (uint32_t)gf, rd.z};
+                            acc = P.decide_box_modes(t, t + s_coff[kd], L, G, mcs, draw, dl, dg);
+                        }
+                        P.b_dl[c] = (int16_t)((dl & 0xFF) | ((dg & 0xFF) << 8));
+                        if (acc) {
+                            fl |= T_ACC;
+                            s_pacc[pi] = 1;
+                        }
+                        P.b_flags[c] = fl;
+                        return;
+                    }
+                    // the neighbour half of the decision, fixed for the pass
+                    const NeighbourPart nb = decide_neighbours<NE, uint16_t, int>(lsd, P.sig, P.adh, s_eoff, t, L, G);
                     P.b_adh[c] = nb.adh;
                     P.b_sabs[c] = nb.sabs;
                     P.b_dl[c] = (int16_t)((nb.dl & 0xFF) | ((nb.dg & 0xFF) << 8));
-                    P.b_xy[c] = (uint32_t)xg[0] | ((uint32_t)xg[1] << 16);
-                    if (D > 2) P.b_x2[c] = (uint16_t)xg[2];
                     // the first decision, on the volumes and interfaces before
                     // any commit of the pass (TileProc::evaluate, made here)
-                    uint32_t fl = (uint32_t)kd | T_PEND;
                     if (L != 0 && P.vol[L] <= lsd.min_cell_volume) {
                         fl |= T_GUARD;
                         atomicAdd(&s_pguard[pi], 1);
@@ -1249,14 +1380,27 @@ static int tiled_index(int D, int NE) {
 
 // The kernel variants of the including unit: even site colouring in
 // cpm_tiled.cu; odd periodic sides in cpm_tiled_odd.cu, which includes this
-// file with CPM_TILED_ODD_UNIT defined (two units build in parallel). The
-// host entry points shared by both are compiled in cpm_tiled.cu only.
-#ifndef CPM_TILED_ODD_UNIT
+// file with CPM_TILED_ODD_UNIT defined; the same two for the modes of the
+// loop (Metropolis-Hastings, Act) in cpm_tiled_modes.cu and
+// cpm_tiled_modes_odd.cu (CPM_TILED_MODES_UNIT). The four units build in
+// parallel; the host entry points they share are compiled in cpm_tiled.cu
+// only.
+#if !defined(CPM_TILED_ODD_UNIT) && !defined(CPM_TILED_MODES_UNIT)
 #define TILED_ODD false
+#define TILED_MODES false
 #define TILED_VARIANT(name) name##_even
+#elif !defined(CPM_TILED_MODES_UNIT)
+#define TILED_ODD true
+#define TILED_MODES false
+#define TILED_VARIANT(name) name##_odd
+#elif !defined(CPM_TILED_ODD_UNIT)
+#define TILED_ODD false
+#define TILED_MODES true
+#define TILED_VARIANT(name) name##_modes_even
 #else
 #define TILED_ODD true
-#define TILED_VARIANT(name) name##_odd
+#define TILED_MODES true
+#define TILED_VARIANT(name) name##_modes_odd
 #endif
 
 // Shared-memory limit raised once per device (see prepare_resident_kernels).
@@ -1269,11 +1413,11 @@ cudaError_t TILED_VARIANT(prepare_tiled_kernels)() {
     std::lock_guard<std::mutex> lk(mu);
     if (dev >= 0 && dev < 64 && done[dev]) return cudaSuccess;
     const int smem = 227 * 1024 - 4096;
-    if ((e = cudaFuncSetAttribute(tiled_kernel<2, 4, TILED_ODD>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) ||
-        (e = cudaFuncSetAttribute(tiled_kernel<2, 8, TILED_ODD>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) ||
-        (e = cudaFuncSetAttribute(tiled_kernel<3, 6, TILED_ODD>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) ||
-        (e = cudaFuncSetAttribute(tiled_kernel<3, 18, TILED_ODD>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) ||
-        (e = cudaFuncSetAttribute(tiled_kernel<3, 26, TILED_ODD>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)))
+    if ((e = cudaFuncSetAttribute(tiled_kernel<2, 4, TILED_ODD, TILED_MODES>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) ||
+        (e = cudaFuncSetAttribute(tiled_kernel<2, 8, TILED_ODD, TILED_MODES>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) ||
+        (e = cudaFuncSetAttribute(tiled_kernel<3, 6, TILED_ODD, TILED_MODES>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) ||
+        (e = cudaFuncSetAttribute(tiled_kernel<3, 18, TILED_ODD, TILED_MODES>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) ||
+        (e = cudaFuncSetAttribute(tiled_kernel<3, 26, TILED_ODD, TILED_MODES>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)))
         return e;
     if (dev >= 0 && dev < 64) done[dev] = true;
     return cudaSuccess;
@@ -1284,7 +1428,7 @@ cudaError_t TILED_VARIANT(tiled_occupancy)(int D, int NE, size_t smem, int* per_
     cudaError_t e = TILED_VARIANT(prepare_tiled_kernels)();
     if (e != cudaSuccess) return e;
 #define TOCC(I, D_, NE_) \
-    case I: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, tiled_kernel<D_, NE_, TILED_ODD>, TB, smem);
+    case I: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, tiled_kernel<D_, NE_, TILED_ODD, TILED_MODES>, TB, smem);
     switch (tiled_index(D, NE)) {
         TOCC(0, 2, 4)
         TOCC(1, 2, 8)
@@ -1310,7 +1454,7 @@ cudaError_t TILED_VARIANT(launch_tiled)(int D, int NE, SimDesc* d_sim, uint64_t 
     uint32_t* slot_all = d_registry ? d_registry + (size_t)grid * (size_t)(n_cells + 1) : nullptr;
 #define TLAUNCH(I, D_, NE_)                                                                                 \
     case I: {                                                                                               \
-        auto k = tiled_kernel<D_, NE_, TILED_ODD>;                                                           \
+        auto k = tiled_kernel<D_, NE_, TILED_ODD, TILED_MODES>;                                                           \
         cudaError_t e = TILED_VARIANT(prepare_tiled_kernels)();                                             \
         if (e != cudaSuccess) return e;                                                                     \
         void* args[] = {(void*)&d_sim, (void*)&n_mcs, (void*)&tg, (void*)&bar, (void*)&d_claims, (void*)&d_t3, \
@@ -1329,7 +1473,7 @@ cudaError_t TILED_VARIANT(launch_tiled)(int D, int NE, SimDesc* d_sim, uint64_t 
 #undef TLAUNCH
 }
 
-#ifndef CPM_TILED_ODD_UNIT
+#ifdef CPM_TILED_MAIN_UNIT
 bool tiled_plan(int D, const int* dims, int periodic, int* nt, int* max_box) {
     (void)periodic;  // odd periodic axes take a third site colour in the kernel
     int box = 1, klass = 1;
@@ -1362,25 +1506,30 @@ int tiled_block() { return TB; }
 
 cudaError_t prepare_tiled_kernels() {
     cudaError_t e = prepare_tiled_kernels_even();
-    return e == cudaSuccess ? prepare_tiled_kernels_odd() : e;
+    if (e == cudaSuccess) e = prepare_tiled_kernels_odd();
+    if (e == cudaSuccess) e = prepare_tiled_kernels_modes_even();
+    if (e == cudaSuccess) e = prepare_tiled_kernels_modes_odd();
+    return e;
 }
 
-cudaError_t tiled_occupancy(int D, int NE, int odd, size_t smem, int* per_sm) {
+cudaError_t tiled_occupancy(int D, int NE, int odd, int modes, size_t smem, int* per_sm) {
+    if (modes) return odd ? tiled_occupancy_modes_odd(D, NE, smem, per_sm) : tiled_occupancy_modes_even(D, NE, smem, per_sm);
     return odd ? tiled_occupancy_odd(D, NE, smem, per_sm) : tiled_occupancy_even(D, NE, smem, per_sm);
 }
 
-cudaError_t launch_tiled(int D, int NE, int odd, SimDesc* d_sim, uint64_t n_mcs, const int* nt, void* d_barrier,
-                         unsigned long long* d_claims, uint32_t* d_registry, const uint64_t* d_t3, int max_box,
-                         int tables_in_smem, int barrier_extra, int cl_cap, int reg_smem, size_t smem, int grid,
-                         cudaStream_t st, int n_cells) {
-    return odd ? launch_tiled_odd(D, NE, d_sim, n_mcs, nt, d_barrier, d_claims, d_registry, d_t3, max_box,
-                                  tables_in_smem, barrier_extra, cl_cap, reg_smem, smem, grid, st, n_cells)
-               : launch_tiled_even(D, NE, d_sim, n_mcs, nt, d_barrier, d_claims, d_registry, d_t3, max_box,
-                                   tables_in_smem, barrier_extra, cl_cap, reg_smem, smem, grid, st, n_cells);
+cudaError_t launch_tiled(int D, int NE, int odd, int modes, SimDesc* d_sim, uint64_t n_mcs, const int* nt,
+                         void* d_barrier, unsigned long long* d_claims, uint32_t* d_registry, const uint64_t* d_t3,
+                         int max_box, int tables_in_smem, int barrier_extra, int cl_cap, int reg_smem, size_t smem,
+                         int grid, cudaStream_t st, int n_cells) {
+    auto* fn = modes ? (odd ? launch_tiled_modes_odd : launch_tiled_modes_even)
+                     : (odd ? launch_tiled_odd : launch_tiled_even);
+    return fn(D, NE, d_sim, n_mcs, nt, d_barrier, d_claims, d_registry, d_t3, max_box, tables_in_smem, barrier_extra,
+              cl_cap, reg_smem, smem, grid, st, n_cells);
 }
 #endif
 
 #undef TILED_ODD
+#undef TILED_MODES
 #undef TILED_VARIANT
 
 }  // namespace cpmgpu

@@ -33,7 +33,13 @@ lattices the tiled sweep cuts, read at several MCS along each trajectory
     energy, medium row 16 and type-type J uniform in [1, 12] from
     default_rng(1), nested-layer placement (one 2x2x2 seed per cell, types
     from the centre out); seeds 1..128, read at 25, 50, 100, 200 and 500 MCS.
-Usage: python tests/golden/make_ks_fixture.py [--fluct | --modes | --odd | --shapes]
+And (`modes_tiled_oracle_summary.npz`, `--modes-tiled`) the loop's other
+modes on a lattice the tiled sweep cuts into 6x6 tiles: 96x96 periodic, one
+type (V*=40, I*=30, lambda_V=3, lambda_I=0.6, 115 cells, phi=0.5),
+J=[[0,6.5],[6.5,2.2]], 2000 burn-in + 1000 readout MCS, seeds 1..128, with
+Metropolis-Hastings acceptance and with the Act term (lambda_act = 20,
+max_act = 20).
+Usage: python tests/golden/make_ks_fixture.py [--fluct | --modes | --modes-tiled | --odd | --shapes]
 """
 
 import os
@@ -103,6 +109,31 @@ def modes_main():
         out[f"{mode}_mean_interface"] = i.mean(1)
     np.savez_compressed(os.path.join(HERE, "modes_oracle_summary.npz"), **out)
     print("wrote", os.path.join(HERE, "modes_oracle_summary.npz"))
+
+
+MODES_TILED_SEEDS = 128
+MODES_TILED_BURN_IN, MODES_TILED_READOUT = 2000, 1000
+
+
+def modes_tiled_spec(mode):
+    return O.ModelSpec((96, 96), True, [(40, 30, 3.0, 0.6)], [[0, 6.5], [6.5, 2.2]], cell_counts=[115], **MODES[mode])
+
+
+def modes_tiled_main():
+    seeds = np.arange(1, MODES_TILED_SEEDS + 1, dtype=np.uint64)
+    out = {"seeds": seeds}
+    for mode in MODES:
+        failed, cells, energy, n = O.run_many(modes_tiled_spec(mode), seeds, MODES_TILED_BURN_IN, MODES_TILED_READOUT,
+                                              threads=0, local_halo=True)
+        assert failed == 0 and np.all(n == 115)
+        v = cells["volume"].astype(np.float64)
+        i = cells["interface"].astype(np.float64)
+        out[f"{mode}_energy"] = energy
+        out[f"{mode}_mean_volume"] = v.mean(1)
+        out[f"{mode}_volume_std"] = v.std(1)
+        out[f"{mode}_mean_interface"] = i.mean(1)
+    np.savez_compressed(os.path.join(HERE, "modes_tiled_oracle_summary.npz"), **out)
+    print("wrote", os.path.join(HERE, "modes_tiled_oracle_summary.npz"))
 
 
 ODD_SEEDS = 96
@@ -211,6 +242,8 @@ def main():
 if __name__ == "__main__":
     if "--fluct" in sys.argv:
         fluct_main()
+    elif "--modes-tiled" in sys.argv:
+        modes_tiled_main()
     elif "--modes" in sys.argv:
         modes_main()
     elif "--odd" in sys.argv:
@@ -221,5 +254,6 @@ if __name__ == "__main__":
         main()
         fluct_main()
         modes_main()
+        modes_tiled_main()
         odd_main()
         shapes_main()
