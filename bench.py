@@ -463,6 +463,43 @@ def run_serve_bench(args):
     lat = np.array(lat)
     alone = np.array(alone)
     ratio = lat / alone
+    nominal = None
+    if args.serve_load_n > 0:
+        # the workload's nominal stream: Poisson arrivals at 200/s, far above
+        # what one GPU serves (each request is ~5e8 attempts), so the queue
+        # grows; the sustained rate is the server's saturation throughput
+        lreqs = serve_requests(args.serve_load_n, rate=args.serve_load_rate, seed=6)
+        lsims = [serve_sim(q) for q in lreqs]
+        latt = [q["side"] ** q["D"] * (q["burn"] + q["readout"]) for q in lreqs]
+        tms = []
+        with cpm.Server() as srv:
+            t0 = time.perf_counter()
+            tickets = []
+            for q, sim in zip(lreqs, lsims):
+                dt = q["arrival"] - (time.perf_counter() - t0)
+                if dt > 0:
+                    time.sleep(dt)
+                tickets.append(srv.submit(sim, q["burn"], q["readout"], q["interval"]))
+            for t in tickets:
+                st, res, tm = srv.wait(t)
+                assert st == "done", st
+                tms.append(tm)
+            lwall = time.perf_counter() - t0
+            lstats = srv.stats()
+        total = np.array([tm["finished_s"] - tm["submitted_s"] for tm in tms])
+        wait = np.array([tm["admitted_s"] - tm["submitted_s"] for tm in tms])
+        service = np.array([tm["finished_s"] - tm["admitted_s"] for tm in tms])
+        nominal = {
+            "requests": len(lreqs), "rate_per_s": args.serve_load_rate,
+            "offered_attempts_per_s": float(sum(latt)) / lreqs[-1]["arrival"],
+            "attempts_per_s": float(sum(latt)) / lwall, "sims_per_s": len(lreqs) / lwall, "wall_s": lwall,
+            "p50_latency_s": float(np.percentile(total, 50)), "p99_latency_s": float(np.percentile(total, 99)),
+            "p50_queue_wait_s": float(np.percentile(wait, 50)), "p99_queue_wait_s": float(np.percentile(wait, 99)),
+            "p50_service_s": float(np.percentile(service, 50)), "p99_service_s": float(np.percentile(service, 99)),
+            "peak_active": lstats["peak_active"], "peak_device_bytes": lstats["peak_bytes"],
+            "how": "submitted at their Poisson arrival times (seed 6); latency = queue wait (submitted to admitted) "
+                   "+ service (admitted to result ready)",
+        }
     return {
         "workload": f"{len(reqs)} requests, Poisson arrivals at {args.serve_rate:g}/s; 70% 2D side U{{64..512}} "
                     "(V*=50, I*=75), 30% 3D side U{32..96} (V*=1048, I*=600, 26-neighbour), phi=0.7, theta as the "
@@ -485,6 +522,7 @@ def run_serve_bench(args):
         "requests": [[q["D"], q["side"], q["burn"] + q["readout"], round(a, 3), round(m, 3)]
                      for q, a, m in zip(reqs, alone, lat)],
         "requests_columns": ["D", "side", "MCS", "isolated_s", "in_stream_s"],
+        "nominal_rate": nominal,
     }
 
 
@@ -951,6 +989,9 @@ def main():
     ap.add_argument("--c1-runs", type=int, default=3, help="end-to-end runs of the quickstart (0 skips them)")
     ap.add_argument("--no-sparse", action="store_true", help="skip the sparse proposal-mode case")
     ap.add_argument("--serve-n", type=int, default=16, help="requests of the serving workload (0 skips it)")
+    ap.add_argument("--serve-load-n", type=int, default=200,
+                    help="requests of the nominal-rate serving stream (0 skips it)")
+    ap.add_argument("--serve-load-rate", type=float, default=200.0, help="arrivals/s of the nominal-rate stream")
     ap.add_argument("--serve-rate", type=float, default=1.0,
                     help="Poisson arrival rate of the requests (1/s); the workload's nominal 200/s offers ~100x what "
                          "one GPU serves, so the default measures latency at a rate the GPU sustains")

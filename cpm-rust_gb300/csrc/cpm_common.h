@@ -130,7 +130,7 @@ struct SimDesc {
     uint32_t* sample_lattice;       // n_samples * n_sites (unpadded) or null
     int32_t* error;                 // first error code (0 = none)
     uint32_t* done_flag;            // optional (host-mapped): set to 1 when a run plan of this simulation ends
-    // ---- modes of the loop (only the global-memory sweep runs them) ----
+    // ---- modes of the loop (every sweep runs them) ----
     int32_t acceptance;             // 0 = Metropolis, 1 = MetropolisHastings (monte_carlo.rs:147-196)
     int32_t act;                    // Act term active (energy.rs:329-471)
     const double* lambda_act;       // per type

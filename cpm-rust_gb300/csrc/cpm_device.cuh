@@ -390,6 +390,17 @@ __device__ __forceinline__ int64_t act_canonical(const SimDesc& s, int64_t f) {
     return out;
 }
 
+// product^(1/count), the geometric mean's last step (energy.rs:410), without
+// the FP64 pow where its value is exact: a zero product (a retained site
+// with no activity left, the usual case once Max_Act MCS have passed) gives
+// +0, and one retained site gives the product itself, both as a correctly
+// rounded pow (the host library's) returns them.
+__device__ __forceinline__ double act_root(double product, uint32_t count) {
+    if (product == 0.0) return 0.0;
+    if (count == 1u) return product;
+    return pow(product, __ddiv_rn(1.0, (double)count));
+}
+
 // Geometric mean of the activity max(0, max_act - (mcs - birth)) over
 // `site` and its copy neighbours owned by `relevant` (energy.rs:377-412).
 template <class SigT>
@@ -403,10 +414,12 @@ __device__ __forceinline__ double act_geometric_mean(const SimDesc& s, const Sig
         if ((uint32_t)sig[c] != relevant) continue;
         const uint64_t b = s.birth[c];
         const uint64_t elapsed = mcs > b ? mcs - b : 0ull;
-        product = __dmul_rn(product, (double)((uint64_t)max_act > elapsed ? (uint64_t)max_act - elapsed : 0ull));
+        const uint64_t a = (uint64_t)max_act > elapsed ? (uint64_t)max_act - elapsed : 0ull;
+        if (a == 0) return 0.0;  // the product stays zero whatever follows (every factor is finite)
+        product = __dmul_rn(product, (double)a);
         count += 1;
     }
-    return pow(product, __ddiv_rn(1.0, (double)count));
+    return act_root(product, count);
 }
 
 // energy.rs:441-451: -(lambda_act / max_act) (GM_src - GM_tgt) of the
@@ -437,9 +450,24 @@ __device__ __forceinline__ bool accept_modes(const SimDesc& s, const SigT* sig, 
         nb += c == G;
     }
     if (na == 0) return false;
+    // dh <= 0 and na >= nb: both factors round to >= 1, so min(ratio, 1) = 1 > u
+    if (dh <= 0.0 && na >= nb) return true;
     const double ratio = __dmul_rn(__ddiv_rn((double)na, (double)nb), exp(-dh));
     return draw.u() < fmin(ratio, 1.0);
 }
+
+// The sweeps' decision under Metropolis acceptance with the Act term: the
+// Act delta first (exact FP64). When it is zero — both geometric means
+// vanish, the usual case since one retained site past its Max_Act MCS
+// zeroes a mean, or they are equal — the total dh + (+-0) decides as dh
+// alone, which decide_move's float bracket and FP64 fallback decide
+// exactly; otherwise the conservative part in FP64 plus the Act delta, in
+// the reference's order. Metropolis-Hastings acceptance: decide_modes.
+template <int NE, class SigT, class Draw>
+__device__ __forceinline__ bool decide_modes_sweep(const SimDesc& s, const SigT* sig, const uint16_t* adh_of,
+                                                   const uint32_t* volume, const uint32_t* interface, int64_t t,
+                                                   int64_t src, uint32_t L, uint32_t G, uint64_t mcs,
+                                                   const Draw& draw, int& dl, int& dg);
 
 // The decision of one attempt under the configured modes; `dh_total`
 // receives the delta-H the decision used (conservative + Act).
@@ -453,6 +481,23 @@ __device__ __forceinline__ bool decide_modes(const SimDesc& s, const SigT* sig, 
     dg = o.dg;
     dh_total = s.act ? __dadd_rn(o.dh, act_delta(s, sig, adh_of, t, src, L, G, mcs)) : o.dh;
     return accept_modes(s, sig, t, L, G, dh_total, draw);
+}
+
+template <int NE, class SigT, class Draw>
+__device__ __forceinline__ bool decide_modes_sweep(const SimDesc& s, const SigT* sig, const uint16_t* adh_of,
+                                                   const uint32_t* volume, const uint32_t* interface, int64_t t,
+                                                   int64_t src, uint32_t L, uint32_t G, uint64_t mcs,
+                                                   const Draw& draw, int& dl, int& dg) {
+    if (s.acceptance == 0 && s.act) {
+        const double act = act_delta(s, sig, adh_of, t, src, L, G, mcs);
+        if (act == 0.0) return decide_move<NE, SigT>(s, sig, adh_of, volume, interface, t, L, G, draw, dl, dg);
+        const DeltaOut o = delta_h<NE, SigT>(s, sig, adh_of, volume, interface, t, L, G);
+        dl = o.dl;
+        dg = o.dg;
+        return accept_modes(s, sig, t, L, G, __dadd_rn(o.dh, act), draw);
+    }
+    double dh_total = 0.0;
+    return decide_modes<NE, SigT, Draw>(s, sig, adh_of, volume, interface, t, src, L, G, mcs, draw, dl, dg, dh_total);
 }
 
 // ------------------------------------------------------------- commit ----

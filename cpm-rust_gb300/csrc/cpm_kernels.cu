@@ -218,10 +218,9 @@ __device__ void color_pass(const SimDesc& s, const PassInfo& p, uint64_t mcs, ui
                 ct.evaluated++;
                 int dl = 0, dg = 0;
                 const PhiloxDraw draw{s.seed, mcs, (uint32_t)t};
-                double dh_total = 0.0;
                 const bool acc = (s.acceptance || s.act)
-                                     ? decide_modes<NE>(s, sig, adh_of, volume, interface, t, t + s.copy_off[k], L, G, mcs,
-                                                        draw, dl, dg, dh_total)
+                                     ? decide_modes_sweep<NE>(s, sig, adh_of, volume, interface, t, t + s.copy_off[k], L,
+                                                              G, mcs, draw, dl, dg)
                                      : decide_move<NE, uint32_t>(s, sig, adh_of, volume, interface, t, L, G, draw, dl, dg);
                 if (acc) {
                     commit_move<D, uint32_t>(s, sig, volume, interface, s.sum_pos, s.sum_outer, x, L, G, dl, dg);
@@ -383,7 +382,12 @@ __global__ void evaluate_moves_kernel(const SimDesc* simp, int64_t n, const int6
                     double dh = 0.0;
                     o.accepted = decide_modes<NE>(s, s.sigma, s.adh_of, s.volume, s.interface, t, o.source_flat, o.losing,
                                                   o.gaining, s.mcs, GivenDraw{u[i]}, dl, dg, dh);
-                    o.accepted_sweep = o.accepted;
+                    // the sweeps' decision (decide_modes_sweep: the float
+                    // bracket when the Act delta is zero) on the same u
+                    int dl2 = 0, dg2 = 0;
+                    o.accepted_sweep = decide_modes_sweep<NE>(s, s.sigma, s.adh_of, s.volume, s.interface, t,
+                                                              o.source_flat, o.losing, o.gaining, s.mcs,
+                                                              GivenDraw{u[i]}, dl2, dg2);
                     o.delta_i_losing = dl;
                     o.delta_i_gaining = dg;
                     o.delta_h = dh;

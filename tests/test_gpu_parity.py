@@ -123,6 +123,62 @@ def test_sweep_decision_at_the_metropolis_threshold(name, cuda_required):
     assert checked > 1000
 
 
+# leaves of very different magnitude in one delta-H: adhesion energies of
+# order 1e6 whose sum cancels to order 1 beside volume/interface terms of
+# order 1e-6 (close calls: the float sum's rounding error is far larger than
+# the result, and the error bound must send every such decision to the FP64
+# fallback), and huge volume/interface couplings beside tiny adhesion
+MIXED = {
+    "mixed_huge_J_2d": lambda: Model((40, 40), "periodic", [("a", 40, 30, 1e-6, 3e-6), ("b", 40, 30, 2e-6, 1e-6)],
+                                     [[0, 1e6, 1e6 + 1.5], [1e6, 7e5, 1e6 - 0.25], [1e6 + 1.5, 1e6 - 0.25, 7e5]],
+                                     [10, 10], seed=42),
+    "mixed_huge_J_3d_26": lambda: Model((16, 16, 16), "periodic", [("a", 60, 90, 1e-6, 2e-6), ("b", 60, 90, 3e-6, 1e-6)],
+                                        [[0, 1e6, 1e6 + 0.75], [1e6, 6e5, 1e6 - 0.5],
+                                         [1e6 + 0.75, 1e6 - 0.5, 6e5 + 0.125]], [8, 8], energy="twenty_six", seed=43),
+    "mixed_huge_lambda_2d": lambda: Model((40, 40), "periodic", [("a", 40, 30, 1e6, 3e5), ("b", 41, 29, 1e6, 2.5e5)],
+                                          [[0, 1e-6, 2e-6], [1e-6, 3e-6, 5e-7], [2e-6, 5e-7, 1e-6]], [10, 10],
+                                          seed=41),
+}
+
+
+def test_sweep_decision_with_mixed_magnitudes(cuda_required):
+    """delta-H summed from terms of magnitude 1e6 and 1e-6 (either way
+    round): the sweeps' float decision with its FP64 fallback equals
+    `u < exp(-dh)` of the reference for random u and for u placed at
+    relative offsets 1e-12 ... 1e-3 from exp(-dh)."""
+    near_checked = 0
+    for name in sorted(MIXED):
+        model = MIXED[name]()
+        sim = model.oracle()
+        eng = _engine(model)
+        rng = np.random.default_rng(17)
+        for _ in range(3):
+            sim.run_mcs(5 if model.D == 2 else 2)
+            v, i, sp, so = padded_cells(sim)
+            eng.write_state(sim.padded(), v, i, sp, so)
+            t = random_interior_targets(sim, 20000, rng)
+            k = rng.integers(0, 2 * model.D, t.size)
+            u = rng.random(t.size)
+            got = eng.evaluate_moves(t, k, u)
+            want = sim.evaluate_moves(t, k, u)
+            _compare(got, want)
+            assert want["evaluated"].sum() > 100
+            # close calls wherever exp(-dh) is a normal double
+            up = np.flatnonzero((want["evaluated"] == 1) & (want["delta_h"] > 0) & (want["delta_h"] < 700))
+            up = up[:300]
+            if up.size == 0:
+                continue
+            tt = np.repeat(t[up], NEAR.size)
+            kk = np.repeat(k[up], NEAR.size)
+            e = np.exp(-np.repeat(want["delta_h"][up], NEAR.size))
+            uu = np.minimum(e * (1.0 + np.tile(NEAR, up.size)), 1 - 2.0**-53)
+            got = eng.evaluate_moves(tt, kk, uu)
+            want2 = sim.evaluate_moves(tt, kk, uu)
+            _compare(got, want2)
+            near_checked += tt.size
+    assert near_checked > 1000, near_checked
+
+
 def test_sweep_decision_for_zero_delta_h(cuda_required):
     """dh == 0 (the float bracket straddles zero) accepts for every u, up to
     the largest u below 1; small non-zero dh keep the reference's rule."""
