@@ -24,7 +24,7 @@ LIB = os.path.join(LIBDIR, "libcpm_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["cpm_kernels.cu", "cpm_resident.cu", "cpm_resident_modes.cu", "cpm_tiled.cu", "cpm_tiled_odd.cu",
-              "cpm_tiled_modes.cu", "cpm_tiled_modes_odd.cu",
+              "cpm_tiled_modes.cu", "cpm_tiled_modes_odd.cu", "cpm_init_device.cu",
               "cpm_noalloc.cu", "cpm_readout.cu"]
 CPP_SOURCES = ["cpm_config.cpp", "cpm_init.cpp", "cpm_engine.cpp", "cpm_serve.cpp", "cpm_capi.cpp"]
 

@@ -221,15 +221,12 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
         const Offs& o = offs[i];
         const size_t n1 = (size_t)L.n_cells + 1, nt = c.types.size();
         std::vector<uint32_t> padded = pad_lattice(L.g, initials[i].lattice);
-        Derived dv = derive(c, L.g, padded, L.n_cells);
         std::memcpy(stage.data() + o.sigma, padded.data(), padded.size() * 4);
         std::vector<uint16_t> adh(n1, 0);
         for (size_t id = 1; id < n1; ++id) adh[id] = (uint16_t)(initials[i].type_of[id - 1] + 1);
         std::memcpy(stage.data() + o.adh, adh.data(), n1 * 2);
-        std::memcpy(stage.data() + o.vol, dv.volume.data(), n1 * 4);
-        std::memcpy(stage.data() + o.itf, dv.interface.data(), n1 * 4);
-        std::memcpy(stage.data() + o.sp, dv.sum_pos.data(), dv.sum_pos.size() * 8);
-        std::memcpy(stage.data() + o.so, dv.sum_outer.data(), dv.sum_outer.size() * 8);
+        // V, I and the position sums stay zero here: launch_derive computes
+        // them on the device from the uploaded lattice
         std::memset(stage.data() + o.slots, 0xFF, n1 * 8);
         std::vector<double> J((nt + 1) * (nt + 1));
         for (size_t a = 0; a <= nt; ++a)
@@ -397,6 +394,12 @@ std::string DeviceSims::create(const std::vector<Config>& configs, const std::ve
     h2d_bytes_ += in_bytes + N * sizeof(SimDesc);
     CUDA_TRY(cudaMemcpyAsync(arena_, stage.data(), in_bytes, cudaMemcpyHostToDevice, stream_));
     CUDA_TRY(cudaMemcpyAsync(d_descs_, descs_.data(), N * sizeof(SimDesc), cudaMemcpyHostToDevice, stream_));
+    // the derived state of every fresh lattice (initialization.rs:396-436)
+    {
+        int64_t max_sites = 1;
+        for (const SimLayout& L : layouts_) max_sites = std::max<int64_t>(max_sites, L.g.n_sites);
+        CUDA_TRY(cpmgpu::launch_derive(d_descs_, (int)N, max_sites, stream_));
+    }
     CUDA_TRY(cudaStreamSynchronize(stream_));
     return "";
 }

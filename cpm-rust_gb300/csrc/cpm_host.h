@@ -95,12 +95,8 @@ struct Geometry {
     int64_t flat(const int64_t* x) const;
 };
 std::vector<uint32_t> pad_lattice(const Geometry& g, const std::vector<uint32_t>& interior);
-// Derived per-cell state of a fresh placement (initialization.rs:396-436).
-struct Derived {
-    std::vector<uint32_t> volume, interface;  // per id (n+1)
-    std::vector<int64_t> sum_pos, sum_outer;  // per id * D, per id * D * D
-};
-Derived derive(const Config& c, const Geometry& g, const std::vector<uint32_t>& padded, int n_cells);
+// (The derived per-cell state of a fresh placement, initialization.rs:396-436,
+// is computed on the device: cpmgpu::launch_derive.)
 
 // 2D simple-point table (simple_point.rs:288-306) and the FastChecker
 // adjacency masks the device uses to generate the 3D table.

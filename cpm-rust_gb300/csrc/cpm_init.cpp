@@ -1,23 +1,30 @@
-// Initial placement and the derived state of a fresh lattice (host side).
+// Initial placement of a fresh lattice (host side).
 //
 // Reproduces the reference's placement bit for bit, including its random
 // stream, so a GPU run starts from exactly the lattice the reference would
 // start from for the same seed:
-//   * explicit placement and its validation (initialization.rs:61-137);
+//   * explicit placement and its validation (initialization.rs:61-137); the
+//     lattice questions (id range, zero volume, connectivity) of a large
+//     lattice are answered on the device (cpm_init_device.cu);
 //   * default scatter-and-grow (initialization.rs:202-277), drawing from
 //     Xoshiro256++ seeded through SplitMix64 (rand_xoshiro 0.6,
 //     `seed_from_u64`) with rand 0.8's `gen_range` (widening multiply with
-//     the `(range << lz) - 1` acceptance zone);
-//   * interface, position sums and the gyration accumulator of the placed
-//     lattice (initialization.rs:396-436).
+//     the `(range << lz) - 1` acceptance zone): one sequential random
+//     stream, so it stays on the host.
+// The interface, position sums and gyration accumulator of the placed
+// lattice (initialization.rs:396-436) are summed on the device after the
+// upload (cpmgpu::launch_derive).
 // Growth reads only canonical interior sites, so the halo is not maintained
 // here; the device lattice gets its halo when it is padded for upload.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdint>
+#include <cstdlib>
 #include <cstring>
 
 #include "cpm_host.h"
+#include "cpm_kernels.h"
 
 namespace cpmhost {
 
@@ -96,36 +103,6 @@ std::vector<uint32_t> pad_lattice(const Geometry& g, const std::vector<uint32_t>
         p[f] = in[q];
     }
     return p;
-}
-
-Derived derive(const Config& c, const Geometry& g, const std::vector<uint32_t>& padded, int n_cells) {
-    const int D = c.D;
-    Derived out;
-    out.volume.assign(n_cells + 1, 0);
-    out.interface.assign(n_cells + 1, 0);
-    out.sum_pos.assign((size_t)(n_cells + 1) * D, 0);
-    out.sum_outer.assign((size_t)(n_cells + 1) * D * D, 0);
-    std::vector<int64_t> eoff;
-    for (auto& o : stencil(c.energy_nbh, D)) {
-        int64_t d = 0;
-        for (int a = 0; a < D; ++a) d += o[a] * g.strides[a];
-        eoff.push_back(d);
-    }
-    int64_t x[3] = {0, 0, 0};
-    for (int64_t i = 0; i < g.n_sites; ++i) {
-        const int64_t f = g.flat(x);
-        const uint32_t cell = padded[f];
-        if (cell) {
-            out.volume[cell] += 1;
-            for (int d = 0; d < D; ++d) {
-                out.sum_pos[(size_t)cell * D + d] += x[d];
-                for (int e = 0; e < D; ++e) out.sum_outer[((size_t)cell * D + d) * D + e] += x[d] * x[e];
-            }
-            for (int64_t off : eoff) out.interface[cell] += padded[f + off] != cell;
-        }
-        for (int d = D - 1; d >= 0; --d) { if (++x[d] < g.dims[d]) break; x[d] = 0; }
-    }
-    return out;
 }
 
 namespace {
@@ -223,9 +200,27 @@ struct Placer {
 };
 }  // namespace
 
+// Explicit lattices of at least this many sites are checked on the device
+// when the process has one (CPM_GPU_INIT_DEVICE_MIN_SITES overrides the
+// default of 65,536; "0" sends every explicit lattice there); smaller ones,
+// and every lattice in a process without a GPU, here. Both give the same
+// verdict and message.
+static int64_t device_check_min_sites() {
+    static const bool has_device = [] {
+        int count = 0;
+        if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) {
+            cudaGetLastError();
+            return false;
+        }
+        return true;
+    }();
+    if (!has_device) return INT64_MAX;
+    const char* e = std::getenv("CPM_GPU_INIT_DEVICE_MIN_SITES");
+    return e ? (int64_t)std::strtoll(e, nullptr, 10) : (int64_t)65536;
+}
+
 std::string initialize(const Config& c, Initial& out) {
-    Placer P(c);
-    const int64_t ns = P.g.n_sites;
+    const int64_t ns = n_sites(c);
     const int ntypes = (int)c.types.size();
     if (c.init_explicit) {
         out.used_default = false;
@@ -237,10 +232,29 @@ std::string initialize(const Config& c, Initial& out) {
             if (c.init_type_of[i] >= (uint64_t)ntypes)
                 return "cell " + std::to_string(i + 1) + " has type_index " + std::to_string(c.init_type_of[i]) +
                        ", but only " + std::to_string(ntypes) + " types are declared";
+        out.lattice = c.init_lattice;
+        out.type_of.assign(n, 0);
+        for (size_t i = 0; i < n; ++i) out.type_of[i] = (uint32_t)c.init_type_of[i];
+        const std::string not_connected =
+            " is not connected under connectivity_neighborhood — every explicitly-placed cell must already be connected";
+        if (ns >= device_check_min_sites() && n < 0xFFFFFFFFull) {
+            // the lattice questions on the device: one upload, a union-find
+            cpmgpu::ExplicitCheck ck;
+            const cudaError_t ce = cpmgpu::check_explicit_lattice(c.D, c.grid, c.periodic ? 1 : 0, c.init_lattice.data(),
+                                                                  ns, (uint32_t)n, &ck);
+            if (ce != cudaSuccess) return std::string("CUDA error: ") + cudaGetErrorString(ce);
+            if (ck.first_bad_site >= 0)
+                return "lattice references cell id " + std::to_string(c.init_lattice[ck.first_bad_site]) +
+                       ", but cell_type_of only covers " + std::to_string(n) + " cells";
+            if (ck.zero_volume_id) return "cell " + std::to_string(ck.zero_volume_id) + " has zero volume in the supplied lattice";
+            if (ck.disconnected_id) return "cell " + std::to_string(ck.disconnected_id) + not_connected;
+            return "";
+        }
         for (uint32_t id : c.init_lattice)
             if ((size_t)id > n)
                 return "lattice references cell id " + std::to_string(id) + ", but cell_type_of only covers " +
                        std::to_string(n) + " cells";
+        Placer P(c);
         std::vector<uint32_t> vol(n, 0);
         int64_t x[3] = {0, 0, 0};
         for (int64_t i = 0; i < ns; ++i) {
@@ -253,15 +267,11 @@ std::string initialize(const Config& c, Initial& out) {
             if (vol[i] == 0) return "cell " + std::to_string(i + 1) + " has zero volume in the supplied lattice";
         const std::vector<uint64_t> comp = P.first_component_sizes(n);
         for (size_t id = 1; id <= n; ++id)
-            if (comp[id] != vol[id - 1])
-                return "cell " + std::to_string(id) +
-                       " is not connected under connectivity_neighborhood — every explicitly-placed cell must already be connected";
-        out.lattice = c.init_lattice;
-        out.type_of.assign(n, 0);
-        for (size_t i = 0; i < n; ++i) out.type_of[i] = (uint32_t)c.init_type_of[i];
+            if (comp[id] != vol[id - 1]) return "cell " + std::to_string(id) + not_connected;
         return "";
     }
     // ---- scatter and grow ----
+    Placer P(c);
     out.used_default = true;
     std::vector<uint32_t> tcell;
     for (size_t t = 0; t < c.cell_counts.size(); ++t)

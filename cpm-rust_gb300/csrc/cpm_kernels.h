@@ -73,6 +73,23 @@ CPM_TILED_VARIANT_DECLS(odd)
 CPM_TILED_VARIANT_DECLS(modes_even)
 CPM_TILED_VARIANT_DECLS(modes_odd)
 #undef CPM_TILED_VARIANT_DECLS
+// Initial state on the device (cpm_init_device.cu). check_explicit_lattice
+// answers the lattice questions of explicit placement
+// (initialization.rs:61-137) for a row-major interior lattice: the first
+// site whose id exceeds n_cells (-1: none), the lowest cell id without a
+// site and the lowest cell id not connected under von Neumann adjacency
+// (0: none). Blocking; its own stream and stream-ordered scratch.
+struct ExplicitCheck {
+    int64_t first_bad_site;
+    uint32_t zero_volume_id;
+    uint32_t disconnected_id;
+};
+cudaError_t check_explicit_lattice(int D, const int64_t* dims, int periodic, const uint32_t* lattice, int64_t n_sites,
+                                   uint32_t n_cells, ExplicitCheck* out);
+// Volume, interface and position sums of every simulation of a set from its
+// padded lattice (initialization.rs:396-436); the per-cell arrays are zero on
+// entry. max_sites: the largest interior site count among them.
+cudaError_t launch_derive(const SimDesc* d_sims, int n_sims, int64_t max_sites, cudaStream_t st);
 // Copies one sample (V, I, position sums, optional lattice) of simulation d_sim.
 cudaError_t launch_sample(int D, const SimDesc* d_sim, int sample, int write_lattice, int64_t n_sites, cudaStream_t st);
 // Topology readouts of lattice snapshots (cpm_readout.cu). Work is cut into

@@ -624,7 +624,9 @@ class CPM:
         return bool(anyd.value), _results_from_handles([_P(out[i]) for i in range(len(rows))])
 
     def initial_state(self):
-        """Host-only placement (no device work): (lattice, cell_type_of, used_default)."""
+        """Placement without a simulation: (lattice, cell_type_of, used_default).
+        An explicit lattice of 65,536 sites or more (CPM_GPU_INIT_DEVICE_MIN_SITES)
+        is checked on the device when the process has one."""
         n_sites = int(np.prod(self._grid))
         lat = np.zeros(n_sites, dtype=np.uint32)
         # every cell holds at least one site, so n_sites bounds the cell count:
