@@ -555,22 +555,12 @@ std::string DeviceSims::run_tiled(const RunPlan& p, const uint64_t* t3) {
     }
     SimDesc* d_sim = d_descs_ + p.sim;
     unsigned long long* claims = descs_[p.sim].slots;
-    // the TMA row copies of box staging: the widest box row (tile + rim on
-    // the last axis) + 3 elements of 16-byte rounding, a multiple of 4
-    alignas(64) unsigned char rows_map[128];
-    const int last = L.g.D - 1;
-    const int bw_max = (int)((L.g.dims[last] + nt[last] - 1) / nt[last]) + 2;
-    int tma_w = ((bw_max + 3 + 3) / 4) * 4;
-    if (tma_w > 256 || cpmgpu::encode_rows_map(descs_[p.sim].sigma, L.g.n_padded, tma_w, rows_map) != cudaSuccess) {
-        cudaGetLastError();
-        tma_w = 0;  // per-site loads
-    }
     auto launch = [&](uint64_t m, int g) -> cudaError_t {
         cudaError_t e = cudaMemsetAsync(d_bar_, 0, 64, stream_);
         if (e == cudaSuccess)
             e = cpmgpu::launch_tiled(L.g.D, L.NE, odd, modes, d_sim, m, nt, d_bar_, claims, reg_smem ? nullptr : d_reg_, t3,
                                      max_box, tables_in_smem, barrier_extra, cl_cap, reg_smem, smem, g, stream_,
-                                     L.n_cells, tma_w ? rows_map : nullptr, tma_w);
+                                     L.n_cells);
         return e;
     };
     // trial launches of TRIAL_MCS each (3D MCS cost more: fewer)

@@ -55,15 +55,10 @@ int tiled_block();
 // `reg_smem`: each CTA's cell registry (stamps and box slots) in shared
 // memory; else `d_registry` holds it: 2 x grid x (n_cells + 1) words.
 cudaError_t tiled_occupancy(int D, int NE, int odd, int modes, size_t smem, int* per_sm);
-// `rows_map`: a CUtensorMap of the simulation's padded sigma as one row of
-// n_padded u32 with box width `tma_w` (a multiple of 4, at least the widest
-// box row + 3), for the TMA staging of box rows; null / 0: per-site loads.
 cudaError_t launch_tiled(int D, int NE, int odd, int modes, SimDesc* d_sim, uint64_t n_mcs, const int* nt,
                          void* d_barrier, unsigned long long* d_claims, uint32_t* d_registry, const uint64_t* d_t3,
                          int max_box, int tables_in_smem, int barrier_extra, int cl_cap, int reg_smem, size_t smem,
-                         int grid, cudaStream_t st, int n_cells, const void* rows_map, int tma_w);
-// The tensor map launch_tiled takes (driver entry point; no libcuda link).
-cudaError_t encode_rows_map(void* sigma, int64_t n_padded, int tma_w, void* map_out /* CUtensorMap */);
+                         int grid, cudaStream_t st, int n_cells);
 // The variants behind them (even site colouring / odd periodic sides, each
 // for the Metropolis chain and for the modes).
 #define CPM_TILED_VARIANT_DECLS(sfx)                                                                              \
@@ -72,8 +67,7 @@ cudaError_t encode_rows_map(void* sigma, int64_t n_padded, int tma_w, void* map_
     cudaError_t launch_tiled_##sfx(int D, int NE, SimDesc* d_sim, uint64_t n_mcs, const int* nt, void* d_barrier, \
                                    unsigned long long* d_claims, uint32_t* d_registry, const uint64_t* d_t3,      \
                                    int max_box, int tables_in_smem, int barrier_extra, int cl_cap, int reg_smem,  \
-                                   size_t smem, int grid, cudaStream_t st, int n_cells, const void* rows_map,     \
-                                   int tma_w);
+                                   size_t smem, int grid, cudaStream_t st, int n_cells);
 CPM_TILED_VARIANT_DECLS(even)
 CPM_TILED_VARIANT_DECLS(odd)
 CPM_TILED_VARIANT_DECLS(modes_even)

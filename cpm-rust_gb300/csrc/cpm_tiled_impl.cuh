@@ -27,11 +27,9 @@
 // counter/generation pair with a bounded spin that records a timeout and
 // returns instead of hanging.
 #include <cooperative_groups.h>
-#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include <cstring>
 #include <mutex>
 #include <type_traits>
 
@@ -85,56 +83,6 @@ __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
-}
-
-// ---- TMA staging of the box's sigma rows
-// The padded lattice is described to the tensor-memory accelerator as one
-// row of n_padded u32 (a rank-1 tensor map: the lattice's row pitch, L + 2
-// elements, is not a multiple of 16 bytes, which higher-rank maps need).
-// Each box row (all positions sharing the outer coordinates) is contiguous
-// in the padded lattice when the box does not cross the lattice end on the
-// last axis (the 1-site halo covers its rim); one 1D tensor copy per row
-// brings W elements from the row's first element rounded down to a 16-byte
-// boundary into a 128-byte aligned slot of shared memory, all rows
-// completing on one mbarrier.
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ void mbar_init(uint64_t* bar) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-__device__ __forceinline__ void mbar_expect(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t phase) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.b32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(phase)
-        : "memory");
-    return ok != 0u;
-}
-__device__ __forceinline__ void tma_row(void* dst, const CUtensorMap* map, int x, uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.1d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2}], [%3];" ::"r"(
-            smem_u32(dst)),
-        "l"((uint64_t)map), "r"(x), "r"(smem_u32(bar))
-        : "memory");
-}
-// Waits for the phase with a time limit (2 s); false when it ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
-    if (mbar_try(bar, phase)) return true;
-    unsigned long long t0 = 0;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
-    for (unsigned spins = 1;; ++spins) {
-        if (mbar_try(bar, phase)) return true;
-        if ((spins & 63u) == 0u) {
-            unsigned long long t;
-            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-            if (t - t0 > 2000000000ull) return false;
-        }
-    }
 }
 
 // Grid barrier: one release-add per CTA on a counter that only grows
@@ -770,8 +718,7 @@ template <int D, int NE, bool ODD, bool MODES>
 __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_mcs, TileGrid tg_in, BarrierState* bar,
                                                    unsigned long long* claims, const uint64_t* t3, int max_box,
                                                    int tables_in_smem, int barrier_extra, int cl_cap,
-                                                   int reg_smem, uint32_t* seen_all, uint32_t* slot_all,
-                                                   const __grid_constant__ CUtensorMap rows_map, int tma_w) {
+                                                   int reg_smem, uint32_t* seen_all, uint32_t* slot_all) {
     extern __shared__ __align__(16) unsigned char sm[];
     __shared__ SimDesc gsd, lsd;
     __shared__ int s_n, s_tile, s_ncell, s_box_dims[3], s_gx0[3], s_g0[3], s_tcnt[3];
@@ -783,12 +730,9 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
     __shared__ int s_ncls[3];
     __shared__ unsigned long long sstat[8];
     const int tid = threadIdx.x;
-    __shared__ __align__(8) uint64_t s_mbar;  // completion of the box rows' tensor copies
     if (tid == 0) gsd = *simp;
     if (tid < 8) sstat[tid] = 0;
-    if (tid == 0 && tma_w > 0) mbar_init(&s_mbar);
     __syncthreads();
-    uint32_t tma_phase = 0;
     // site colours per axis: the two parities, plus (ODD) the last
     // coordinate of an odd periodic axis as a third
     if (tid < 3) s_ncls[tid] = tid < D ? ((ODD && gsd.periodic && (gsd.dims[tid] & 1)) ? 3 : 2) : 1;
@@ -980,63 +924,20 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                 const uint32_t stamp = stamp_of(k) + salt;
                 int box = 1;
                 for (int d = 0; d < D; ++d) box *= s_box_dims[d];
-                // Box rows by tensor copies when the box does not cross the
-                // lattice end on the last axis and the slots fit the
-                // candidate storage (free while a box is staged); else one
-                // L2 load per site.
-                const int bw = s_box_dims[D - 1], rows = box / bw;
-                const int gi0 = s_g0[D - 1];  // padded index, last axis, of box position 0
-                const int pitch = ((tma_w * 4 + 127) / 128) * 32;  // slot of a row, in u32
-                uint32_t* stg = (uint32_t*)(((uintptr_t)(sm + ts.c_site) + 127) & ~(uintptr_t)127);
-                const bool tma = tma_w >= bw + 3 && gi0 + bw - 1 <= g.dims[D - 1] + 1 &&
-                                 (uintptr_t)(stg + (size_t)rows * pitch) <= (uintptr_t)(sm + ts.c_x2 + TCMAX * 2);
-                // padded index of box position (r, 0): outer coordinates through
-                // the periodic wrap (or a fixed lattice's halo), the last axis
-                // through the halo
-                auto row_start = [&](int r) -> int {
-                    int f = gi0 * (int)g.strides[D - 1];
-                    for (int d = D - 2; d >= 0; --d) {
-                        const int y = r % s_box_dims[d];
-                        r /= s_box_dims[d];
-                        f += (P.gcoord(d, y) + 1) * (int)g.strides[d];
-                    }
-                    return f;
-                };
-                auto staged_id = [&](int q) -> uint32_t {
-                    const int r = q / bw;
-                    return stg[r * pitch + (row_start(r) & 3) + (q - r * bw)];
-                };
-                if (tma) {
-                    // generic accesses before the async proxy's: the slots
-                    // (the last pass's candidates) it overwrites, and the
-                    // lattice the other CTAs wrote before the grid barrier
-                    asm volatile("fence.proxy.async;" ::: "memory");
-                    __syncthreads();
-                    if (tid == 0) mbar_expect(&s_mbar, (uint32_t)(rows * tma_w * 4));
-                    __syncthreads();
-                    for (int r = tid; r < rows; r += TB) tma_row(stg + r * pitch, &rows_map, row_start(r) & ~3, &s_mbar);
-                    if (!mbar_wait(&s_mbar, tma_phase)) {
-                        // record the timeout (every CTA leaves at the next grid
-                        // barrier) and give the copies in flight one more limit
-                        atomicExch(&bar->error, 1);
-                        mbar_wait(&s_mbar, tma_phase);
-                    }
-                    tma_phase ^= 1u;
-                }
                 // four sites per thread in flight: their sigma loads first, then the rest
                 // the loop bound is uniform across the block: every lane reaches
                 // the warp-wide match below, lanes past the box with id 0
                 for (int base = 0; base < box; base += 4 * TB) {
                     const int q0 = base + tid;
+                    int gfs[4];
                     uint32_t ids[4];
 #pragma unroll
                     for (int u = 0; u < 4; ++u) {
                         const int q = q0 + u * TB;
                         int xg[3];
                         // a fixed lattice's rim outside the box maps to its medium halo
-                        if (q >= box) ids[u] = 0u;
-                        else if (tma) ids[u] = staged_id(q);
-                        else ids[u] = __ldcg(g.sigma + P.gflat_of_box(q, xg));
+                        gfs[u] = q < box ? P.gflat_of_box(q, xg) : 0;
+                        ids[u] = q < box ? __ldcg(g.sigma + gfs[u]) : 0u;
                     }
 #pragma unroll
                     for (int u = 0; u < 4; ++u) {
@@ -1048,7 +949,7 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                         const unsigned peers = __match_any_sync(0xffffffffu, id);
                         const bool leader = (int)(threadIdx.x & 31) == __ffs(peers) - 1;
                         if (!valid) continue;
-                        if (!tma) sid[q] = id;  // (with tma the ids stay in their slots)
+                        sid[q] = id;
                         if (id && leader && reg_first(id, stamp)) {
                             if (claim) atomicMin(claims + id, key);
                             const int k1 = atomicAdd(&s_ncell, 1);
@@ -1075,7 +976,7 @@ __global__ void __launch_bounds__(TB, 1) tiled_kernel(SimDesc* simp, uint64_t n_
                 }
 #pragma unroll 4
                 for (int q = tid; q < box; q += TB) {
-                    const uint32_t id = tma ? staged_id(q) : sid[q];
+                    const uint32_t id = sid[q];
                     P.sig[q] = id ? (uint16_t)reg_get(id) : (uint16_t)0;
                 }
                 const int nc = s_ncell;
@@ -1544,13 +1445,7 @@ cudaError_t TILED_VARIANT(launch_tiled)(int D, int NE, SimDesc* d_sim, uint64_t 
                                         void* d_barrier, unsigned long long* d_claims, uint32_t* d_registry,
                                         const uint64_t* d_t3, int max_box, int tables_in_smem, int barrier_extra,
                                         int cl_cap, int reg_smem, size_t smem, int grid, cudaStream_t st,
-                                        int n_cells, const void* rows_map, int tma_w) {
-    CUtensorMap map;
-    if (rows_map && tma_w > 0) map = *(const CUtensorMap*)rows_map;
-    else {
-        std::memset(&map, 0, sizeof map);
-        tma_w = 0;
-    }
+                                        int n_cells) {
     TileGrid tg;
     for (int d = 0; d < 3; ++d) { tg.nt[d] = d < D ? nt[d] : 1; tg.off[d] = 0; }
     tg.colors = 1 << D;
@@ -1565,7 +1460,7 @@ cudaError_t TILED_VARIANT(launch_tiled)(int D, int NE, SimDesc* d_sim, uint64_t 
         if (e != cudaSuccess) return e;                                                                     \
         void* args[] = {(void*)&d_sim, (void*)&n_mcs, (void*)&tg, (void*)&bar, (void*)&d_claims, (void*)&d_t3, \
                         (void*)&max_box, (void*)&tables_in_smem, (void*)&barrier_extra, (void*)&cl_cap,    \
-                        (void*)&reg_smem, (void*)&seen_all, (void*)&slot_all, (void*)&map, (void*)&tma_w};  \
+                        (void*)&reg_smem, (void*)&seen_all, (void*)&slot_all};                              \
         return cudaLaunchCooperativeKernel((const void*)k, dim3(grid), dim3(TB), args, smem, st);            \
     }
     switch (tiled_index(D, NE)) {
@@ -1605,35 +1500,6 @@ bool tiled_plan(int D, const int* dims, int periodic, int* nt, int* max_box) {
     return box <= TMAX_BOX && box <= 65535 && klass <= TCMAX;
 }
 
-cudaError_t encode_rows_map(void* sigma, int64_t n_padded, int tma_w, void* map_out) {
-    using Encode = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-    static Encode encode = nullptr;
-    static std::once_flag once;
-    std::call_once(once, [] {
-        void* fp = nullptr;
-        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fp, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            encode = (Encode)fp;
-        cudaGetLastError();
-    });
-    if (!encode) return cudaErrorNotSupported;
-    if (n_padded <= 0 || n_padded > ((int64_t)1 << 32) || tma_w < 4 || tma_w > 256 || (tma_w & 3) ||
-        ((uintptr_t)sigma & 15))
-        return cudaErrorInvalidValue;
-    const cuuint64_t dim[1] = {(cuuint64_t)n_padded};
-    const cuuint64_t stride[1] = {(cuuint64_t)n_padded * 4};  // unused for rank 1
-    const cuuint32_t box[1] = {(cuuint32_t)tma_w};
-    const cuuint32_t step[1] = {1};
-    const CUresult r = encode((CUtensorMap*)map_out, CU_TENSOR_MAP_DATA_TYPE_UINT32, 1, sigma, dim, stride, box, step,
-                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
-                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
-}
-
 size_t tiled_smem_bytes(int max_box, int n_cells, int cl_cap, int D, int reg_smem) {
     return tile_shared(max_box, n_cells, cl_cap, D, reg_smem != 0).total;
 }
@@ -1655,11 +1521,11 @@ cudaError_t tiled_occupancy(int D, int NE, int odd, int modes, size_t smem, int*
 cudaError_t launch_tiled(int D, int NE, int odd, int modes, SimDesc* d_sim, uint64_t n_mcs, const int* nt,
                          void* d_barrier, unsigned long long* d_claims, uint32_t* d_registry, const uint64_t* d_t3,
                          int max_box, int tables_in_smem, int barrier_extra, int cl_cap, int reg_smem, size_t smem,
-                         int grid, cudaStream_t st, int n_cells, const void* rows_map, int tma_w) {
+                         int grid, cudaStream_t st, int n_cells) {
     auto* fn = modes ? (odd ? launch_tiled_modes_odd : launch_tiled_modes_even)
                      : (odd ? launch_tiled_odd : launch_tiled_even);
     return fn(D, NE, d_sim, n_mcs, nt, d_barrier, d_claims, d_registry, d_t3, max_box, tables_in_smem, barrier_extra,
-              cl_cap, reg_smem, smem, grid, st, n_cells, rows_map, tma_w);
+              cl_cap, reg_smem, smem, grid, st, n_cells);
 }
 #endif
 
