@@ -370,6 +370,10 @@ TILED_MODELS = {
     "tiled_3d_odd_periodic": lambda: Model((33, 31, 35), "periodic", [("a", 60, 90, 2.0, 0.5), ("b", 60, 90, 2.0, 0.5)],
                                            [[0, 16, 16], [16, 4, 9], [16, 9, 5]], [30, 30], energy="twenty_six",
                                            seed=19),
+    # the headline shapes at full size: the 512x512 sorting lattice (24x24
+    # tiles, 4196 cells) and a 96^3 organoid (10^3 tiles)
+    "tiled_2d_512_sorting": lambda: sorting_model(side=512, seed=22),
+    "tiled_3d_96_organoid": lambda: organoid_model(side=96, counts=(400, 400), vol=100, seed=23),
 }
 
 
