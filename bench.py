@@ -243,6 +243,7 @@ def run_batch_bench(args):
         loop_t.append(time.perf_counter() - t0)
     loop_sims_s = len(loop_t) / sum(loop_t)
     batch_sims_s = args.batch_n / t_batch
+    cpu = batch_cpu_baseline(sides, thetas, seeds, burn, readout, args) if not args.no_cpu else None
     return {
         "workload": f"{args.batch_n} thetas, 2 types (V*=50, I*=75), side uniform in {list(BATCH_SIDES)}, phi=0.7, "
                     f"Moore energy, periodic; {burn} burn-in + {readout} readout MCS, sampling every {interval}",
@@ -257,7 +258,51 @@ def run_batch_bench(args):
                           "device": split["device_us"], "readouts": split["host_read_us"],
                           "python_side": t_batch - sum(split.values())},
         "timed": "cpm.run_many(...) end to end: host placement, upload, one persistent launch, readouts",
+        "cpu_baseline": cpu,
     }
+
+
+def batch_cpu_baseline(sides, thetas, seeds, burn, readout, args):
+    """The batch on the host cores, one simulation per core (the reference's
+    rayon par_iter over thetas, batch.rs:126-152): the oracle port runs the
+    first thetas of the workload, each its whole window, on a thread pool
+    as wide as the host; sims/s over the wall time."""
+    import concurrent.futures as cf
+    import warnings
+
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    import cpm
+
+    O.build()
+    cores = os.cpu_count() or 1
+    n = min(len(thetas), args.batch_cpu_n)
+
+    def one(i):
+        th, side = thetas[i], sides[i]
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            per = cpm.cells_for_density((side, side), 50, 0.35)
+        j = th[4:10]
+        adh = [[j[0], j[1], j[2]], [j[1], j[3], j[4]], [j[2], j[4], j[5]]]
+        spec = O.ModelSpec((side, side), True, [(50, 75, th[0], th[2]), (50, 75, th[1], th[3])], adh,
+                           cell_counts=[per, per])
+        failed, *_ = O.run_many(spec, np.array([seeds[i]], dtype=np.uint64), burn_in=burn, readout=readout,
+                                threads=1, local_halo=True)
+        assert failed == 0
+        return side * side * (burn + readout)
+
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=cores) as ex:
+        attempts = sum(ex.map(one, range(n)))
+    dt = time.perf_counter() - t0
+    return {"sims_per_s": n / dt, "attempts_per_s": attempts / dt, "cores": cores, "kind": "port",
+            "cpu_model": cpu_model(),
+            "sample": f"the first {n} thetas of the workload, each its whole {burn} + {readout} MCS window, "
+                      f"one per host thread ({cores} threads)"}
 
 
 # ------------------------------------------------ serving workload (C5) ----
@@ -820,8 +865,20 @@ def cpu_baseline(args):
     sim.run_mcs(args.cpu_mcs)
     dt = time.perf_counter() - t0
     att = args.cpu_mcs * GRID[0] * GRID[1]
+    # the reference's own halo rule: the whole periodic halo refreshed after
+    # every accepted move on a boundary site (dynamics.rs:206-224); the same
+    # trajectory
+    full = O.OracleSim(oracle_spec(), SEED)
+    full.set_local_halo(False)
+    full.init_default()
+    mf = max(1, args.cpu_mcs // 4)
+    t1 = time.perf_counter()
+    full.run_mcs(mf)
+    df = time.perf_counter() - t1
     return {"value": att / dt, "unit": "attempts/s", "cores": 1, "kind": "port", "cpu_model": cpu_model(),
-            "sample": f"{args.cpu_mcs} MCS of the same 512x512 lattice from the same placement, one thread"}
+            "sample": f"{args.cpu_mcs} MCS of the same 512x512 lattice from the same placement, one thread",
+            "whole_halo_refresh_value": mf * GRID[0] * GRID[1] / df,
+            "whole_halo_refresh_sample": f"{mf} MCS, the reference's whole-halo refresh on boundary accepts"}
 
 
 def run_gpu(args, rank, world, dist):
@@ -978,6 +1035,7 @@ def main():
     ap.add_argument("--ref-mcs", type=int, default=200, help="MCS per host thread and step of the reference arm")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--batch-n", type=int, default=4096, help="thetas of the batch workload (0 skips it)")
+    ap.add_argument("--batch-cpu-n", type=int, default=32, help="thetas of the batch's CPU baseline (all host cores)")
     ap.add_argument("--batch-mcs", type=lambda v: tuple(int(x) for x in v.split(",")), default=(2000, 2000, 100),
                     help="burn-in,readout,interval MCS of each batch member")
     ap.add_argument("--c3-mcs", type=int, default=100, help="timed MCS of the 3D organoid case (0 skips it)")
