@@ -62,6 +62,31 @@ def test_explicit_placement_errors_match_reference():
         m.builder(lattice=np.zeros(10, np.uint32), cell_type_of=[0]).initial_state()
 
 
+def test_explicit_placement_errors_on_a_large_lattice_without_a_gpu():
+    """Explicit lattices of 65,536 sites or more are checked on the device
+    when the process has one, else on the host (as here, without a GPU);
+    either way the reference's messages in its order (range, zero volume,
+    connectivity; tests/test_gpu_init.py compares the two paths)."""
+    m = Model((256, 256), "periodic", [("a", 50, 75, 10.0, 2.0)], [[0, 5], [5, 2]], [3])
+    lat = np.zeros((256, 256), dtype=np.uint32)
+    lat[10:14, 10:14] = 1
+    lat[100:104, 100:104] = 2
+    lat[200, 200] = 2  # cell 2 split
+    lat[0:3, 250:256] = 3
+    lat[0:3, 0:2] = 3  # cell 3 joined across the periodic edge
+    with pytest.raises(ValueError, match="^cell 2 is not connected under connectivity_neighborhood"):
+        m.builder(lattice=lat, cell_type_of=[0, 0, 0]).initial_state()
+    lat[200, 200] = 0
+    lat2, cto, used = m.builder(lattice=lat, cell_type_of=[0, 0, 0]).initial_state()
+    assert not used and np.array_equal(lat2, lat)
+    lat[100:104, 100:104] = 0
+    with pytest.raises(ValueError, match="^cell 2 has zero volume in the supplied lattice$"):
+        m.builder(lattice=lat, cell_type_of=[0, 0, 0]).initial_state()
+    lat[255, 255] = 7
+    with pytest.raises(ValueError, match="^lattice references cell id 7, but cell_type_of only covers 3 cells$"):
+        m.builder(lattice=lat, cell_type_of=[0, 0, 0]).initial_state()
+
+
 def test_crowded_scatter_reports_reference_error():
     m = Model((10, 10), "periodic", [("a", 50, 75, 1.0, 1.0)], [[0, 1], [1, 1]], [20])
     with pytest.raises(ValueError, match="could not place all 20 seed points"):
