@@ -232,9 +232,13 @@ std::string initialize(const Config& c, Initial& out) {
             if (c.init_type_of[i] >= (uint64_t)ntypes)
                 return "cell " + std::to_string(i + 1) + " has type_index " + std::to_string(c.init_type_of[i]) +
                        ", but only " + std::to_string(ntypes) + " types are declared";
-        out.lattice = c.init_lattice;
-        out.type_of.assign(n, 0);
-        for (size_t i = 0; i < n; ++i) out.type_of[i] = (uint32_t)c.init_type_of[i];
+        // the placement, once every check has passed
+        auto accept = [&]() -> std::string {
+            out.lattice = c.init_lattice;
+            out.type_of.assign(n, 0);
+            for (size_t i = 0; i < n; ++i) out.type_of[i] = (uint32_t)c.init_type_of[i];
+            return "";
+        };
         const std::string not_connected =
             " is not connected under connectivity_neighborhood — every explicitly-placed cell must already be connected";
         if (ns >= device_check_min_sites() && n < 0xFFFFFFFFull) {
@@ -248,7 +252,7 @@ std::string initialize(const Config& c, Initial& out) {
                        ", but cell_type_of only covers " + std::to_string(n) + " cells";
             if (ck.zero_volume_id) return "cell " + std::to_string(ck.zero_volume_id) + " has zero volume in the supplied lattice";
             if (ck.disconnected_id) return "cell " + std::to_string(ck.disconnected_id) + not_connected;
-            return "";
+            return accept();
         }
         for (uint32_t id : c.init_lattice)
             if ((size_t)id > n)
@@ -268,7 +272,7 @@ std::string initialize(const Config& c, Initial& out) {
         const std::vector<uint64_t> comp = P.first_component_sizes(n);
         for (size_t id = 1; id <= n; ++id)
             if (comp[id] != vol[id - 1]) return "cell " + std::to_string(id) + not_connected;
-        return "";
+        return accept();
     }
     // ---- scatter and grow ----
     Placer P(c);
