@@ -869,8 +869,12 @@ def cpu_baseline(args):
     # every accepted move on a boundary site (dynamics.rs:206-224); the same
     # trajectory
     full = O.OracleSim(oracle_spec(), SEED)
-    full.set_local_halo(False)
+    # placed with the local refresh (the placement is the same either way;
+    # the reference's whole-halo rule during the growth makes it O(N^2)),
+    # then swept with the whole-halo rule
+    full.set_local_halo(True)
     full.init_default()
+    full.set_local_halo(False)
     mf = max(1, args.cpu_mcs // 4)
     t1 = time.perf_counter()
     full.run_mcs(mf)
