@@ -1,4 +1,4 @@
-"""Distributional parity (spec bar (d)): summary statistics of the GPU
+"""Distributional parity: summary statistics of the GPU
 chain over 256 seeds against the oracle's over the same 256 seeds.
 
 The GPU chain is a checkerboard colour-pass chain with exact per-cell

@@ -1,11 +1,11 @@
 """Per-move and bookkeeping parity of the GB300 kernels against the oracle.
 
-Spec bar (a)/(b): for any lattice state and proposed move, the
-connectivity verdict, the volume guard, the integer interface deltas and the
-FP64 Delta-H bits are identical to the reference's (oracle: restated
+Per move: for any lattice state and proposed move, the connectivity
+verdict, the volume guard, the integer interface deltas and the FP64
+Delta-H bits are identical to the reference's (oracle: restated
 crates/cpm-core/src/monte_carlo.rs:52-145, connectivity.rs:42-65,
-energy.rs:92-264). Bar (c): the device's incremental V/I always equal a full
-recount. All compare through the C ABI (libcpm_gpu.so).
+energy.rs:92-264). Exact state: the device's incremental V/I always equal a
+full recount. All compare through the C ABI (libcpm_gpu.so).
 """
 
 import numpy as np
